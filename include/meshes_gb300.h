@@ -1,0 +1,146 @@
+/* meshes_gb300.h - C ABI of the GB300 mesh-propagation library (libmeshes_gb300.so).
+ *
+ * Plain C: raw device pointers, sizes and a cudaStream_t (passed as void*).  Every entry point is
+ * asynchronous on `stream`, returns 0 on success and a negative MG_E* code when an argument is
+ * rejected before anything is launched; mg_last_error() then names the problem.  Kernels record
+ * run-time faults (a malformed geometry array, a wait that ran past its time limit) in the status
+ * word at the start of the workspace; mg_read_status() fetches it.
+ *
+ * Fields follow the reference GPU API (gpu/mesh.py:147-174): B vectors of N modes, vector b at
+ * u + b*ldu (the reference's (N, B) Fortran-order arrays); complex64 (float2) for the mzi and sym
+ * crossings, float32 for orth.  Parameters follow the reference grid (gpu/mesh.py:77-81):
+ * p[l*ldp + q*n_p + k] for layer l < L, slot q < N/2 and k < n_p (mzi/sym: n_p = 2 (theta, phi),
+ * orth: n_p = 1); splitter errors s[l*lds + q*n_s + k] (mzi: n_s = 2 (alpha, beta), sym: 1) or NULL
+ * for ideal splitters.  Geometry arrays are device int32 arrays of length L: lens/shifts for
+ * nearest-neighbour meshes (Clements, Reck, ...), strides (log2 of the stride) for butterfly meshes.
+ *
+ * Limits: N even, 2 <= N <= 512; ldu >= N and even; u pointers 16-byte aligned (complex) or 8-byte
+ * aligned (real).
+ */
+#ifndef MESHES_GB300_H
+#define MESHES_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* crossings (gpu/mesh.py:66-73) */
+#define MG_MZI 0
+#define MG_SYM 1
+#define MG_ORTH 2
+#define MG_GENERIC 3
+
+/* operations and geometries */
+#define MG_OP_FWD 0
+#define MG_OP_FWDDIFF 1
+#define MG_OP_BWD 2
+#define MG_GEO_NN 0
+#define MG_GEO_FFT 1
+
+/* return codes */
+#define MG_OK 0
+#define MG_E_ARG (-1)         /* invalid argument (see mg_last_error) */
+#define MG_E_WORKSPACE (-2)   /* workspace missing or too small */
+#define MG_E_CUDA (-3)        /* a CUDA runtime call failed */
+#define MG_E_CONFIG (-4)      /* no kernel instantiated for the requested tile configuration */
+
+/* run-time status codes (mg_read_status) */
+#define MG_ST_OK 0
+#define MG_ST_TIMEOUT 1       /* a shared-memory pipeline wait ran past its time limit */
+#define MG_ST_BAD_GEOMETRY 2  /* lens/shifts/strides place MZIs outside the N modes */
+#define MG_ST_BAD_WORK 3      /* batched launch: malformed work item */
+
+/* Tile configuration of one launch: modes per lane M (2..16), vectors per lane V, warps per CTA W,
+ * layers per pipeline stage CL, pipeline stages S.  Zero fields are filled by the built-in
+ * heuristic; the autotuner (meshes_gb300/autotune.py) measures and stores better choices. */
+typedef struct mg_config {
+  int M, V, W, CL, S;
+} mg_config;
+
+/* ---- library ---------------------------------------------------------------------------- */
+
+/* Last argument error of the calling thread (empty string if none). */
+const char* mg_last_error(void);
+
+/* Library version string. */
+const char* mg_version(void);
+
+/* Bytes of workspace an entry point needs for (op, N, L, B, crossing, geometry) with config cfg
+ * (NULL = heuristic).  The workspace is caller-allocated device memory, 256-byte aligned; its first
+ * 256 bytes hold the status word. */
+size_t mg_workspace_bytes(int op, int N, int L, int B, int crossing, int geometry, const mg_config* cfg);
+
+/* Zero the status word of a freshly allocated workspace. */
+int mg_workspace_init(void* workspace, size_t workspace_bytes, void* stream);
+
+/* Synchronise `stream`, return the workspace's status word (MG_ST_*), clear it if `clear`. */
+int mg_read_status(void* workspace, int clear, void* stream);
+
+/* The configuration the heuristic picks (filled into *out). */
+int mg_default_config(int op, int N, int B, int crossing, mg_config* out);
+
+/* ---- reference-shaped entry points ---------------------------------------------------------
+ * Each replaces one CuPy RawKernel launch of the reference: coefficient precompute and the
+ * propagation kernel run back to back on `stream`. */
+
+/* Forward propagation u_out = U u_in.  Replaces fwdprop_N{N}_{X} (gpu/fwdprop.cu:25-27, launched at
+ * gpu/mesh.py:158-164).  u_in == u_out is allowed. */
+int mg_fwdprop(int N, int L, int B, const int* lens, const int* shifts, const float* p, int ldp, const float* s,
+               int lds, const void* u_in, void* u_out, int ldu, int crossing, void* workspace,
+               size_t workspace_bytes, void* stream);
+
+/* Same for butterfly meshes: replaces fwdprop_ft_N{N}_{X} (gpu/fwdprop.cu with FFT=1, gpu/mzi_ft.cu:15-47). */
+int mg_fwdprop_ft(int N, int L, int B, const int* strides, const float* p, int ldp, const float* s, int lds,
+                  const void* u_in, void* u_out, int ldu, int crossing, void* workspace, size_t workspace_bytes,
+                  void* stream);
+
+/* Forward-mode derivative along dp: (u_out, du_out) = (U u_in, dU u_in + U du_in); du_in may be NULL
+ * (zero).  Replaces fwddiff_N{N}_{X} (gpu/fwddiff.cu:24-27, launched at gpu/mesh.py:166-174). */
+int mg_fwddiff(int N, int L, int B, const int* lens, const int* shifts, const float* p, const float* dp, int ldp,
+               const float* s, int lds, const void* u_in, const void* du_in, void* u_out, void* du_out, int ldu,
+               int crossing, void* workspace, size_t workspace_bytes, void* stream);
+int mg_fwddiff_ft(int N, int L, int B, const int* strides, const float* p, const float* dp, int ldp, const float* s,
+                  int lds, const void* u_in, const void* du_in, void* u_out, void* du_out, int ldu, int crossing,
+                  void* workspace, size_t workspace_bytes, void* stream);
+
+/* Back-propagation from the outputs: given u_out and dJdu_out (= 2 dJ/du_out*, the reference's
+ * convention, gpu/mesh.py:176-181), reconstruct u_in (may be NULL), write dJdu_in = U^H dJdu_out and
+ * dp = dJ/dp in the parameter grid layout.  accumulate = 0 overwrites dp (deterministic; inactive
+ * slots get 0), accumulate = 1 adds to it as the reference's atomics do (the reference zeroes dp
+ * first, gpu/mesh.py:214).  Replaces backdiff_N{N}_{X} (gpu/backdiff.cu:24-27, launched at
+ * gpu/mesh.py:227-231).  Valid for unitary crossings (mzi, sym, orth). */
+int mg_backdiff(int N, int L, int B, const int* lens, const int* shifts, const float* p, float* dp, int ldp,
+                const float* s, int lds, const void* u_out, const void* dJdu_out, void* u_in, void* dJdu_in, int ldu,
+                int crossing, int accumulate, void* workspace, size_t workspace_bytes, void* stream);
+int mg_backdiff_ft(int N, int L, int B, const int* strides, const float* p, float* dp, int ldp, const float* s,
+                   int lds, const void* u_out, const void* dJdu_out, void* u_in, void* dJdu_in, int ldu, int crossing,
+                   int accumulate, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- programmed-mesh entry points (coefficients kept resident between calls) -----------------
+ * mg_build_tiles runs only the coefficient precompute of `op` into the workspace; mg_propagate runs
+ * only the propagation kernel on tiles built earlier with the same (op, N, L, crossing, geometry,
+ * cfg).  Used by the autograd function, the batched engine and the server, which re-use one set of
+ * tiles across many batches.  Tgen/Dgen (crossing MG_GENERIC) give T per slot as 4 complex64
+ * (t00, t01, t10, t11) and, for op MG_OP_BWD, dT/dp0 and dT/dp1 (8 complex64). */
+int mg_build_tiles(int op, int N, int L, int geometry, const int* lens, const int* shifts, const int* strides,
+                   int crossing, const float* p, int ldp, const float* s, int lds, const float* dp, const void* Tgen,
+                   const void* Dgen, int B, const mg_config* cfg, void* workspace, size_t workspace_bytes, void* stream);
+
+int mg_propagate(int op, int N, int L, int B, int crossing, int geometry, const void* in0, const void* in1, void* out0,
+                 void* out1, int ldu, float* dp, int ldp, int accumulate, const mg_config* cfg, void* workspace,
+                 size_t workspace_bytes, void* stream);
+
+/* ---- measurement helpers -------------------------------------------------------------------- */
+
+/* FP32 FMA throughput probe: `blocks` x `threads` threads each run `iters` iterations of 64
+ * independent FMAs; writes one float per thread to `sink`.  Used by bench.py to measure the FP32
+ * CUDA-core peak of the device it runs on. */
+int mg_fma_probe(float* sink, int blocks, int threads, int iters, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MESHES_GB300_H */

@@ -1,0 +1,106 @@
+"""ctypes binding of libmeshes_gb300.so (the C ABI declared in include/meshes_gb300.h).
+
+The library is the only compute path: if it is missing or fails to load, every call raises
+``MeshLibraryError``.  There is no CPU or PyTorch fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+from ctypes import POINTER, Structure, c_char_p, c_int, c_size_t, c_void_p
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libmeshes_gb300.so")
+
+MZI, SYM, ORTH, GENERIC = 0, 1, 2, 3
+OP_FWD, OP_FWDDIFF, OP_BWD = 0, 1, 2
+GEO_NN, GEO_FFT = 0, 1
+CROSSING_CODES = {"mzi": MZI, "sym": SYM, "orth": ORTH, "generic": GENERIC}
+STATUS_NAMES = {0: "ok", 1: "timeout", 2: "bad geometry", 3: "bad work item"}
+
+
+class MeshLibraryError(RuntimeError):
+    pass
+
+
+class mg_config(Structure):
+    _fields_ = [("M", c_int), ("V", c_int), ("W", c_int), ("CL", c_int), ("S", c_int)]
+
+    def as_tuple(self):
+        return (self.M, self.V, self.W, self.CL, self.S)
+
+
+_SIGS = {
+    "mg_last_error": (c_char_p, []),
+    "mg_version": (c_char_p, []),
+    "mg_workspace_bytes": (c_size_t, [c_int, c_int, c_int, c_int, c_int, c_int, POINTER(mg_config)]),
+    "mg_workspace_init": (c_int, [c_void_p, c_size_t, c_void_p]),
+    "mg_read_status": (c_int, [c_void_p, c_int, c_void_p]),
+    "mg_default_config": (c_int, [c_int, c_int, c_int, c_int, POINTER(mg_config)]),
+    "mg_fwdprop": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p,
+                           c_void_p, c_int, c_int, c_void_p, c_size_t, c_void_p]),
+    "mg_fwdprop_ft": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p,
+                              c_int, c_int, c_void_p, c_size_t, c_void_p]),
+    "mg_fwddiff": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int,
+                           c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p, c_size_t, c_void_p]),
+    "mg_fwddiff_ft": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p,
+                              c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p, c_size_t, c_void_p]),
+    "mg_backdiff": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int,
+                            c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_size_t,
+                            c_void_p]),
+    "mg_backdiff_ft": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p,
+                               c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_size_t, c_void_p]),
+    "mg_build_tiles": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int,
+                               c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_int, POINTER(mg_config), c_void_p,
+                               c_size_t, c_void_p]),
+    "mg_propagate": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
+                             c_void_p, c_int, c_int, POINTER(mg_config), c_void_p, c_size_t, c_void_p]),
+    "mg_fma_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load (once) and return the ctypes library handle."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(path):
+                raise MeshLibraryError(
+                    "libmeshes_gb300.so is not built (%s); run `python -m meshes_gb300.build`" % path)
+            try:
+                lib = ctypes.CDLL(path)
+            except OSError as e:   # pragma: no cover - exercised only on broken installs
+                raise MeshLibraryError("cannot load %s: %s" % (path, e)) from e
+            for name, (res, args) in _SIGS.items():
+                f = getattr(lib, name)
+                f.restype = res
+                f.argtypes = args
+            _lib = lib
+    return _lib
+
+
+def exported_symbols():
+    return sorted(_SIGS)
+
+
+def last_error() -> str:
+    return (load().mg_last_error() or b"").decode()
+
+
+def check(rc: int, what: str):
+    if rc != 0:
+        raise MeshLibraryError("%s failed (rc=%d): %s" % (what, rc, last_error()))
+
+
+def config(M=0, V=0, W=0, CL=0, S=0):
+    return mg_config(M, V, W, CL, S)
+
+
+def cfg_ptr(cfg):
+    return None if cfg is None else ctypes.byref(cfg)

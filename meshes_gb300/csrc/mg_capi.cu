@@ -1,0 +1,449 @@
+// C ABI of libmeshes_gb300.so (declared in include/meshes_gb300.h).
+//
+// Each reference-shaped entry point checks its arguments on the host, derives a launch plan (tile
+// configuration, shared-memory footprint, workspace layout), then enqueues on the caller's stream:
+//   coef_kernel      p, s[, dp] -> coefficient tiles + layer kinds (+ dT/dp tiles for back-prop)
+//   prop_kernel      the propagation itself
+//   dp_reduce_kernel (back-prop only) deterministic sum of the per-CTA gradient partials
+// Nothing is allocated: all scratch lives in the caller's workspace.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/meshes_gb300.h"
+#include "mg_coeffs.cuh"
+#include "mg_inst_table.h"
+#include "mg_launch.h"
+
+using namespace mg;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(MG_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+int pow2ceil(int x) {
+  int p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+int ilog2(int x) {
+  int l = 0;
+  while ((1 << l) < x) ++l;
+  return l;
+}
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct DevInfo {
+  int sms = 0;
+  int smem_optin = 0;
+};
+DevInfo dev_info() {
+  static std::mutex mu;
+  static DevInfo cache[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  DevInfo& d = cache[dev & 63];
+  if (d.sms == 0) {
+    cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&d.smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (d.sms <= 0) d.sms = 152;
+    if (d.smem_optin <= 0) d.smem_optin = 227 * 1024;
+  }
+  return d;
+}
+
+bool instantiated(int op, int M, int V) {
+  for (int i = 0; i < kInstCount[op]; ++i)
+    if (kInst[op][i][0] == M && kInst[op][i][1] == V) return true;
+  return false;
+}
+
+struct Plan {
+  int op, N, L, B, crossing, geometry;
+  bool real;
+  int M, V, W, CL, S, G, logG, R, np2, grid;
+  unsigned lb, dlb;
+  size_t smem;
+  size_t off_kinds, off_tiles, off_dtiles, off_partial, total;
+};
+
+int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_config* cfg, Plan* P) {
+  if (op < 0 || op > 2) return fail(MG_E_ARG, "op %d not in {0,1,2}", op);
+  if (crossing < 0 || crossing > 3) return fail(MG_E_ARG, "crossing %d not in {0,1,2,3}", crossing);
+  if (geometry < 0 || geometry > 1) return fail(MG_E_ARG, "geometry %d not in {0,1}", geometry);
+  if (N < 2 || N % 2) return fail(MG_E_ARG, "N=%d must be even and >= 2 (reference gpu/mesh.py:67)", N);
+  if (N > 512) return fail(MG_E_ARG, "N=%d above the supported maximum 512", N);
+  if (L < 0 || B < 0) return fail(MG_E_ARG, "L=%d, B=%d must be non-negative", L, B);
+  const DevInfo di = dev_info();
+  Plan& p = *P;
+  p.op = op; p.N = N; p.L = L; p.B = B; p.crossing = crossing; p.geometry = geometry;
+  p.real = crossing == CR_ORTH;
+  const int Np = pow2ceil(N);
+  int M = (cfg && cfg->M) ? cfg->M : std::max(std::min(8, Np), Np / 32);
+  if (M < 2 || M > 16 || (M & (M - 1))) return fail(MG_E_CONFIG, "modes per lane M=%d not in {2,4,8,16}", M);
+  if (M > Np) M = Np;
+  const int G = Np / M;
+  if (G > 32) return fail(MG_E_CONFIG, "N=%d needs more than 32 lanes at M=%d", N, M);
+  int V = (cfg && cfg->V) ? cfg->V : 0;
+  if (!V) {
+    static const int vd[3][5] = {{8, 8, 4, 2, 0}, {4, 4, 2, 1, 0}, {4, 4, 4, 2, 0}};   // by ilog2(M)-1
+    V = vd[op][ilog2(M) - 1];
+  }
+  if (!instantiated(op, M, V)) return fail(MG_E_CONFIG, "no kernel instantiated for op=%d M=%d V=%d", op, M, V);
+  p.M = M; p.V = V; p.G = G; p.logG = ilog2(G); p.R = 32 / G; p.np2 = G * M / 2;
+  const unsigned tslot = p.real ? 16 : 32;               // bytes per slot of a T tile
+  p.lb = (unsigned)(p.np2 * tslot * (op == OP_FWDDIFF ? 2 : 1));
+  p.dlb = (op == OP_BWD) ? (unsigned)(p.np2 * (p.real ? 16 : 64)) : 0;
+  const size_t gstl = (op == OP_BWD) ? (size_t)p.np2 * (p.real ? 16 : 32) : 0;
+  const int maxw = prop_max_threads(op, M, V) / 32;
+  int W = (cfg && cfg->W) ? cfg->W : 0;
+  if (!W) {
+    const long per_warp = (long)p.R * V;
+    const long warps = (B + per_warp - 1) / per_warp;
+    W = (int)std::min<long>(std::max<long>((warps + di.sms - 1) / di.sms, 1), std::min(8, maxw));
+  }
+  if (W < 1 || W > maxw) return fail(MG_E_CONFIG, "W=%d warps outside [1, %d]", W, maxw);
+  int S = (cfg && cfg->S) ? cfg->S : 3;
+  if (S < 1 || S > 8) return fail(MG_E_CONFIG, "S=%d stages outside [1, 8]", S);
+  const size_t budget = (size_t)di.smem_optin - 1024;
+  int CL = (cfg && cfg->CL) ? cfg->CL : 0;
+  const size_t per_layer = (size_t)S * p.lb + p.dlb + W * gstl;
+  if (!CL) {
+    const size_t target = (op == OP_BWD) ? budget : std::min<size_t>(budget, 96 * 1024);
+    CL = (int)std::max<size_t>(1, std::min<size_t>(16, target / per_layer));
+    if (L > 0) CL = std::min(CL, L);
+  }
+  if (CL < 1) return fail(MG_E_CONFIG, "CL=%d", CL);
+  p.W = W; p.S = S; p.CL = CL;
+  p.smem = prop_smem_bytes(op, p.real, M, G, W, CL, S, p.lb, p.dlb);
+  if (p.smem > budget)
+    return fail(MG_E_CONFIG, "shared memory %zu B above the %zu B available (M=%d W=%d CL=%d S=%d)", p.smem, budget, M,
+                W, CL, S);
+  if ((size_t)CL * p.lb >= (1u << 20) || (size_t)CL * p.dlb >= (1u << 20))
+    return fail(MG_E_CONFIG, "one pipeline stage exceeds the 1 MB bulk-copy limit");
+  const long per_cta = (long)W * p.R * V;
+  p.grid = (int)((B + per_cta - 1) / per_cta);
+  p.off_kinds = 256;
+  p.off_tiles = p.off_kinds + align256((size_t)std::max(L, 1) * 4);
+  p.off_dtiles = p.off_tiles + align256((size_t)L * p.lb);
+  p.off_partial = p.off_dtiles + align256((size_t)L * p.dlb);
+  p.total = p.off_partial + ((op == OP_BWD) ? align256((size_t)p.grid * L * p.np2 * 8) : 0);
+  return MG_OK;
+}
+
+int check_ws(const Plan& p, void* ws, size_t bytes) {
+  if (!ws) return fail(MG_E_WORKSPACE, "workspace is NULL (need %zu bytes)", p.total);
+  if ((reinterpret_cast<uintptr_t>(ws) & 255) != 0) return fail(MG_E_WORKSPACE, "workspace not 256-byte aligned");
+  if (bytes < p.total) return fail(MG_E_WORKSPACE, "workspace has %zu bytes, needs %zu", bytes, p.total);
+  return MG_OK;
+}
+
+int check_field(const void* ptr, const char* name, bool real, bool required) {
+  if (!ptr) return required ? fail(MG_E_ARG, "%s is NULL", name) : MG_OK;
+  const uintptr_t a = reinterpret_cast<uintptr_t>(ptr);
+  if (a & (real ? 7 : 15)) return fail(MG_E_ARG, "%s not %d-byte aligned", name, real ? 8 : 16);
+  return MG_OK;
+}
+
+int check_params(const Plan& p, const float* pp, int ldp, const float* s, int lds, const void* Tgen) {
+  if (p.L == 0) return MG_OK;
+  if (p.crossing == CR_GENERIC) {
+    if (!Tgen) return fail(MG_E_ARG, "generic crossing needs Tgen");
+    return MG_OK;
+  }
+  const int n_p = crossing_np(p.crossing), n_s = crossing_ns(p.crossing);
+  if (!pp) return fail(MG_E_ARG, "p is NULL");
+  if (ldp < p.N / 2 * n_p) return fail(MG_E_ARG, "ldp=%d < N/2*n_p=%d (gpu/mesh.py:155)", ldp, p.N / 2 * n_p);
+  if (s && n_s == 0) return fail(MG_E_ARG, "crossing %d takes no splitter array", p.crossing);
+  if (s && lds < p.N / 2 * n_s) return fail(MG_E_ARG, "lds=%d < N/2*n_s=%d", lds, p.N / 2 * n_s);
+  return MG_OK;
+}
+
+int build_tiles(const Plan& P, const int* lens, const int* shifts, const int* strides, const float* p, int ldp,
+                const float* s, int lds, const float* dp, const void* Tgen, const void* Dgen, unsigned char* ws,
+                cudaStream_t st) {
+  if (P.L == 0) return MG_OK;
+  if (P.geometry == GEO_NN && (!lens || !shifts)) return fail(MG_E_ARG, "lens/shifts are NULL");
+  if (P.geometry == GEO_FFT && !strides) return fail(MG_E_ARG, "strides is NULL");
+  CoefArgs a;
+  a.N = P.N; a.L = P.L; a.crossing = P.crossing; a.geometry = P.geometry; a.op = P.op;
+  a.M = P.M; a.G = P.G;
+  a.lens = lens; a.shifts = shifts; a.strides = strides;
+  a.p = p; a.ldp = ldp; a.s = s; a.lds = lds; a.dp = dp;
+  a.Tgen = static_cast<const float2*>(Tgen);
+  a.Dgen = static_cast<const float2*>(Dgen);
+  a.tiles = ws + P.off_tiles; a.layer_bytes = P.lb;
+  a.dtiles = ws + P.off_dtiles; a.dlayer_bytes = P.dlb;
+  a.kinds = reinterpret_cast<int*>(ws + P.off_kinds);
+  a.status = reinterpret_cast<int*>(ws);
+  const int n = P.L * P.np2;
+  coef_kernel<<<(n + 255) / 256, 256, 0, st>>>(a);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MG_OK : cuda_fail(e, "coef_kernel launch");
+}
+
+int run_prop(const Plan& P, const void* in0, const void* in1, void* out0, void* out1, int ldu, float* dp, int ldp,
+             int accumulate, unsigned char* ws, cudaStream_t st) {
+  if (P.B == 0) return MG_OK;
+  PropArgs a;
+  a.N = P.N; a.L = P.L; a.B = P.B; a.ldu = ldu;
+  a.G = P.G; a.logG = P.logG; a.W = P.W; a.CL = P.CL; a.S = P.S;
+  a.layer_bytes = P.lb; a.dlayer_bytes = P.dlb;
+  a.tiles = ws + P.off_tiles; a.dtiles = ws + P.off_dtiles;
+  a.kinds = reinterpret_cast<const int*>(ws + P.off_kinds);
+  a.in0 = in0; a.in1 = in1; a.out0 = out0; a.out1 = out1;
+  a.partial = reinterpret_cast<float2*>(ws + P.off_partial);
+  a.status = reinterpret_cast<int*>(ws);
+  LaunchCfg lc;
+  lc.grid = dim3(P.grid);
+  lc.block = dim3(32 * P.W);
+  lc.smem = P.smem;
+  lc.stream = st;
+  cudaError_t e;
+  if (P.op == OP_FWD) e = launch_prop_fwd(P.real, P.M, P.V, lc, a);
+  else if (P.op == OP_FWDDIFF) e = launch_prop_fwddiff(P.real, P.M, P.V, lc, a);
+  else e = launch_prop_bwd(P.real, P.M, P.V, lc, a);
+  if (e != cudaSuccess) return cuda_fail(e, "prop_kernel launch");
+  if (P.op == OP_BWD && dp && P.L > 0) {
+    const int n = P.L * (P.N / 2);
+    dp_reduce_kernel<<<(n + 127) / 128, 128, 0, st>>>(a.partial, P.grid, P.L, P.np2, P.N, dp, ldp,
+                                                        crossing_np(P.crossing), accumulate);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "dp_reduce_kernel launch");
+  }
+  return MG_OK;
+}
+
+int check_ldu(const Plan& P, int ldu) {
+  if (ldu < P.N || (ldu & 1)) return fail(MG_E_ARG, "ldu=%d must be >= N=%d and even", ldu, P.N);
+  return MG_OK;
+}
+
+#define TRY(x)                  \
+  do {                          \
+    int _rc = (x);              \
+    if (_rc != MG_OK) return _rc; \
+  } while (0)
+
+int fwdprop_impl(int geo, int N, int L, int B, const int* lens, const int* shifts, const int* strides, const float* p,
+                 int ldp, const float* s, int lds, const void* u_in, void* u_out, int ldu, int crossing, void* ws,
+                 size_t wsb, void* stream) {
+  g_err.clear();
+  Plan P;
+  TRY(make_plan(OP_FWD, N, L, B, crossing, geo, nullptr, &P));
+  if (crossing == CR_GENERIC) return fail(MG_E_ARG, "use mg_build_tiles for generic crossings");
+  TRY(check_ws(P, ws, wsb));
+  TRY(check_ldu(P, ldu));
+  TRY(check_field(u_in, "u_in", P.real, B > 0));
+  TRY(check_field(u_out, "u_out", P.real, B > 0));
+  TRY(check_params(P, p, ldp, s, lds, nullptr));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned char* w = static_cast<unsigned char*>(ws);
+  TRY(build_tiles(P, lens, shifts, strides, p, ldp, s, lds, nullptr, nullptr, nullptr, w, st));
+  return run_prop(P, u_in, nullptr, u_out, nullptr, ldu, nullptr, 0, 0, w, st);
+}
+
+int fwddiff_impl(int geo, int N, int L, int B, const int* lens, const int* shifts, const int* strides, const float* p,
+                 const float* dp, int ldp, const float* s, int lds, const void* u_in, const void* du_in, void* u_out,
+                 void* du_out, int ldu, int crossing, void* ws, size_t wsb, void* stream) {
+  g_err.clear();
+  Plan P;
+  TRY(make_plan(OP_FWDDIFF, N, L, B, crossing, geo, nullptr, &P));
+  if (crossing == CR_GENERIC) return fail(MG_E_ARG, "use mg_build_tiles for generic crossings");
+  TRY(check_ws(P, ws, wsb));
+  TRY(check_ldu(P, ldu));
+  TRY(check_field(u_in, "u_in", P.real, B > 0));
+  TRY(check_field(du_in, "du_in", P.real, false));
+  TRY(check_field(u_out, "u_out", P.real, B > 0));
+  TRY(check_field(du_out, "du_out", P.real, B > 0));
+  TRY(check_params(P, p, ldp, s, lds, nullptr));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned char* w = static_cast<unsigned char*>(ws);
+  TRY(build_tiles(P, lens, shifts, strides, p, ldp, s, lds, dp, nullptr, nullptr, w, st));
+  return run_prop(P, u_in, du_in, u_out, du_out, ldu, nullptr, 0, 0, w, st);
+}
+
+int backdiff_impl(int geo, int N, int L, int B, const int* lens, const int* shifts, const int* strides, const float* p,
+                  float* dp, int ldp, const float* s, int lds, const void* u_out, const void* dJdu_out, void* u_in,
+                  void* dJdu_in, int ldu, int crossing, int accumulate, void* ws, size_t wsb, void* stream) {
+  g_err.clear();
+  Plan P;
+  TRY(make_plan(OP_BWD, N, L, B, crossing, geo, nullptr, &P));
+  if (crossing == CR_GENERIC) return fail(MG_E_ARG, "use mg_build_tiles for generic crossings");
+  TRY(check_ws(P, ws, wsb));
+  TRY(check_ldu(P, ldu));
+  TRY(check_field(u_out, "u_out", P.real, B > 0));
+  TRY(check_field(dJdu_out, "dJdu_out", P.real, B > 0));
+  TRY(check_field(u_in, "u_in", P.real, false));
+  TRY(check_field(dJdu_in, "dJdu_in", P.real, B > 0));
+  TRY(check_params(P, p, ldp, s, lds, nullptr));
+  if (!dp && L > 0) return fail(MG_E_ARG, "dp is NULL");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned char* w = static_cast<unsigned char*>(ws);
+  if (B == 0) {
+    if (!accumulate && L > 0) {
+      cudaError_t e = cudaMemsetAsync(dp, 0, sizeof(float) * ((size_t)(L - 1) * ldp + (size_t)N / 2 * crossing_np(crossing)), st);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(dp)");
+    }
+    return MG_OK;
+  }
+  TRY(build_tiles(P, lens, shifts, strides, p, ldp, s, lds, nullptr, nullptr, nullptr, w, st));
+  return run_prop(P, u_out, dJdu_out, u_in, dJdu_in, ldu, dp, ldp, accumulate, w, st);
+}
+
+__global__ void fma_probe_kernel(float* sink, int iters, float m) {
+  float a[32];
+#pragma unroll
+  for (int k = 0; k < 32; ++k) a[k] = threadIdx.x * 1e-3f + k;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int k = 0; k < 32; ++k) a[k] = fmaf(a[k], m, 0.25f);
+#pragma unroll
+    for (int k = 0; k < 32; ++k) a[k] = fmaf(a[k], m, -0.25f);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < 32; ++k) s += a[k];
+  sink[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mg_last_error(void) { return g_err.c_str(); }
+
+const char* mg_version(void) { return "meshes_gb300 0.1 (sm_103a)"; }
+
+size_t mg_workspace_bytes(int op, int N, int L, int B, int crossing, int geometry, const mg_config* cfg) {
+  Plan P;
+  if (make_plan(op, N, L, B, crossing, geometry, cfg, &P) != MG_OK) return 0;
+  return P.total;
+}
+
+int mg_workspace_init(void* ws, size_t bytes, void* stream) {
+  g_err.clear();
+  if (!ws || bytes < 256) return fail(MG_E_WORKSPACE, "workspace NULL or smaller than 256 bytes");
+  cudaError_t e = cudaMemsetAsync(ws, 0, 256, static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? MG_OK : cuda_fail(e, "cudaMemsetAsync(status)");
+}
+
+int mg_read_status(void* ws, int clear, void* stream) {
+  g_err.clear();
+  if (!ws) return fail(MG_E_WORKSPACE, "workspace is NULL");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int v = 0;
+  cudaError_t e = cudaMemcpyAsync(&v, ws, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "reading status");
+  if (clear && v) {
+    e = cudaMemsetAsync(ws, 0, sizeof(int), st);
+    if (e != cudaSuccess) return cuda_fail(e, "clearing status");
+  }
+  return v;
+}
+
+int mg_default_config(int op, int N, int B, int crossing, mg_config* out) {
+  g_err.clear();
+  Plan P;
+  TRY(make_plan(op, N, 1, B, crossing, GEO_NN, nullptr, &P));
+  if (out) {
+    out->M = P.M; out->V = P.V; out->W = P.W; out->CL = P.CL; out->S = P.S;
+  }
+  return MG_OK;
+}
+
+int mg_fwdprop(int N, int L, int B, const int* lens, const int* shifts, const float* p, int ldp, const float* s,
+               int lds, const void* u_in, void* u_out, int ldu, int crossing, void* ws, size_t wsb, void* stream) {
+  return fwdprop_impl(GEO_NN, N, L, B, lens, shifts, nullptr, p, ldp, s, lds, u_in, u_out, ldu, crossing, ws, wsb,
+                      stream);
+}
+int mg_fwdprop_ft(int N, int L, int B, const int* strides, const float* p, int ldp, const float* s, int lds,
+                  const void* u_in, void* u_out, int ldu, int crossing, void* ws, size_t wsb, void* stream) {
+  return fwdprop_impl(GEO_FFT, N, L, B, nullptr, nullptr, strides, p, ldp, s, lds, u_in, u_out, ldu, crossing, ws,
+                      wsb, stream);
+}
+int mg_fwddiff(int N, int L, int B, const int* lens, const int* shifts, const float* p, const float* dp, int ldp,
+               const float* s, int lds, const void* u_in, const void* du_in, void* u_out, void* du_out, int ldu,
+               int crossing, void* ws, size_t wsb, void* stream) {
+  return fwddiff_impl(GEO_NN, N, L, B, lens, shifts, nullptr, p, dp, ldp, s, lds, u_in, du_in, u_out, du_out, ldu,
+                      crossing, ws, wsb, stream);
+}
+int mg_fwddiff_ft(int N, int L, int B, const int* strides, const float* p, const float* dp, int ldp, const float* s,
+                  int lds, const void* u_in, const void* du_in, void* u_out, void* du_out, int ldu, int crossing,
+                  void* ws, size_t wsb, void* stream) {
+  return fwddiff_impl(GEO_FFT, N, L, B, nullptr, nullptr, strides, p, dp, ldp, s, lds, u_in, du_in, u_out, du_out,
+                      ldu, crossing, ws, wsb, stream);
+}
+int mg_backdiff(int N, int L, int B, const int* lens, const int* shifts, const float* p, float* dp, int ldp,
+                const float* s, int lds, const void* u_out, const void* dJdu_out, void* u_in, void* dJdu_in, int ldu,
+                int crossing, int accumulate, void* ws, size_t wsb, void* stream) {
+  return backdiff_impl(GEO_NN, N, L, B, lens, shifts, nullptr, p, dp, ldp, s, lds, u_out, dJdu_out, u_in, dJdu_in,
+                       ldu, crossing, accumulate, ws, wsb, stream);
+}
+int mg_backdiff_ft(int N, int L, int B, const int* strides, const float* p, float* dp, int ldp, const float* s,
+                   int lds, const void* u_out, const void* dJdu_out, void* u_in, void* dJdu_in, int ldu, int crossing,
+                   int accumulate, void* ws, size_t wsb, void* stream) {
+  return backdiff_impl(GEO_FFT, N, L, B, nullptr, nullptr, strides, p, dp, ldp, s, lds, u_out, dJdu_out, u_in,
+                       dJdu_in, ldu, crossing, accumulate, ws, wsb, stream);
+}
+
+int mg_build_tiles(int op, int N, int L, int geometry, const int* lens, const int* shifts, const int* strides,
+                   int crossing, const float* p, int ldp, const float* s, int lds, const float* dp, const void* Tgen,
+                   const void* Dgen, int B, const mg_config* cfg, void* ws, size_t wsb, void* stream) {
+  g_err.clear();
+  Plan P;
+  TRY(make_plan(op, N, L, B, crossing, geometry, cfg, &P));
+  TRY(check_ws(P, ws, wsb));
+  TRY(check_params(P, p, ldp, s, lds, Tgen));
+  if (crossing == CR_GENERIC && op == OP_BWD && !Dgen && L > 0) return fail(MG_E_ARG, "generic back-prop needs Dgen");
+  if (crossing == CR_GENERIC && op == OP_FWDDIFF) return fail(MG_E_ARG, "generic crossings support fwd and bwd only");
+  return build_tiles(P, lens, shifts, strides, p, ldp, s, lds, dp, Tgen, Dgen, static_cast<unsigned char*>(ws),
+                     static_cast<cudaStream_t>(stream));
+}
+
+int mg_propagate(int op, int N, int L, int B, int crossing, int geometry, const void* in0, const void* in1, void* out0,
+                 void* out1, int ldu, float* dp, int ldp, int accumulate, const mg_config* cfg, void* ws, size_t wsb,
+                 void* stream) {
+  g_err.clear();
+  Plan P;
+  TRY(make_plan(op, N, L, B, crossing, geometry, cfg, &P));
+  TRY(check_ws(P, ws, wsb));
+  TRY(check_ldu(P, ldu));
+  TRY(check_field(in0, "in0", P.real, B > 0));
+  TRY(check_field(in1, "in1", P.real, op == OP_BWD && B > 0));
+  TRY(check_field(out0, "out0", P.real, op != OP_BWD && B > 0));
+  TRY(check_field(out1, "out1", P.real, op != OP_FWD && B > 0));
+  if (op == OP_BWD && dp && ldp < N / 2 * crossing_np(crossing)) return fail(MG_E_ARG, "ldp too small");
+  return run_prop(P, in0, in1, out0, out1, ldu, dp, ldp, accumulate, static_cast<unsigned char*>(ws),
+                  static_cast<cudaStream_t>(stream));
+}
+
+int mg_fma_probe(float* sink, int blocks, int threads, int iters, void* stream) {
+  g_err.clear();
+  if (!sink || blocks < 1 || threads < 32 || threads > 1024 || iters < 1) return fail(MG_E_ARG, "bad probe arguments");
+  fma_probe_kernel<<<blocks, threads, 0, static_cast<cudaStream_t>(stream)>>>(sink, iters, 0.999f);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MG_OK : cuda_fail(e, "fma_probe launch");
+}
+
+}  // extern "C"

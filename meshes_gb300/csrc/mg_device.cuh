@@ -1,0 +1,229 @@
+// Device-side building blocks shared by every kernel of the library:
+//   * complex64 arithmetic on float2 (explicit FMA forms so the compiler emits one FFMA per term)
+//   * mbarrier / bulk-TMA (cp.async.bulk) wrappers in inline PTX for sm_103a
+//   * bounded waits: every spin on an mbarrier gives up after a time limit, records an error code in
+//     the caller's status word and lets the kernel return (no __trap, no unbounded loop)
+//   * the closed forms of the crossing matrices T(p, s) and their derivatives dT/dp (double precision)
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mg {
+
+// ---------------------------------------------------------------------------------------------
+// status codes written by kernels into the status word of the workspace
+// ---------------------------------------------------------------------------------------------
+enum : int {
+  ST_OK = 0,
+  ST_TIMEOUT = 1,        // an mbarrier wait ran past its time limit
+  ST_BAD_GEOMETRY = 2,   // lens/shifts/strides describe MZIs outside the N modes
+  ST_BAD_WORK = 3,       // persistent kernel: malformed work item
+};
+
+// ---------------------------------------------------------------------------------------------
+// complex helpers (float2 = complex64)
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {          // a*b
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {  // c + a*b
+  return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, c.y)));
+}
+__device__ __forceinline__ float2 ccmul(float2 a, float2 b) {         // conj(a)*b
+  return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.x, b.y, -a.y * b.x));
+}
+__device__ __forceinline__ float2 ccfma(float2 a, float2 b, float2 c) {  // c + conj(a)*b
+  return make_float2(fmaf(a.x, b.x, fmaf(a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(-a.y, b.x, c.y)));
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ float2 cscale(float s, float2 a) { return make_float2(s * a.x, s * a.y); }
+__device__ __forceinline__ float2 ci(float2 a) { return make_float2(-a.y, a.x); }  // i*a
+
+// real "complex" overloads used by the real (orth) instantiation of the same templates
+__device__ __forceinline__ float cmul(float a, float b) { return a * b; }
+__device__ __forceinline__ float cfma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ float ccmul(float a, float b) { return a * b; }
+__device__ __forceinline__ float ccfma(float a, float b, float c) { return fmaf(a, b, c); }
+
+__device__ __forceinline__ float2 shfl_down(float2 v, int d, int w) {
+  return make_float2(__shfl_down_sync(0xffffffffu, v.x, d, w), __shfl_down_sync(0xffffffffu, v.y, d, w));
+}
+__device__ __forceinline__ float2 shfl_up(float2 v, int d, int w) {
+  return make_float2(__shfl_up_sync(0xffffffffu, v.x, d, w), __shfl_up_sync(0xffffffffu, v.y, d, w));
+}
+__device__ __forceinline__ float2 shfl_xor(float2 v, int d, int w) {
+  return make_float2(__shfl_xor_sync(0xffffffffu, v.x, d, w), __shfl_xor_sync(0xffffffffu, v.y, d, w));
+}
+__device__ __forceinline__ float shfl_down(float v, int d, int w) { return __shfl_down_sync(0xffffffffu, v, d, w); }
+__device__ __forceinline__ float shfl_up(float v, int d, int w) { return __shfl_up_sync(0xffffffffu, v, d, w); }
+__device__ __forceinline__ float shfl_xor(float v, int d, int w) { return __shfl_xor_sync(0xffffffffu, v, d, w); }
+
+template <typename F> __device__ __forceinline__ F fzero();
+template <> __device__ __forceinline__ float2 fzero<float2>() { return make_float2(0.f, 0.f); }
+template <> __device__ __forceinline__ float fzero<float>() { return 0.f; }
+
+// ---------------------------------------------------------------------------------------------
+// mbarrier + bulk TMA (inline PTX, sm_90+ forms valid on sm_103a)
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// 1-D bulk copy global -> this CTA's shared memory, completion signalled on `bar` (complete_tx).
+// Both addresses 16-byte aligned, bytes a multiple of 16 (checked by the host launchers).
+__device__ __forceinline__ void tma_load_1d(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Time limit of one mbarrier wait.  A bulk copy of a few tens of KB completes in microseconds; the
+// limit only has to separate "slow" from "never" (profilers replaying kernels are slow, not stuck).
+constexpr uint64_t kWaitLimitNs = 4000000000ull;   // 4 s
+
+// Wait for phase `parity` of `bar`; false after the time limit (the caller then records ST_TIMEOUT).
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  for (uint32_t it = 1;; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 63u) == 0 && globaltimer_ns() - t0 > kWaitLimitNs) return false;
+  }
+}
+
+__device__ __forceinline__ void set_status(int* status, int code) {
+  if (status) atomicCAS(status, 0, code);
+}
+
+// ---------------------------------------------------------------------------------------------
+// crossing matrices.  Ct = complex 2x2 (t00, t01, t10, t11).
+// ---------------------------------------------------------------------------------------------
+struct C2x2 {
+  float2 t00, t01, t10, t11;
+};
+struct R2x2 {
+  float t00, t01, t10, t11;
+};
+
+__device__ __forceinline__ C2x2 c2x2_identity() {
+  C2x2 r;
+  r.t00 = make_float2(1.f, 0.f); r.t01 = make_float2(0.f, 0.f);
+  r.t10 = make_float2(0.f, 0.f); r.t11 = make_float2(1.f, 0.f);
+  return r;
+}
+__device__ __forceinline__ C2x2 c2x2_zero() {
+  C2x2 r;
+  r.t00 = r.t01 = r.t10 = r.t11 = make_float2(0.f, 0.f);
+  return r;
+}
+
+// The closed forms below are evaluated in double precision and rounded once to float32.  Float32
+// sincosf carries a small systematic error that a deep mesh accumulates coherently (the relative
+// error then grows linearly with the depth L: 1.1e-5 at L = 512 measured on a GB300); double
+// trigonometry rounded to float32 leaves only unbiased rounding, whose effect grows as sqrt(L).
+// This runs once per slot per call (or once per programmed mesh), never in the propagation loop.
+struct Z {
+  double x, y;
+};
+__device__ __forceinline__ Z zmul(Z a, Z b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+__device__ __forceinline__ Z zadd(Z a, Z b) { return {a.x + b.x, a.y + b.y}; }
+__device__ __forceinline__ Z zscale(double s, Z a) { return {s * a.x, s * a.y}; }
+__device__ __forceinline__ Z zi(Z a) { return {-a.y, a.x}; }
+__device__ __forceinline__ float2 zf(Z a) { return make_float2((float)a.x, (float)a.y); }
+
+// Standard MZI T = S(beta) P(theta) S(alpha) P(phi) (reference crossing.py:216-221):
+//   T = e^{i th/2} [[e^{i ph}(i S Cm - C Sp),  i C Cp - S Sm],
+//                   [e^{i ph}(i C Cp + S Sm), -i S Cm - C Sp]]
+// with C,S = cos,sin(th/2) and C+-,S+- = cos,sin(alpha +- beta).  D0 = dT/dth, D1 = dT/dph
+// (crossing.py:223-231): dE/dth = (i/2)E for both exponentials, dT/dph = T diag(i, 0).
+__device__ __forceinline__ void mzi_T(float th, float ph, float al, float be, C2x2* T, C2x2* D0, C2x2* D1) {
+  double S, C, Sph, Cph, Sp = 0.0, Cp = 1.0, Sm = 0.0, Cm = 1.0;
+  sincos(0.5 * (double)th, &S, &C);
+  sincos((double)ph, &Sph, &Cph);
+  if (al != 0.f || be != 0.f) {
+    sincos((double)al + (double)be, &Sp, &Cp);
+    sincos((double)al - (double)be, &Sm, &Cm);
+  }
+  const Z E0 = {C, S};                                      // e^{i th/2}
+  const Z E1 = zmul(E0, Z{Cph, Sph});                       // e^{i(th/2+ph)}
+  const Z A00 = {-C * Sp, S * Cm}, A01 = {-S * Sm, C * Cp};
+  const Z A10 = {S * Sm, C * Cp}, A11 = {-C * Sp, -S * Cm};
+  const Z T00 = zmul(E1, A00), T01 = zmul(E0, A01), T10 = zmul(E1, A10), T11 = zmul(E0, A11);
+  T->t00 = zf(T00); T->t01 = zf(T01); T->t10 = zf(T10); T->t11 = zf(T11);
+  if (D0) {
+    // dA/dth with dC = -S/2, dS = C/2
+    const Z dA00 = {0.5 * S * Sp, 0.5 * C * Cm}, dA01 = {-0.5 * C * Sm, -0.5 * S * Cp};
+    const Z dA10 = {0.5 * C * Sm, -0.5 * S * Cp}, dA11 = {0.5 * S * Sp, -0.5 * C * Cm};
+    D0->t00 = zf(zmul(E1, zadd(zscale(0.5, zi(A00)), dA00)));
+    D0->t01 = zf(zmul(E0, zadd(zscale(0.5, zi(A01)), dA01)));
+    D0->t10 = zf(zmul(E1, zadd(zscale(0.5, zi(A10)), dA10)));
+    D0->t11 = zf(zmul(E0, zadd(zscale(0.5, zi(A11)), dA11)));
+  }
+  if (D1) {
+    D1->t00 = zf(zi(T00)); D1->t10 = zf(zi(T10));
+    D1->t01 = make_float2(0.f, 0.f); D1->t11 = make_float2(0.f, 0.f);
+  }
+}
+
+// Symmetric crossing (reference crossing.py:377-381, gpu/crossing.cu:90-126):
+//   T = [[e^{i ph}(S + i C sin2a), i C cos2a], [i C cos2a, e^{-i ph}(S - i C sin2a)]]
+__device__ __forceinline__ void sym_T(float th, float ph, float al, C2x2* T, C2x2* D0, C2x2* D1) {
+  double S, C, Sph, Cph, S2a = 0.0, C2a = 1.0;
+  sincos(0.5 * (double)th, &S, &C);
+  sincos((double)ph, &Sph, &Cph);
+  if (al != 0.f) sincos(2.0 * (double)al, &S2a, &C2a);
+  const Z e = {Cph, Sph}, em = {Cph, -Sph};
+  const Z T00 = zmul(e, Z{S, C * S2a}), T11 = zmul(em, Z{S, -C * S2a});
+  T->t00 = zf(T00);
+  T->t01 = T->t10 = zf(Z{0.0, C * C2a});
+  T->t11 = zf(T11);
+  if (D0) {
+    D0->t00 = zf(zmul(e, Z{0.5 * C, -0.5 * S * S2a}));
+    D0->t01 = D0->t10 = zf(Z{0.0, -0.5 * S * C2a});
+    D0->t11 = zf(zmul(em, Z{0.5 * C, 0.5 * S * S2a}));
+  }
+  if (D1) {
+    D1->t00 = zf(zi(T00));
+    D1->t11 = zf(zscale(-1.0, zi(T11)));
+    D1->t01 = D1->t10 = make_float2(0.f, 0.f);
+  }
+}
+
+// Real orthogonal crossing (reference gpu/crossing.cu:132-148): T = [[S, -C], [C, S]], S,C of th/2.
+__device__ __forceinline__ void orth_T(float th, R2x2* T, R2x2* D0) {
+  double S, C;
+  sincos(0.5 * (double)th, &S, &C);
+  T->t00 = (float)S; T->t01 = (float)-C; T->t10 = (float)C; T->t11 = (float)S;
+  if (D0) {
+    D0->t00 = (float)(0.5 * C); D0->t01 = (float)(0.5 * S); D0->t10 = (float)(-0.5 * S); D0->t11 = (float)(0.5 * C);
+  }
+}
+
+}  // namespace mg

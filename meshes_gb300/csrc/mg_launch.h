@@ -1,0 +1,51 @@
+// Internal host-side launch plumbing shared by the instantiation units and the C ABI.
+#pragma once
+#include <atomic>
+#include <cuda_runtime.h>
+
+#include "mg_prop.cuh"
+
+namespace mg {
+
+struct LaunchCfg {
+  dim3 grid, block;
+  size_t smem;
+  cudaStream_t stream;
+};
+
+// Raise a kernel's dynamic shared-memory limit to the device opt-in maximum, once per device.
+template <typename K>
+inline cudaError_t ensure_smem_attr(K kernel, std::atomic<unsigned long long>& done) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (done.load(std::memory_order_acquire) & bit) return cudaSuccess;
+  int optin = 0;
+  e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  if (e != cudaSuccess) return e;
+  done.fetch_or(bit, std::memory_order_acq_rel);
+  return cudaSuccess;
+}
+
+template <int OP, int M, int V, bool REAL>
+inline cudaError_t launch_one(const LaunchCfg& lc, const PropArgs& a) {
+  static std::atomic<unsigned long long> done{0};
+  auto k = prop_kernel<OP, M, V, REAL>;
+  cudaError_t e = ensure_smem_attr(k, done);
+  if (e != cudaSuccess) return e;
+  k<<<lc.grid, lc.block, lc.smem, lc.stream>>>(a);
+  return cudaGetLastError();
+}
+
+// max threads per CTA the instantiation was compiled for
+inline int prop_max_threads(int op, int M, int V) { return (op == OP_FWD && M * V <= 16) ? 512 : 256; }
+
+// per-op dispatchers (one translation unit each, compiled in parallel)
+cudaError_t launch_prop_fwd(bool real, int M, int V, const LaunchCfg& lc, const PropArgs& a);
+cudaError_t launch_prop_fwddiff(bool real, int M, int V, const LaunchCfg& lc, const PropArgs& a);
+cudaError_t launch_prop_bwd(bool real, int M, int V, const LaunchCfg& lc, const PropArgs& a);
+
+}  // namespace mg

@@ -1,0 +1,522 @@
+// The mesh-propagation kernel family (forward, forward-mode derivative, back-propagation).
+//
+// Work decomposition (one CTA = one batch tile of one mesh):
+//   * a vector of N complex64 modes is held in the registers of a group of G lanes (G a power of
+//     two <= 32), lane j owning the M contiguous modes [j*M, j*M+M); a warp holds R = 32/G such
+//     groups and every lane holds V vectors ("register block over the batch"), so each coefficient
+//     fetched from shared memory is reused V times;
+//   * the per-layer coefficient tiles (precomputed by mg_coeffs.cu in the exact order lanes consume
+//     them) are streamed through a ring of S shared-memory stages by 1-D bulk TMA copies
+//     (cp.async.bulk + mbarrier complete_tx), CL layers per stage, issued by one thread;
+//   * layer kinds: pairs inside a lane (nearest-neighbour aligned layers and butterfly strides
+//     < M) need no communication; a nearest-neighbour layer with odd shift couples the last mode of
+//     lane j with the first of lane j+1 (one __shfl_down / __shfl_up pair per vector); butterfly
+//     strides >= M couple lane j with lane j ^ (stride/M) (one __shfl_xor per mode, each lane
+//     computing its own outputs);
+//   * back-propagation walks the layers in reverse from the OUTPUTS, rebuilding each layer's input
+//     with T^H (lossless crossings need no stored activations, as the reference does in
+//     gpu/backdiff.cu and c/dot.cpp mode 2), accumulating dJ/dT_ij = sum_b conj(g_i) x_j in
+//     registers over the lane's V vectors, reducing over the R groups of a warp with __shfl_xor,
+//     staging per-warp sums in shared memory and, once per chunk, summing the warps in a fixed order
+//     and contracting with dT/dp into a per-CTA partial (no float atomics: bit-stable results).
+//
+// Reference counterparts: gpu/fwdprop.cu:25-123, gpu/fwddiff.cu:24-141, gpu/backdiff.cu:24-153,
+// gpu/crossing.cu:214-333 (the 2x2 appliers) and c/dot.cpp:146-288.
+#pragma once
+#include <type_traits>
+
+#include "mg_device.cuh"
+
+namespace mg {
+
+enum { OP_FWD = 0, OP_FWDDIFF = 1, OP_BWD = 2 };
+
+__host__ __device__ constexpr int ilog2_const(int x) { return x <= 1 ? 0 : 1 + ilog2_const(x >> 1); }
+
+// layer kinds written by the coefficient kernel (kinds[l])
+//   0..4          : pairs (a, a+2^k) inside one lane (k = 0: aligned nearest-neighbour layer)
+//   KIND_MIS      : nearest-neighbour layer with odd shift
+//   KIND_XL + e   : butterfly stride 2^e >= M, partner lane j ^ (2^e / M)
+constexpr int KIND_MIS = 8;
+constexpr int KIND_XL = 16;
+
+struct PropArgs {
+  int N, L, B, ldu;
+  int G, logG, W, CL, S;
+  unsigned layer_bytes;          // bytes of one layer's coefficient tile
+  unsigned dlayer_bytes;         // BWD: bytes of one layer of the dT/dp tile
+  const unsigned char* tiles;    // [L][layer_bytes]
+  const unsigned char* dtiles;   // BWD: [L][dlayer_bytes]
+  const int* kinds;              // [L]
+  const void* in0;               // FWD/FWDDIFF: u_in      BWD: u_out
+  const void* in1;               // FWDDIFF: du_in (may be null = 0)   BWD: dJ/du_out*
+  void* out0;                    // FWD/FWDDIFF: u_out     BWD: u_in (may be null)
+  void* out1;                    // FWDDIFF: du_out        BWD: dJ/du_in*
+  float2* partial;               // BWD: [gridDim.x][L][Np/2] (dJ/dp0, dJ/dp1) per CTA
+  int* status;
+};
+
+template <bool REAL> struct Fld { using T = float2; using C = C2x2; };
+template <> struct Fld<true> { using T = float; using C = R2x2; };
+
+// ---- coefficient access: complex tiles hold two float4 rows per entry ([e][h][j]), real tiles one
+__device__ __forceinline__ void ld_coef(const float4* tl, int e, int G, int j, C2x2& t) {
+  const float4 r0 = tl[(2 * e) * G + j], r1 = tl[(2 * e + 1) * G + j];
+  t.t00 = make_float2(r0.x, r0.y); t.t01 = make_float2(r0.z, r0.w);
+  t.t10 = make_float2(r1.x, r1.y); t.t11 = make_float2(r1.z, r1.w);
+}
+__device__ __forceinline__ void ld_coef(const float4* tl, int e, int G, int j, R2x2& t) {
+  const float4 q = tl[e * G + j];
+  t.t00 = q.x; t.t01 = q.y; t.t10 = q.z; t.t11 = q.w;
+}
+// float4 offset of the dT half of a FWDDIFF layer tile
+template <bool REAL, int M> __device__ __forceinline__ int dt_off(int G) { return REAL ? (M / 2) * G : M * G; }
+
+// ---- one 2x2 crossing on one vector
+template <typename F, typename CT>
+__device__ __forceinline__ void x_fwd(const CT& t, F& a, F& b) {
+  const F ya = cfma(t.t01, b, cmul(t.t00, a));
+  const F yb = cfma(t.t11, b, cmul(t.t10, a));
+  a = ya; b = yb;
+}
+template <typename F, typename CT>
+__device__ __forceinline__ void x_fwddiff(const CT& t, const CT& d, F& a, F& b, F& da, F& db) {
+  const F nda = cfma(d.t01, b, cfma(d.t00, a, cfma(t.t01, db, cmul(t.t00, da))));
+  const F ndb = cfma(d.t11, b, cfma(d.t10, a, cfma(t.t11, db, cmul(t.t10, da))));
+  da = nda; db = ndb;
+  x_fwd(t, a, b);
+}
+// back-propagation of one crossing: (y, g) at the output -> (x, g_in) at the input, G += conj(g) x^T
+template <typename F, typename CT>
+__device__ __forceinline__ void x_bwd(const CT& t, F& a, F& b, F& ga, F& gb, CT& acc) {
+  const F xa = ccfma(t.t10, b, ccmul(t.t00, a));
+  const F xb = ccfma(t.t11, b, ccmul(t.t01, a));
+  acc.t00 = ccfma(ga, xa, acc.t00); acc.t01 = ccfma(ga, xb, acc.t01);
+  acc.t10 = ccfma(gb, xa, acc.t10); acc.t11 = ccfma(gb, xb, acc.t11);
+  const F nga = ccfma(t.t10, gb, ccmul(t.t00, ga));
+  const F ngb = ccfma(t.t11, gb, ccmul(t.t01, ga));
+  a = xa; b = xb; ga = nga; gb = ngb;
+}
+
+__device__ __forceinline__ void acc_zero(C2x2& a) { a = c2x2_zero(); }
+__device__ __forceinline__ void acc_zero(R2x2& a) { a.t00 = a.t01 = a.t10 = a.t11 = 0.f; }
+
+__device__ __forceinline__ void acc_xor_reduce(C2x2& a, int G) {
+  for (int off = G; off < 32; off <<= 1) {
+    a.t00 = cadd(a.t00, shfl_xor(a.t00, off, 32)); a.t01 = cadd(a.t01, shfl_xor(a.t01, off, 32));
+    a.t10 = cadd(a.t10, shfl_xor(a.t10, off, 32)); a.t11 = cadd(a.t11, shfl_xor(a.t11, off, 32));
+  }
+}
+__device__ __forceinline__ void acc_xor_reduce(R2x2& a, int G) {
+  for (int off = G; off < 32; off <<= 1) {
+    a.t00 += shfl_xor(a.t00, off, 32); a.t01 += shfl_xor(a.t01, off, 32);
+    a.t10 += shfl_xor(a.t10, off, 32); a.t11 += shfl_xor(a.t11, off, 32);
+  }
+}
+// stage the warp's dJ/dT of entry e (same [e][h][j] layout as the coefficient tile)
+__device__ __forceinline__ void acc_stage(float4* gl, int e, int G, int j, int r, C2x2& a) {
+  acc_xor_reduce(a, G);
+  if (r == 0) {
+    gl[(2 * e) * G + j] = make_float4(a.t00.x, a.t00.y, a.t01.x, a.t01.y);
+    gl[(2 * e + 1) * G + j] = make_float4(a.t10.x, a.t10.y, a.t11.x, a.t11.y);
+  }
+}
+__device__ __forceinline__ void acc_stage(float4* gl, int e, int G, int j, int r, R2x2& a) {
+  acc_xor_reduce(a, G);
+  if (r == 0) gl[e * G + j] = make_float4(a.t00, a.t01, a.t10, a.t11);
+}
+
+// ---- one crossing entry e of a layer, applied to all V vectors of the lane
+template <int OP, int V, bool REAL, typename F>
+__device__ __forceinline__ void entry(const float4* tl, int doff, int e, int G, int j, int r, F* pa[V], F* pb[V],
+                                      F* pga[V], F* pgb[V], float4* gl) {
+  using CT = typename Fld<REAL>::C;
+  CT t;
+  ld_coef(tl, e, G, j, t);
+  if constexpr (OP == OP_FWD) {
+#pragma unroll
+    for (int v = 0; v < V; ++v) x_fwd(t, *pa[v], *pb[v]);
+  } else if constexpr (OP == OP_FWDDIFF) {
+    CT d;
+    ld_coef(tl + doff, e, G, j, d);
+#pragma unroll
+    for (int v = 0; v < V; ++v) x_fwddiff(t, d, *pa[v], *pb[v], *pga[v], *pgb[v]);
+  } else {
+    CT acc;
+    acc_zero(acc);
+#pragma unroll
+    for (int v = 0; v < V; ++v) x_bwd(t, *pa[v], *pb[v], *pga[v], *pgb[v], acc);
+    acc_stage(gl, e, G, j, r, acc);
+  }
+}
+
+// ---- layer with all pairs inside the lane: (a, a+SS), a = 2*SS*(e/SS) + e%SS
+template <int OP, int M, int V, bool REAL, int SS, typename F>
+__device__ __forceinline__ void layer_local(const float4* tl, int G, int j, int r, F (&u)[V][M], F (&w)[V][M],
+                                            float4* gl) {
+  const int doff = dt_off<REAL, M>(G);
+#pragma unroll
+  for (int e = 0; e < M / 2; ++e) {
+    const int a = 2 * SS * (e / SS) + (e % SS), b = a + SS;
+    F* pa[V]; F* pb[V]; F* pga[V]; F* pgb[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) { pa[v] = &u[v][a]; pb[v] = &u[v][b]; pga[v] = &w[v][a]; pgb[v] = &w[v][b]; }
+    entry<OP, V, REAL>(tl, doff, e, G, j, r, pa, pb, pga, pgb, gl);
+  }
+}
+
+// ---- nearest-neighbour layer with odd shift: pairs (2e+1, 2e+2) and the lane-boundary pair
+// (mode M-1 of lane j, mode 0 of lane j+1) computed by lane j (reference gpu/fwdprop.cu:98-106)
+template <int OP, int M, int V, bool REAL, typename F>
+__device__ __forceinline__ void layer_mis(const float4* tl, int G, int j, int r, F (&u)[V][M], F (&w)[V][M],
+                                          float4* gl) {
+  const int doff = dt_off<REAL, M>(G);
+  F nu[V], nw[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    nu[v] = shfl_down(u[v][0], 1, G);
+    if constexpr (OP != OP_FWD) nw[v] = shfl_down(w[v][0], 1, G);
+  }
+#pragma unroll
+  for (int e = 0; e < M / 2 - 1; ++e) {
+    F* pa[V]; F* pb[V]; F* pga[V]; F* pgb[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      pa[v] = &u[v][2 * e + 1]; pb[v] = &u[v][2 * e + 2]; pga[v] = &w[v][2 * e + 1]; pgb[v] = &w[v][2 * e + 2];
+    }
+    entry<OP, V, REAL>(tl, doff, e, G, j, r, pa, pb, pga, pgb, gl);
+  }
+  {
+    F* pa[V]; F* pb[V]; F* pga[V]; F* pgb[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) { pa[v] = &u[v][M - 1]; pb[v] = &nu[v]; pga[v] = &w[v][M - 1]; pgb[v] = &nw[v]; }
+    entry<OP, V, REAL>(tl, doff, M / 2 - 1, G, j, r, pa, pb, pga, pgb, gl);
+  }
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    const F bu = shfl_up(nu[v], 1, G);
+    if (j != 0) u[v][0] = bu;
+    if constexpr (OP != OP_FWD) {
+      const F bw = shfl_up(nw[v], 1, G);
+      if (j != 0) w[v][0] = bw;
+    }
+  }
+}
+
+__device__ __forceinline__ float2 fadd(float2 a, float2 b) { return cadd(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return a + b; }
+// staged row of the own mode m: (G_own,own, G_own,partner)
+__device__ __forceinline__ void stage_xl(float4* gl, int m, int G, int j, float2 aoo, float2 aop) {
+  gl[m * G + j] = make_float4(aoo.x, aoo.y, aop.x, aop.y);
+}
+__device__ __forceinline__ void stage_xl(float4* gl, int m, int G, int j, float aoo, float aop) {
+  reinterpret_cast<float2*>(&gl[(m >> 1) * G + j])[m & 1] = make_float2(aoo, aop);
+}
+
+// ---- butterfly layer whose stride spans lanes: partner lane j ^ d holds the paired mode at the
+// same register index; each lane computes its own output u' = c_self u + c_part u_partner.
+__device__ __forceinline__ void ld_xl(const float4* tl, int m, int G, int j, float2& cs, float2& cp) {
+  const float4 q = tl[m * G + j];
+  cs = make_float2(q.x, q.y); cp = make_float2(q.z, q.w);
+}
+__device__ __forceinline__ void ld_xl(const float4* tl, int m, int G, int j, float& cs, float& cp) {
+  const float4 q = tl[(m >> 1) * G + j];
+  if (m & 1) { cs = q.z; cp = q.w; } else { cs = q.x; cp = q.y; }
+}
+template <int OP, int M, int V, bool REAL, typename F>
+__device__ __forceinline__ void layer_xl(const float4* tl, int d, int G, int j, int r, F (&u)[V][M], F (&w)[V][M],
+                                         float4* gl) {
+  const int doff = dt_off<REAL, M>(G);
+#pragma unroll
+  for (int m = 0; m < M; ++m) {
+    F cs, cp;
+    ld_xl(tl, m, G, j, cs, cp);
+    if constexpr (OP == OP_FWD) {
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        const F ru = shfl_xor(u[v][m], d, G);
+        u[v][m] = cfma(cp, ru, cmul(cs, u[v][m]));
+      }
+    } else if constexpr (OP == OP_FWDDIFF) {
+      F ds, dp;
+      ld_xl(tl + doff, m, G, j, ds, dp);
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        const F ru = shfl_xor(u[v][m], d, G);
+        const F rw = shfl_xor(w[v][m], d, G);
+        w[v][m] = cfma(dp, ru, cfma(ds, u[v][m], cfma(cp, rw, cmul(cs, w[v][m]))));
+        u[v][m] = cfma(cp, ru, cmul(cs, u[v][m]));
+      }
+    } else {
+      // coefficients of the BWD tile are the own row of T^H
+      F aoo = fzero<F>(), aop = fzero<F>();
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        const F ry = shfl_xor(u[v][m], d, G);
+        const F rg = shfl_xor(w[v][m], d, G);
+        const F x = cfma(cp, ry, cmul(cs, u[v][m]));
+        const F rx = shfl_xor(x, d, G);
+        aoo = ccfma(w[v][m], x, aoo);
+        aop = ccfma(w[v][m], rx, aop);
+        w[v][m] = cfma(cp, rg, cmul(cs, w[v][m]));
+        u[v][m] = x;
+      }
+      for (int off = G; off < 32; off <<= 1) {
+        aoo = fadd(aoo, shfl_xor(aoo, off, 32));
+        aop = fadd(aop, shfl_xor(aop, off, 32));
+      }
+      if (r == 0) stage_xl(gl, m, G, j, aoo, aop);
+    }
+  }
+}
+
+// ---- field I/O: lane j of the vector's group owns modes [j*M, j*M+M); out-of-range modes read 0
+template <int M, int V, bool REAL, typename F>
+__device__ __forceinline__ void load_fields(F (&u)[V][M], const void* src, int vb0, int B, int N, int ldu, int j) {
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    const int b = vb0 + v;
+    const bool okb = (src != nullptr) && (b < B);
+    if constexpr (!REAL) {
+      const float4* p = reinterpret_cast<const float4*>(static_cast<const float2*>(src) + (size_t)b * ldu + j * M);
+#pragma unroll
+      for (int k = 0; k < M / 2; ++k) {
+        float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (okb && j * M + 2 * k < N) q = p[k];
+        u[v][2 * k] = make_float2(q.x, q.y);
+        u[v][2 * k + 1] = make_float2(q.z, q.w);
+      }
+    } else {
+      const float2* p = reinterpret_cast<const float2*>(static_cast<const float*>(src) + (size_t)b * ldu + j * M);
+#pragma unroll
+      for (int k = 0; k < M / 2; ++k) {
+        float2 q = make_float2(0.f, 0.f);
+        if (okb && j * M + 2 * k < N) q = p[k];
+        u[v][2 * k] = q.x;
+        u[v][2 * k + 1] = q.y;
+      }
+    }
+  }
+}
+template <int M, int V, bool REAL, typename F>
+__device__ __forceinline__ void store_fields(const F (&u)[V][M], void* dst, int vb0, int B, int N, int ldu, int j) {
+  if (dst == nullptr) return;
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    const int b = vb0 + v;
+    if (b >= B) continue;
+    if constexpr (!REAL) {
+      float4* p = reinterpret_cast<float4*>(static_cast<float2*>(dst) + (size_t)b * ldu + j * M);
+#pragma unroll
+      for (int k = 0; k < M / 2; ++k)
+        if (j * M + 2 * k < N) p[k] = make_float4(u[v][2 * k].x, u[v][2 * k].y, u[v][2 * k + 1].x, u[v][2 * k + 1].y);
+    } else {
+      float2* p = reinterpret_cast<float2*>(static_cast<float*>(dst) + (size_t)b * ldu + j * M);
+#pragma unroll
+      for (int k = 0; k < M / 2; ++k)
+        if (j * M + 2 * k < N) p[k] = make_float2(u[v][2 * k], u[v][2 * k + 1]);
+    }
+  }
+}
+
+// Shared-memory footprint of one launch (host and device agree on this layout):
+//   [ring: S*CL*layer_bytes][BWD: dT/dp chunk CL*dlayer_bytes][BWD: per-warp dJ/dT W*CL*Np/2*gslot]
+//   [mbarriers: S+1]
+__host__ __device__ inline size_t prop_smem_bytes(int op, bool real, int M, int G, int W, int CL, int S,
+                                                  unsigned layer_bytes, unsigned dlayer_bytes) {
+  size_t b = (size_t)S * CL * layer_bytes;
+  if (op == OP_BWD) {
+    const size_t np2 = (size_t)G * M / 2;
+    b += (size_t)CL * dlayer_bytes + (size_t)W * CL * np2 * (real ? 16 : 32);
+  }
+  return b + 8 * (size_t)(S + 1);
+}
+
+// ---- chunk-end gradient reduction (BWD): sum the W warps' staged dJ/dT of every slot of the chunk
+// in a fixed order, contract with dT/dp and write this CTA's partial (dJ/dp0, dJ/dp1).
+template <int M, bool REAL>
+__device__ __forceinline__ void chunk_reduce(const PropArgs& a, int lo, int nl, const unsigned char* gst,
+                                             const unsigned char* dbuf, int np2) {
+  const size_t gslot = REAL ? 16 : 32;
+  const size_t gst_layer = (size_t)np2 * gslot;
+  const int G = a.G;
+  for (int idx = threadIdx.x; idx < nl * np2; idx += blockDim.x) {
+    const int li = idx / np2, q = idx - li * np2;
+    const int l = lo + li;
+    const int kind = __ldg(a.kinds + l);
+    // locate the two staged rows of slot q: (lane, float4 index) for row 0 and row 1
+    int la, ia, lb, ib;   // lanes and entry indices
+    bool xl = kind >= KIND_XL;
+    int mrow_a = 0, mrow_b = 0;
+    if (!xl) {
+      la = lb = q / (M / 2);
+      const int e = q - la * (M / 2);
+      ia = REAL ? e : 2 * e;
+      ib = REAL ? e : 2 * e + 1;
+    } else {
+      const int st = 1 << (kind - KIND_XL);
+      const int ma = 2 * st * (q / st) + (q % st), mb = ma + st;
+      la = ma / M; lb = mb / M;
+      mrow_a = ma % M; mrow_b = mb % M;
+      ia = REAL ? (mrow_a >> 1) : mrow_a;
+      ib = REAL ? (mrow_b >> 1) : mrow_b;
+    }
+    float dth = 0.f, dph = 0.f;
+    if constexpr (!REAL) {
+      float4 ra = make_float4(0.f, 0.f, 0.f, 0.f), rb = ra;
+      for (int w = 0; w < a.W; ++w) {
+        const float4* gl = reinterpret_cast<const float4*>(gst + ((size_t)w * a.CL + li) * gst_layer);
+        const float4 x = gl[ia * G + la], y = gl[ib * G + lb];
+        ra.x += x.x; ra.y += x.y; ra.z += x.z; ra.w += x.w;
+        rb.x += y.x; rb.y += y.y; rb.z += y.z; rb.w += y.w;
+      }
+      // G = [[g00, g01], [g10, g11]]
+      float2 g00, g01, g10, g11;
+      if (!xl) {
+        g00 = make_float2(ra.x, ra.y); g01 = make_float2(ra.z, ra.w);
+        g10 = make_float2(rb.x, rb.y); g11 = make_float2(rb.z, rb.w);
+      } else {   // row a = (G_aa, G_ab), row b = (G_bb, G_ba)
+        g00 = make_float2(ra.x, ra.y); g01 = make_float2(ra.z, ra.w);
+        g11 = make_float2(rb.x, rb.y); g10 = make_float2(rb.z, rb.w);
+      }
+      const float4* D = reinterpret_cast<const float4*>(dbuf + (size_t)li * a.dlayer_bytes) + 4 * q;
+      const float4 d0r0 = D[0], d0r1 = D[1], d1r0 = D[2], d1r1 = D[3];
+      dth = d0r0.x * g00.x - d0r0.y * g00.y + d0r0.z * g01.x - d0r0.w * g01.y +
+            d0r1.x * g10.x - d0r1.y * g10.y + d0r1.z * g11.x - d0r1.w * g11.y;
+      dph = d1r0.x * g00.x - d1r0.y * g00.y + d1r0.z * g01.x - d1r0.w * g01.y +
+            d1r1.x * g10.x - d1r1.y * g10.y + d1r1.z * g11.x - d1r1.w * g11.y;
+    } else {
+      float4 ra = make_float4(0.f, 0.f, 0.f, 0.f), rb = ra;
+      for (int w = 0; w < a.W; ++w) {
+        const float4* gl = reinterpret_cast<const float4*>(gst + ((size_t)w * a.CL + li) * gst_layer);
+        const float4 x = gl[ia * G + la], y = gl[ib * G + lb];
+        ra.x += x.x; ra.y += x.y; ra.z += x.z; ra.w += x.w;
+        rb.x += y.x; rb.y += y.y; rb.z += y.z; rb.w += y.w;
+      }
+      float g00, g01, g10, g11;
+      if (!xl) {
+        g00 = ra.x; g01 = ra.y; g10 = ra.z; g11 = ra.w;
+      } else {
+        const float2 A = (mrow_a & 1) ? make_float2(ra.z, ra.w) : make_float2(ra.x, ra.y);
+        const float2 Bq = (mrow_b & 1) ? make_float2(rb.z, rb.w) : make_float2(rb.x, rb.y);
+        g00 = A.x; g01 = A.y; g11 = Bq.x; g10 = Bq.y;
+      }
+      const float4 D = reinterpret_cast<const float4*>(dbuf + (size_t)li * a.dlayer_bytes)[q];
+      dth = D.x * g00 + D.y * g01 + D.z * g10 + D.w * g11;
+    }
+    a.partial[((size_t)blockIdx.x * a.L + l) * np2 + q] = make_float2(dth, dph);
+  }
+}
+
+template <int OP, int M, int V, bool REAL>
+struct PropTraits {
+  static constexpr int kMaxThreads = (OP == OP_FWD && M * V <= 16) ? 512 : 256;
+};
+
+template <int OP, int M, int V, bool REAL>
+__global__ void __launch_bounds__(PropTraits<OP, M, V, REAL>::kMaxThreads)
+prop_kernel(const PropArgs a) {
+  using F = typename Fld<REAL>::T;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int G = a.G, j = lane & (G - 1), r = lane >> a.logG, R = 32 >> a.logG;
+  const int np2 = (G * M) >> 1;
+  const int vb0 = blockIdx.x * (a.W * R * V) + (warp * R + r) * V;
+
+  const size_t ring_bytes = (size_t)a.S * a.CL * a.layer_bytes;
+  const size_t dbuf_bytes = (OP == OP_BWD) ? (size_t)a.CL * a.dlayer_bytes : 0;
+  const size_t gst_layer = (size_t)np2 * (REAL ? 16 : 32);
+  const size_t gst_bytes = (OP == OP_BWD) ? (size_t)a.W * a.CL * gst_layer : 0;
+  unsigned char* ring = smem;
+  unsigned char* dbuf = smem + ring_bytes;
+  unsigned char* gst = dbuf + dbuf_bytes;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(gst + gst_bytes);   // [S] ring, [S] = dT/dp buffer
+
+  F u[V][M];
+  F w[V][M];
+  load_fields<M, V, REAL>(u, a.in0, vb0, a.B, a.N, a.ldu, j);
+  if constexpr (OP != OP_FWD) load_fields<M, V, REAL>(w, a.in1, vb0, a.B, a.N, a.ldu, j);
+
+  const int nch = (a.L + a.CL - 1) / a.CL;
+  if (tid == 0) {
+    for (int s = 0; s <= a.S; ++s) mbar_init(smem_u32(bars + s), 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  auto chunk_lo = [&](int c) { return (OP == OP_BWD) ? max(0, a.L - (c + 1) * a.CL) : c * a.CL; };
+  auto chunk_hi = [&](int c) { return (OP == OP_BWD) ? a.L - c * a.CL : min(a.L, (c + 1) * a.CL); };
+  auto issue = [&](int c) {
+    const int lo = chunk_lo(c), hi = chunk_hi(c);
+    const unsigned bytes = (unsigned)(hi - lo) * a.layer_bytes;
+    const uint32_t bar = smem_u32(bars + (c % a.S));
+    mbar_arrive_expect_tx(bar, bytes);
+    tma_load_1d(smem_u32(ring + (size_t)(c % a.S) * a.CL * a.layer_bytes), a.tiles + (size_t)lo * a.layer_bytes,
+                bytes, bar);
+  };
+  auto issue_d = [&](int c) {
+    const int lo = chunk_lo(c), hi = chunk_hi(c);
+    const unsigned bytes = (unsigned)(hi - lo) * a.dlayer_bytes;
+    const uint32_t bar = smem_u32(bars + a.S);
+    mbar_arrive_expect_tx(bar, bytes);
+    tma_load_1d(smem_u32(dbuf), a.dtiles + (size_t)lo * a.dlayer_bytes, bytes, bar);
+  };
+  int issued = 0;
+  if (tid == 0) {
+    for (; issued < min(a.S, nch); ++issued) issue(issued);
+  }
+
+  for (int c = 0; c < nch; ++c) {
+    const int lo = chunk_lo(c), hi = chunk_hi(c);
+    const bool ok = mbar_wait_bounded(smem_u32(bars + (c % a.S)), (uint32_t)((c / a.S) & 1));
+    if (__syncthreads_or(!ok)) {
+      // give up: record, wait (bounded) for the copies still in flight, leave
+      if (tid == 0) {
+        set_status(a.status, ST_TIMEOUT);
+        for (int cc = c + 1; cc < issued; ++cc) mbar_wait_bounded(smem_u32(bars + (cc % a.S)), (uint32_t)((cc / a.S) & 1));
+      }
+      return;
+    }
+    if constexpr (OP == OP_BWD) {
+      if (tid == 0) issue_d(c);
+    }
+    const unsigned char* st = ring + (size_t)(c % a.S) * a.CL * a.layer_bytes;
+    const int nl = hi - lo;
+    for (int i = 0; i < nl; ++i) {
+      const int l = (OP == OP_BWD) ? (hi - 1 - i) : (lo + i);
+      const int li = l - lo;
+      const int kind = __ldg(a.kinds + l);
+      const float4* tl = reinterpret_cast<const float4*>(st + (size_t)li * a.layer_bytes);
+      float4* gl = reinterpret_cast<float4*>(gst + ((size_t)warp * a.CL + li) * gst_layer);
+      switch (kind) {
+        case 0: layer_local<OP, M, V, REAL, 1>(tl, G, j, r, u, w, gl); break;
+        case 1: if constexpr (M >= 4) layer_local<OP, M, V, REAL, 2>(tl, G, j, r, u, w, gl); break;
+        case 2: if constexpr (M >= 8) layer_local<OP, M, V, REAL, 4>(tl, G, j, r, u, w, gl); break;
+        case 3: if constexpr (M >= 16) layer_local<OP, M, V, REAL, 8>(tl, G, j, r, u, w, gl); break;
+        case KIND_MIS: layer_mis<OP, M, V, REAL>(tl, G, j, r, u, w, gl); break;
+        default: {
+          const int d = 1 << (kind - KIND_XL - ilog2_const(M));
+          layer_xl<OP, M, V, REAL>(tl, d, G, j, r, u, w, gl);
+        }
+      }
+    }
+    __syncthreads();
+    if constexpr (OP == OP_BWD) {
+      const bool okd = mbar_wait_bounded(smem_u32(bars + a.S), (uint32_t)(c & 1));
+      if (__syncthreads_or(!okd)) {
+        if (tid == 0) {
+          set_status(a.status, ST_TIMEOUT);
+          for (int cc = c + 1; cc < issued; ++cc) mbar_wait_bounded(smem_u32(bars + (cc % a.S)), (uint32_t)((cc / a.S) & 1));
+        }
+        return;
+      }
+      chunk_reduce<M, REAL>(a, lo, nl, gst, dbuf, np2);
+    }
+    if (tid == 0 && issued < nch) issue(issued++);
+  }
+  (void)R;
+  store_fields<M, V, REAL>(u, a.out0, vb0, a.B, a.N, a.ldu, j);
+  if constexpr (OP != OP_FWD) store_fields<M, V, REAL>(w, a.out1, vb0, a.B, a.N, a.ldu, j);
+}
+
+}  // namespace mg

@@ -1,0 +1,166 @@
+"""Generate the golden fixtures in this folder by running the REFERENCE implementation itself.
+
+Run from the repository root, in a container where the reference tree is mounted:
+
+    make -C oracle ref                      # compiles the reference's c/dot.cpp into oracle/_ref/dot.so
+    python tests/golden/make_golden.py [/path/to/reference]
+
+The reference package (``mesh.py`` + ``crossing.py`` + geometry classes) is imported from its own tree
+with two stand-ins that the survey found necessary: ``numba.njit`` as the identity and an empty
+``matplotlib.pyplot`` (neither library is on the path).  Its C backend (``mesh.py:82-95``) is pointed at
+``oracle/_ref/dot.so``, so every number stored here comes from the reference's own
+``StructuredMeshNetwork.dot`` / ``dot_vjp`` (complex128, ``mesh.py:351-392``) and its complex64
+``meshdot_helper32`` (``mesh.py:97-113``).  Back-propagation runs with one OpenMP thread
+(``mesh.OMP_THREADS = 1``) because the reference's threaded mode-2 reduction races (``c/dot.cpp:135,
+281-284``).
+
+Fixtures are small ``.npz`` files; fields are stored (B, N), parameters in the GPU grid layout
+(L, N//2, n_p) used by ``gpu/mesh.py:77-81``.
+"""
+import ctypes
+import importlib.util
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from oracle.meshes_oracle import flat_to_grid, butterfly_strides  # noqa: E402
+
+
+def import_reference(path):
+    nb = types.ModuleType("numba")
+    nb.njit = lambda *a, **k: (a[0] if a and callable(a[0]) else (lambda f: f))
+    sys.modules["numba"] = nb
+    mpl = types.ModuleType("matplotlib")
+    plt = types.ModuleType("matplotlib.pyplot")
+    mpl.pyplot = plt
+    sys.modules["matplotlib"] = mpl
+    sys.modules["matplotlib.pyplot"] = plt
+    spec = importlib.util.spec_from_file_location("meshes", os.path.join(path, "__init__.py"),
+                                                  submodule_search_locations=[path])
+    m = importlib.util.module_from_spec(spec)
+    sys.modules["meshes"] = m
+    spec.loader.exec_module(m)
+    mm = sys.modules["meshes.mesh"]
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "dot.so"))
+    for name in ("meshdot_helper32", "meshdot_helper64"):
+        h = getattr(lib, name)
+        h.argtypes = (ctypes.c_int,) * 4 + (ctypes.c_void_p,) * 10 + (ctypes.c_int,) * 4
+        setattr(mm, name, h)
+    mm.BACKEND = "c"
+    mm.OMP_THREADS = 1
+    return m
+
+
+def main(ref_path):
+    meshes = import_reference(ref_path)
+    mm = sys.modules["meshes.mesh"]
+    from meshes.clements import ClementsNetwork
+    from meshes.reck import ReckNetwork
+    from meshes.butterfly import ButterflyNetwork
+    from meshes.crossing import MZICrossing, SymCrossing
+
+    rng = np.random.default_rng(20240501)
+    written = []
+
+    def save(name, **kw):
+        fn = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(fn, **kw)
+        written.append(fn)
+
+    def nn_case(name, net, N, B, crossing="mzi", diff=True):
+        n_p, n_s = {"mzi": (2, 2), "sym": (2, 1)}[crossing]
+        lens, shifts = list(map(int, net.lens)), list(map(int, net.shifts))
+        n_cr = sum(lens)
+        # float32-representable parameters so the GPU grid holds them exactly
+        p_cr = rng.uniform(0, 2 * np.pi, (n_cr, n_p)).astype(np.float32).astype(np.float64)
+        net.p_phase[:n_cr * n_p] = p_cr.reshape(-1)
+        if net.is_phase:
+            net.p_phase[n_cr * n_p:] = 0.0
+        if net.p_splitter.ndim:
+            sp = net.p_splitter.astype(np.float32).astype(np.float64)
+            net.p_splitter = sp
+        x = (rng.standard_normal((B, N)) + 1j * rng.standard_normal((B, N)))
+        x /= np.linalg.norm(x, axis=1, keepdims=True)
+        y = net.dot(x.T).T
+        out = dict(N=N, L=len(lens), crossing=crossing, lens=np.array(lens), shifts=np.array(shifts),
+                   p=flat_to_grid(p_cr, lens, shifts, N, n_p),
+                   x=x, y=y)
+        if net.p_splitter.ndim:
+            out["s"] = flat_to_grid(net.p_splitter.reshape(n_cr, n_s), lens, shifts, N, n_s)
+        if diff:
+            dp_cr = rng.standard_normal((n_cr, n_p))
+            dp_full = np.zeros(net.n_phase)
+            dp_full[:n_cr * n_p] = dp_cr.reshape(-1)
+            y2, dy = net.dot(x.T, dp=dp_full)
+            out["dp_dir"] = flat_to_grid(dp_cr, lens, shifts, N, n_p)
+            out["dy"] = dy.T
+            t = (rng.standard_normal((B, N)) + 1j * rng.standard_normal((B, N)))
+            g = 2 * (y - t)
+            dJdp, dJdv = net.dot_vjp(y.T, g.T)
+            out["g"] = g
+            out["dJdp"] = flat_to_grid(dJdp[:n_cr * n_p].reshape(n_cr, n_p), lens, shifts, N, n_p)
+            out["g_in"] = dJdv.T
+            # complex64 arithmetic of the reference C backend (meshdot_helper32) on the same forward
+            T = np.ascontiguousarray(net.X.T(p_cr, net.p_splitter if net.p_splitter.ndim else 0.))
+            inds = np.array(net.inds, dtype=np.int32)
+            v32 = np.ascontiguousarray(x.T.astype(np.complex64))
+            ph = np.zeros(N, dtype=np.float32)
+            mm.meshdot_helper_c(T.astype(np.complex64), np.empty((0, 0, 0), np.complex64), ph[:0],
+                                np.empty((0,), np.float32), v32, np.empty((0, 0), np.complex64), inds,
+                                np.array(lens, np.int32), np.array(shifts, np.int32), np.empty((0, 0), np.int32),
+                                -1, 0)
+            out["y_c64"] = v32.T
+        save(name, **out)
+
+    # Clements, MZI with splitter errors
+    N = 8
+    net = ClementsNetwork(N=N, is_phase=False, phi_out=None, p_splitter=rng.normal(0, 0.02, (N * (N - 1) // 2, 2)))
+    nn_case("clements_mzi_N8_split", net, N, 5)
+    # Clements, ideal splitters, odd batch
+    N = 16
+    net = ClementsNetwork(N=N, is_phase=False, phi_out=None)
+    nn_case("clements_mzi_N16", net, N, 7)
+    # Clements N=64 (the plain-forward shape with a small batch)
+    N = 64
+    net = ClementsNetwork(N=N, is_phase=False, phi_out=None, p_splitter=rng.normal(0, 0.02, (N * (N - 1) // 2, 2)))
+    nn_case("clements_mzi_N64_split", net, N, 16)
+    # Reck triangle, splitter errors
+    N = 10
+    net = ReckNetwork(N=N, p_splitter=rng.normal(0, 0.02, (N * (N - 1) // 2, 2)))
+    nn_case("reck_mzi_N10_split", net, N, 6)
+    # symmetric crossing (forward only: the reference CPU SymCrossing has no dT)
+    N = 8
+    net = ClementsNetwork(N=N, is_phase=False, phi_out=None, X=SymCrossing(),
+                          p_splitter=rng.normal(0, 0.02, (N * (N - 1) // 2, 1)))
+    nn_case("clements_sym_N8_split", net, N, 4, crossing="sym", diff=False)
+
+    # Butterfly (reference form: N-1 layers of adjacent MZIs between permutations)
+    N = 16
+    bf = ButterflyNetwork(N=N, p_splitter=rng.normal(0, 0.02, (N // 2 * (N - 1), 2)))
+    L = N - 1
+    n_cr = L * (N // 2)
+    p_cr = rng.uniform(0, 2 * np.pi, (n_cr, 2)).astype(np.float32).astype(np.float64)
+    bf.p_phase[:n_cr * 2] = p_cr.reshape(-1)
+    bf.p_phase[n_cr * 2:] = 0.0
+    bf.p_splitter = bf.p_splitter.astype(np.float32).astype(np.float64)
+    B = 6
+    x = (rng.standard_normal((B, N)) + 1j * rng.standard_normal((B, N)))
+    x /= np.linalg.norm(x, axis=1, keepdims=True)
+    y = bf.dot(x.T).T
+    t = (rng.standard_normal((B, N)) + 1j * rng.standard_normal((B, N)))
+    g = 2 * (y - t)
+    dJdp, dJdv = bf.dot_vjp(y.T, g.T)
+    save("butterfly_mzi_N16_split", N=N, L=L, crossing="mzi", strides=np.array(butterfly_strides(N)),
+         p=p_cr.reshape(L, N // 2, 2), s=bf.p_splitter.reshape(L, N // 2, 2), x=x, y=y, g=g,
+         dJdp=dJdp[:n_cr * 2].reshape(L, N // 2, 2), g_in=dJdv.T)
+
+    print("wrote", *written, sep="\n  ")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

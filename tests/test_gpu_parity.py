@@ -1,0 +1,248 @@
+"""GPU parity: the sm_103a kernels (through the C ABI, via MeshNetworkGPU) against the complex128
+oracle and the reference-generated golden fixtures.
+
+Tolerances (relative Frobenius error ||gpu - ref|| / ||ref||):
+  * forward fields, forward derivatives, input gradients, reconstructed inputs: 1e-5
+  * parameter gradients dJ/dp: 1e-5 against the exact complex128 adjoint; 2e-4 against central
+    differences (their own truncation/rounding error at h=1e-6 dominates there)
+"""
+import os
+import zlib
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import meshes_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+TOL = 1e-5
+
+
+def gpu_mesh(om: "O.OracleMesh", **kw):
+    from meshes_gb300 import MeshNetworkGPU
+    p = np.asarray(om.p, dtype=np.float32).reshape(-1)
+    s = None if om.s is None else np.asarray(om.s, dtype=np.float32)
+    if om.fft:
+        return MeshNetworkGPU(om.N, om.L, None, None, p, s, om.crossing, is_phase=False, strides=om.strides, **kw)
+    return MeshNetworkGPU(om.N, om.L, om.lens, om.shifts, p, s, om.crossing, is_phase=False, **kw)
+
+
+def to_dev(x, real=False):
+    """(B, N) numpy -> (N, B) device tensor with contiguous columns (the reference layout)."""
+    dt = np.float32 if real else np.complex64
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(x).astype(dt))).cuda().t()
+
+
+def to_np(t):
+    return t.t().contiguous().cpu().numpy()
+
+
+def fixtures():
+    return sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+
+
+def load_fixture(name):
+    z = np.load(os.path.join(GOLDEN, name))
+    kw = dict(lens=z["lens"].tolist(), shifts=z["shifts"].tolist()) if "lens" in z else dict(strides=z["strides"].tolist())
+    om = O.OracleMesh(N=int(z["N"]), L=int(z["L"]), crossing=str(z["crossing"]), p=z["p"],
+                      s=z["s"] if "s" in z else None, **kw)
+    return z, om
+
+
+@pytest.mark.parametrize("name", fixtures())
+def test_golden_forward(name):
+    z, om = load_fixture(name)
+    m = gpu_mesh(om)
+    y = to_np(m.dot(to_dev(z["x"])))
+    assert O.rel_err(y, z["y"]) < TOL
+    assert m.status() == 0
+
+
+@pytest.mark.parametrize("name", [f for f in fixtures() if "sym" not in f])
+def test_golden_backward(name):
+    z, om = load_fixture(name)
+    m = gpu_mesh(om)
+    dp, gin = m.grad_phi(to_dev(z["y"]), to_dev(z["g"]), vpos="out")
+    dp = dp.cpu().numpy().reshape(om.L, om.N // 2, 2)
+    assert O.rel_err(dp, z["dJdp"]) < TOL
+    assert O.rel_err(to_np(gin), z["g_in"]) < TOL
+
+
+@pytest.mark.parametrize("name", [f for f in fixtures() if "dy" in np.load(os.path.join(GOLDEN, f))])
+def test_golden_fwddiff(name):
+    z, om = load_fixture(name)
+    m = gpu_mesh(om)
+    y, dy = m.dot(to_dev(z["x"]), dp=z["dp_dir"].astype(np.float32).reshape(-1))
+    assert O.rel_err(to_np(y), z["y"]) < TOL
+    assert O.rel_err(to_np(dy), z["dy"]) < TOL
+
+
+CASES = [
+    # (geometry, crossing, N, B, splitter sigma)
+    ("clements", "mzi", 2, 3, 0.02), ("clements", "mzi", 4, 5, 0.0), ("clements", "mzi", 6, 1, 0.02),
+    ("clements", "mzi", 8, 33, 0.02), ("clements", "mzi", 10, 7, 0.02), ("clements", "mzi", 30, 17, 0.02),
+    ("clements", "mzi", 64, 65, 0.02), ("clements", "mzi", 100, 9, 0.02), ("clements", "mzi", 128, 40, 0.02),
+    ("clements", "mzi", 200, 5, 0.01), ("clements", "mzi", 256, 37, 0.02), ("clements", "mzi", 512, 6, 0.02),
+    ("reck", "mzi", 8, 9, 0.02), ("reck", "mzi", 64, 31, 0.02), ("reck", "mzi", 130, 3, 0.0),
+    ("clements", "sym", 16, 11, 0.02), ("clements", "sym", 96, 10, 0.02), ("reck", "sym", 32, 4, 0.0),
+    ("clements", "orth", 8, 13, 0.0), ("clements", "orth", 64, 50, 0.0), ("reck", "orth", 34, 8, 0.0),
+    ("clements", "orth", 256, 9, 0.0),
+    ("fft", "mzi", 8, 5, 0.02), ("fft", "mzi", 64, 21, 0.02), ("fft", "mzi", 256, 9, 0.02),
+    ("fft", "mzi", 512, 4, 0.02), ("butterfly", "mzi", 16, 7, 0.02), ("butterfly", "mzi", 64, 12, 0.02),
+    ("fft", "sym", 128, 6, 0.02), ("fft", "orth", 32, 10, 0.0), ("fft", "orth", 256, 3, 0.0),
+    ("butterfly", "orth", 32, 5, 0.0),
+]
+
+
+def _case(geo, cr, N, B, sig, seed):
+    rng = np.random.default_rng(seed)
+    om = O.random_mesh(rng, N, geo, cr, sig)
+    real = cr == "orth"
+    x = O.unit_columns(rng, N, B, real=real)
+    t = O.unit_columns(rng, N, B, real=real)
+    return rng, om, real, x, t
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: "%s-%s-N%d-B%d" % c[:4])
+def test_random_forward(case):
+    rng, om, real, x, t = _case(*case, seed=zlib.crc32(repr(case).encode()))
+    m = gpu_mesh(om)
+    y = to_np(m.dot(to_dev(x, real)))
+    ref = O.propagate(om, x)
+    assert O.rel_err(y, ref) < TOL
+    assert m.status() == 0
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: "%s-%s-N%d-B%d" % c[:4])
+def test_random_backward(case):
+    rng, om, real, x, t = _case(*case, seed=zlib.crc32(repr(case).encode()) + 1)
+    m = gpu_mesh(om)
+    y = O.propagate(om, x)
+    g = 2 * (y - t)
+    G, xrec, g_in = O.vjp_unitary(om, y, g)
+    dp_ref = O.contract_dp(om, G)
+    dp, gin = m.grad_phi(to_dev(y, real), to_dev(g, real), vpos="out")
+    n_p = O.CROSSINGS[om.crossing][0]
+    dp = dp.cpu().numpy().reshape(om.L, om.N // 2, n_p)
+    assert O.rel_err(dp, dp_ref) < TOL
+    assert O.rel_err(to_np(gin), g_in) < TOL
+    assert m.status() == 0
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: "%s-%s-N%d-B%d" % c[:4])
+def test_random_fwddiff(case):
+    rng, om, real, x, t = _case(*case, seed=zlib.crc32(repr(case).encode()) + 2)
+    m = gpu_mesh(om)
+    n_p = O.CROSSINGS[om.crossing][0]
+    dpdir = rng.standard_normal((om.L, om.N // 2, n_p)).astype(np.float32)
+    dx = O.unit_columns(rng, om.N, x.shape[0], real=real)
+    y_ref, dy_ref = O.fwddiff(om, x, dpdir, dx)
+    y, dy = m.dot(to_dev(x, real), dp=dpdir.reshape(-1), dv=to_dev(dx, real))
+    assert O.rel_err(to_np(y), y_ref) < TOL
+    assert O.rel_err(to_np(dy), dy_ref) < TOL
+
+
+def test_random_nn_layouts():
+    """Random shifts and lens per layer, odd shifts included (reference gpu/test.py:32-42)."""
+    rng = np.random.default_rng(7)
+    for N in (16, 128, 254):
+        L = 13
+        shifts = rng.integers(0, N - 1, L)
+        lens = np.array([rng.integers(0, (N - s) // 2 + 1) for s in shifts])
+        p = rng.uniform(0, 2 * np.pi, (L, N // 2, 2)).astype(np.float32)
+        s = rng.normal(0, 0.1, (L, N // 2, 2)).astype(np.float32)
+        om = O.OracleMesh(N=N, L=L, crossing="mzi", lens=lens.tolist(), shifts=shifts.tolist(), p=p, s=s)
+        x = O.unit_columns(rng, N, 19)
+        m = gpu_mesh(om)
+        assert O.rel_err(to_np(m.dot(to_dev(x))), O.propagate(om, x)) < TOL
+        y = O.propagate(om, x)
+        g = rng.standard_normal(y.shape) + 1j * rng.standard_normal(y.shape)
+        G, _, gin_ref = O.vjp_unitary(om, y, g)
+        dp, gin = m.grad_phi(to_dev(y), to_dev(g), vpos="out")
+        assert O.rel_err(dp.cpu().numpy().reshape(L, N // 2, 2), O.contract_dp(om, G)) < TOL
+        assert O.rel_err(to_np(gin), gin_ref) < TOL
+
+
+def test_plain_forward_full_size():
+    """Plain forward at the full N=64, L=64, B=1024 Clements shape (seed 1000)."""
+    rng = np.random.default_rng(1000)
+    om = O.random_mesh(rng, 64, "clements", "mzi", 0.0)
+    x = O.unit_columns(rng, 64, 1024)
+    m = gpu_mesh(om)
+    y = to_np(m.dot(to_dev(x)))
+    ref = O.propagate(om, x)
+    err = O.rel_err(y, ref)
+    U = to_np(m.matrix())
+    unit = np.linalg.norm(U.conj().T @ U - np.eye(64))
+    print("rel err %.2e  ||UU^H - I|| %.2e" % (err, unit))
+    assert err < TOL
+    assert unit < 1e-4
+
+
+def test_determinism_and_inplace():
+    rng = np.random.default_rng(3)
+    om = O.random_mesh(rng, 128, "clements", "mzi", 0.02)
+    x = O.unit_columns(rng, 128, 300)
+    m = gpu_mesh(om)
+    v = to_dev(x)
+    y1 = m.dot(v)
+    g = to_dev(rng.standard_normal(x.shape) + 1j * rng.standard_normal(x.shape))
+    dp1, gi1 = m.grad_phi(y1, g, vpos="out")
+    dp2, gi2 = m.grad_phi(y1, g, vpos="out")
+    assert torch.equal(dp1, dp2) and torch.equal(gi1, gi2)
+    v2 = v.clone()
+    m.dot(v2, out=v2)             # in place
+    assert torch.equal(v2, y1)
+
+
+def test_edge_sizes():
+    from meshes_gb300 import MeshNetworkGPU
+    rng = np.random.default_rng(5)
+    om = O.random_mesh(rng, 16, "clements", "mzi", 0.0)
+    m = gpu_mesh(om)
+    v0 = torch.zeros((16, 0), dtype=torch.complex64, device="cuda")
+    assert m.dot(v0).shape == (16, 0)
+    # L = 0 is the identity
+    m0 = MeshNetworkGPU(16, 0, [], [], np.zeros(0, np.float32), None, "mzi", is_phase=False)
+    x = O.unit_columns(rng, 16, 4)
+    assert np.allclose(to_np(m0.dot(to_dev(x))), x)
+    # accumulate semantics of grad_phi(out_dp=...)
+    y = O.propagate(om, x)
+    g = 2 * y
+    dp_a, _ = m.grad_phi(to_dev(y), to_dev(g), vpos="out")
+    acc = torch.ones_like(dp_a)
+    m.grad_phi(to_dev(y), to_dev(g), vpos="out", out_dp=acc)
+    assert torch.allclose(acc, dp_a + 1, atol=1e-6)
+
+
+def test_bad_geometry_reports_status():
+    """Malformed device geometry (shift + 2*len > N) is caught by the kernel, not a fault."""
+    from meshes_gb300 import _lib
+    lib = _lib.load()
+    N, L, B = 8, 2, 4
+    lens = torch.tensor([4, 4], dtype=torch.int32, device="cuda")
+    shifts = torch.tensor([0, 1], dtype=torch.int32, device="cuda")   # layer 1: 1 + 8 > 8
+    p = torch.zeros(L * N // 2 * 2, device="cuda")
+    u = torch.zeros((B, N), dtype=torch.complex64, device="cuda")
+    out = torch.empty_like(u)
+    nb = lib.mg_workspace_bytes(0, N, L, B, 0, 0, None)
+    ws = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    assert lib.mg_workspace_init(ws.data_ptr(), nb, st) == 0
+    assert lib.mg_fwdprop(N, L, B, lens.data_ptr(), shifts.data_ptr(), p.data_ptr(), N, None, 0, u.data_ptr(),
+                          out.data_ptr(), N, 0, ws.data_ptr(), nb, st) == 0
+    assert lib.mg_read_status(ws.data_ptr(), 1, st) == 2
+    assert lib.mg_read_status(ws.data_ptr(), 0, st) == 0
+
+
+def test_argument_errors():
+    from meshes_gb300 import _lib
+    lib = _lib.load()
+    st = torch.cuda.current_stream().cuda_stream
+    assert lib.mg_fwdprop(7, 1, 1, None, None, None, 0, None, 0, None, None, 7, 0, None, 0, st) == -1
+    assert "even" in _lib.last_error()
+    assert lib.mg_fwdprop(1024, 1, 1, None, None, None, 0, None, 0, None, None, 1024, 0, None, 0, st) == -1
+    assert lib.mg_fwdprop(8, 1, 1, None, None, None, 0, None, 0, None, None, 8, 0, None, 0, st) == -2
