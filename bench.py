@@ -1,0 +1,376 @@
+"""Benchmark of the mesh-propagation hot path on GB300.
+
+Workload (one "step"): forward propagation plus back-propagation of phase gradients through an
+imperfect Clements MZI mesh, N=256 modes, L=256 layers (32640 MZIs), splitting errors
+alpha, beta ~ N(0, 0.02), B=4096 complex64 unit-norm input vectors, loss J = sum |y - y_t|^2:
+  mg_fwdprop (x -> y), g = 2 (y - y_t), mg_backdiff (y, g -> dJ/dp, dJ/dx*).
+Metric: MZI applications per second for fwd+bwd (n_MZI * B per step), with the fraction of the FP32
+CUDA-core peak at the reference's own FLOP counts (32 per MZI-application forward, 96 backward).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank runs an independent replica on its own GPU (the path needs no
+collective); value = all ranks' MZI applications / max-over-ranks time.  ``--impl reference`` times
+the reference algorithm's CPU implementation (the oracle's C++ port of c/dot.cpp, all host threads)
+on the same workload, on rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N, B, SIGMA, SEED = 256, 4096, 0.02, 1002
+FLOP_FWD, FLOP_BWD = 32, 96           # reference gpu/test.py:208,220
+METRIC = "MZI-apps/s (fwd+bwd)"
+WORKLOAD = "clements_mzi_N256_L256_B4096_fwd+bwd"
+
+
+def host_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:   # pragma: no cover
+        return os.cpu_count() or 1
+
+
+def make_problem():
+    """Seeded synthetic mesh and fields (numpy), independent of the oracle."""
+    from meshes_gb300 import geometry as gm
+    rng = np.random.default_rng(SEED)
+    lens, shifts = gm.clements(N)
+    L = len(lens)
+    mask = gm.active_mask_nn(N, lens, shifts)
+    p = rng.uniform(0, 2 * np.pi, (L, N // 2, 2)).astype(np.float32)
+    s = rng.normal(0, SIGMA, (L, N // 2, 2)).astype(np.float32)
+    p[~mask] = 0
+    s[~mask] = 0
+
+    def unit(rows):
+        x = rng.standard_normal((rows, N)) + 1j * rng.standard_normal((rows, N))
+        return (x / np.linalg.norm(x, axis=1, keepdims=True)).astype(np.complex64)
+
+    x = unit(B)
+    yt = unit(B)
+    return lens, shifts, p, s, x, yt, int(mask.sum())
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def gpu_id(torch, dev) -> str:
+    """nvidia-smi -i selector of this process's GPU (PCI bus id when torch exposes it)."""
+    pr = torch.cuda.get_device_properties(dev)
+    try:
+        return "%08x:%02x:%02x.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+    except AttributeError:
+        return str(dev.index or 0)
+
+
+def cpu_baseline(problem, seconds=10.0):
+    """Reference algorithm on the host cores: the oracle's C++ port of c/dot.cpp (complex64, OpenMP),
+    forward (mode 0) + back-propagation (mode 2) on a bounded sample of the batch."""
+    from oracle import meshes_oracle as O
+    from oracle import port as P
+    lens, shifts, p, s, x, yt, n_mzi = problem
+    om = O.OracleMesh(N=N, L=len(lens), crossing="mzi", lens=lens, shifts=shifts, p=p, s=s)
+    fns = P.port_lib()
+    threads = host_threads()
+    bs = max(8, min(B, 16 * threads))
+    xs, ts = x[:bs], yt[:bs]
+    t0 = time.perf_counter()
+    reps, work = 0, 0.0
+    while True:
+        a = time.perf_counter()
+        y = P.forward(fns, om, xs, threads=threads, dtype=np.complex64)
+        P.vjp(fns, om, y, 2 * (y - ts), threads=threads, dtype=np.complex64)
+        work += time.perf_counter() - a
+        reps += 1
+        if time.perf_counter() - t0 > seconds and reps >= 2:
+            break
+    rate = n_mzi * bs * reps / work
+    return {"value": rate, "unit": "MZI-apps/s", "cores": threads, "kind": "port",
+            "sample": "%d of the %d vectors, fwd (mode 0) + bwd (mode 2), %d repeats, %.1f s" % (bs, B, reps, work)}
+
+
+def traffic_from_profiles(name: str):
+    """dram bytes per launch recorded in profiles/<name> ('dram_bytes_per_launch: X'), else None."""
+    fn = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(fn):
+            if line.strip().startswith("dram_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    problem = make_problem()
+    n_mzi = problem[6]
+    per_step = max(2.0, 60.0 / max(args.steps + args.warmup, 1))
+    for _ in range(args.warmup):
+        cpu_baseline(problem, seconds=0.5)
+    vals = []
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(problem, seconds=per_step))
+    value = statistics.median(v["value"] for v in vals)
+    cb = dict(vals[0])
+    cb["value"] = value
+    line = {"metric": METRIC, "value": value, "unit": "MZI-apps/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * n_mzi * B / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "N": N, "L": N, "B": B, "n_mzi": n_mzi, "splitter_sigma": SIGMA},
+            "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": "MZI-apps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+
+    from meshes_gb300 import _lib
+    lib = _lib.load()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.current_stream(dev)
+    st = stream.cuda_stream
+
+    lens, shifts, p, s, x_h, yt_h, n_mzi = make_problem()
+    L = len(lens)
+    lens_d = torch.tensor(lens, dtype=torch.int32, device=dev)
+    shifts_d = torch.tensor(shifts, dtype=torch.int32, device=dev)
+    p_d = torch.from_numpy(p).to(dev).reshape(-1)
+    s_d = torch.from_numpy(s).to(dev).reshape(-1)
+    x = torch.from_numpy(x_h).to(dev)                      # (B, N): vector b at b*N (ldu = N)
+    yt = torch.from_numpy(yt_h).to(dev)
+    y = torch.empty_like(x)
+    g = torch.empty_like(x)
+    gin = torch.empty_like(x)
+    dp = torch.empty(L * N // 2 * 2, dtype=torch.float32, device=dev)
+    ldp, lds = N // 2 * 2, N // 2 * 2
+    wsb_f = lib.mg_workspace_bytes(0, N, L, B, 0, 0, None)
+    wsb_b = lib.mg_workspace_bytes(2, N, L, B, 0, 0, None)
+    ws_f = torch.empty(wsb_f, dtype=torch.uint8, device=dev)
+    ws_b = torch.empty(wsb_b, dtype=torch.uint8, device=dev)
+    for w, n in ((ws_f, wsb_f), (ws_b, wsb_b)):
+        _lib.check(lib.mg_workspace_init(w.data_ptr(), n, st), "mg_workspace_init")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # > 129 MB L2
+    launches_per_step = 5                                  # coef+prop (fwd), coef+prop+reduce (bwd)
+
+    def step(xx, yy_t):
+        _lib.check(lib.mg_fwdprop(N, L, B, lens_d.data_ptr(), shifts_d.data_ptr(), p_d.data_ptr(), ldp,
+                                  s_d.data_ptr(), lds, xx.data_ptr(), y.data_ptr(), N, 0, ws_f.data_ptr(), wsb_f, st),
+                   "mg_fwdprop")
+        torch.sub(y, yy_t, out=g).mul_(2.0)
+        _lib.check(lib.mg_backdiff(N, L, B, lens_d.data_ptr(), shifts_d.data_ptr(), p_d.data_ptr(), dp.data_ptr(),
+                                   ldp, s_d.data_ptr(), lds, y.data_ptr(), g.data_ptr(), None, gin.data_ptr(), N, 0, 0,
+                                   ws_b.data_ptr(), wsb_b, st), "mg_backdiff")
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    def timed(fn, k):
+        """K timed calls, each bracketed by CUDA events on the launch stream, L2 flushed in between."""
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+        for a, b in evs:
+            flush.zero_()
+            a.record(stream)
+            fn()
+            b.record(stream)
+        torch.cuda.synchronize(dev)
+        return [a.elapsed_time(b) * 1e-3 for a, b in evs]
+
+    # ---- device-resident step (value)
+    for _ in range(args.warmup):
+        step(x, yt)
+    barrier()
+    with ClockSampler(gpu_id(torch, dev)) as cs:
+        times = timed(lambda: step(x, yt), args.steps)
+        barrier()
+    t_step = sum(times) / len(times)
+    status = max(lib.mg_read_status(ws_f.data_ptr(), 0, st), lib.mg_read_status(ws_b.data_ptr(), 0, st))
+    if status != 0:
+        raise RuntimeError("kernel status %d" % status)
+
+    # ---- end to end through the C ABI with host buffers: H2D x, y_t; D2H dJ/dp and the loss
+    x_pin = torch.from_numpy(x_h).pin_memory()
+    yt_pin = torch.from_numpy(yt_h).pin_memory()
+    dp_pin = torch.empty(dp.numel(), dtype=torch.float32).pin_memory()
+    loss_pin = torch.empty(1, dtype=torch.float32).pin_memory()
+    xd = torch.empty_like(x)
+    ytd = torch.empty_like(yt)
+    loss = torch.empty(1, dtype=torch.float32, device=dev)
+
+    def e2e_step():
+        xd.copy_(x_pin, non_blocking=True)
+        ytd.copy_(yt_pin, non_blocking=True)
+        step(xd, ytd)
+        loss.copy_((g.abs().square().sum() * 0.25).reshape(1))     # J = sum |y - y_t|^2
+        dp_pin.copy_(dp, non_blocking=True)
+        loss_pin.copy_(loss, non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier()
+    times_e2e = timed(e2e_step, args.steps)
+    barrier()
+    t_e2e = sum(times_e2e) / len(times_e2e)
+    h2d = 2 * x.numel() * 8
+    d2h = dp.numel() * 4 + 4
+
+    # ---- roofline of the dominant kernel: the back-propagation kernel alone (tiles built once)
+    def bwd_kernel():
+        _lib.check(lib.mg_propagate(2, N, L, B, 0, 0, y.data_ptr(), g.data_ptr(), None, gin.data_ptr(), N, None, 0, 0,
+                                    None, ws_b.data_ptr(), wsb_b, st), "mg_propagate")
+
+    def fwd_kernel():
+        _lib.check(lib.mg_propagate(0, N, L, B, 0, 0, x.data_ptr(), None, y.data_ptr(), None, N, None, 0, 0, None,
+                                    ws_f.data_ptr(), wsb_f, st), "mg_propagate")
+
+    bwd_kernel()
+    t_bwd = statistics.median(timed(bwd_kernel, max(5, args.steps)))
+    t_fwd = statistics.median(timed(fwd_kernel, max(5, args.steps)))
+    # FP32 FMA peak of this device (the measured-peaks file has HBM and bf16 only)
+    props = torch.cuda.get_device_properties(dev)
+    sink = torch.empty(props.multi_processor_count * 4 * 256, device=dev)
+    iters = 4000
+
+    def probe():
+        _lib.check(lib.mg_fma_probe(sink.data_ptr(), props.multi_processor_count * 4, 256, iters, st), "fma_probe")
+
+    probe()
+    t_probe = min(timed(probe, 3))
+    peak = props.multi_processor_count * 4 * 256 * iters * 64 * 2 / t_probe
+
+    # ---- reduce over ranks
+    t_max = t_step
+    if world > 1:
+        tt = torch.tensor([t_step, t_e2e], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max, t_e2e = float(tt[0]), float(tt[1])
+    if rank != 0:
+        return
+    units = n_mzi * B * world
+    value = units / t_max
+    bwd_flops = n_mzi * B * FLOP_BWD
+    achieved = bwd_flops / t_bwd
+    traffic = traffic_from_profiles("prop_bwd_clements_N256_L256_B4096.md")
+    line = {
+        "metric": METRIC, "value": value, "unit": "MZI-apps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded normal fields, uniform phases)",
+        "config": {"workload": WORKLOAD, "N": N, "L": L, "B": B, "n_mzi": n_mzi, "splitter_sigma": SIGMA,
+                   "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "pct_fp32_peak": 100 * value / world * (FLOP_FWD + FLOP_BWD) / peak,
+        "fp32_peak_tflops": peak / 1e12,
+        "kernels": {"fwd_prop_ms": t_fwd * 1e3, "bwd_prop_ms": t_bwd * 1e3,
+                    "fwd_mzi_per_s": n_mzi * B / t_fwd, "bwd_mzi_per_s": n_mzi * B / t_bwd},
+        "roofline": {"kernel": "prop_kernel<BWD> (back-propagation)", "bound": "fp32", "achieved": achieved / 1e12,
+                     "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / peak,
+                     "peak_source": "measured: FP32 FMA probe on this GPU (no FP32 entry in the measured-peaks file)",
+                     "traffic": traffic, "algorithmic_flops_per_launch": bwd_flops},
+        "e2e": {"value": units / t_e2e, "unit": "MZI-apps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": cs.summary(),
+    }
+    line["cpu_baseline"] = cpu_baseline((lens, shifts, p, s, x_h, yt_h, n_mzi), seconds=10.0)
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    try:
+        run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

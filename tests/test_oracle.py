@@ -1,0 +1,164 @@
+"""CPU tests: the oracle pinned to the reference's own outputs, the C++ port pinned to the reference's
+compiled c/dot.cpp, geometry helpers, and the C ABI library's exports (no GPU calls)."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import meshes_oracle as O
+from oracle import port as P
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def fixtures():
+    return sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, name))
+    kw = dict(lens=z["lens"].tolist(), shifts=z["shifts"].tolist()) if "lens" in z else dict(strides=z["strides"].tolist())
+    return z, O.OracleMesh(N=int(z["N"]), L=int(z["L"]), crossing=str(z["crossing"]), p=z["p"],
+                           s=z["s"] if "s" in z else None, **kw)
+
+
+@pytest.mark.parametrize("name", fixtures())
+def test_oracle_matches_reference_fixtures(name):
+    z, om = load(name)
+    assert O.rel_err(O.propagate(om, z["x"]), z["y"]) < 1e-12
+    if "dy" in z:
+        y, dy = O.fwddiff(om, z["x"], z["dp_dir"])
+        assert O.rel_err(dy, z["dy"]) < 1e-12
+    if "dJdp" in z:
+        G, xr, gin = O.vjp_unitary(om, z["y"], z["g"])
+        assert O.rel_err(O.contract_dp(om, G), z["dJdp"]) < 1e-12
+        assert O.rel_err(gin, z["g_in"]) < 1e-12
+        assert O.rel_err(xr, z["x"]) < 1e-12
+        G2, gin2 = O.vjp_stored(om, z["x"], z["g"])
+        assert O.rel_err(O.contract_dp(om, G2), z["dJdp"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", [f for f in fixtures() if "y_c64" in np.load(os.path.join(GOLDEN, f))])
+def test_port_matches_reference_fixtures(name):
+    """The C++ port against the reference's complex128 dot and its complex64 meshdot_helper32."""
+    z, om = load(name)
+    fns = P.port_lib()
+    y64 = P.forward(fns, om, z["x"], dtype=np.complex128)
+    assert O.rel_err(y64, z["y"]) < 1e-12
+    y32 = P.forward(fns, om, z["x"], dtype=np.complex64)
+    assert O.rel_err(y32, z["y_c64"]) < 1e-6
+    G, gin = P.vjp(fns, om, z["y"], z["g"], dtype=np.complex128)
+    assert O.rel_err(O.contract_dp(om, G), z["dJdp"]) < 1e-12
+    assert O.rel_err(gin, z["g_in"]) < 1e-12
+
+
+def _random_flat_case(rng, N, B, perm=False, pos=-1):
+    lens, shifts = O.clements_geometry(N)
+    om = O.random_mesh(rng, N, "clements", "mzi", 0.05)
+    T, inds = P.packed_T(om)
+    nT = T.shape[2]
+    dT = (rng.standard_normal(T.shape) + 1j * rng.standard_normal(T.shape))
+    v = rng.standard_normal((N, B)) + 1j * rng.standard_normal((N, B))
+    dv = rng.standard_normal((N, B)) + 1j * rng.standard_normal((N, B))
+    ph = rng.uniform(0, 2 * np.pi, N) if pos >= 0 else np.zeros(0)
+    dph = rng.standard_normal(N) if pos >= 0 else np.zeros(0)
+    perms = np.array([rng.permutation(N) for _ in range(len(lens) + 1)], np.int32) if perm else np.empty((0, 0), np.int32)
+    return om, T, dT, ph, dph, v, dv, inds, lens, shifts, perms, nT
+
+
+@pytest.mark.skipif(P.ref_lib() is None, reason="reference c/dot.cpp not compiled here (oracle/_ref)")
+@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("perm,pos", [(False, -1), (True, -1), (False, 1), (True, 0)])
+def test_port_matches_reference_binary(mode, perm, pos):
+    """Port vs the reference's own compiled c/dot.cpp on random inputs, phase screens and permutations
+    included (mode 2 with one thread: the reference's threaded reduction races)."""
+    rng = np.random.default_rng(100 + mode + 10 * perm + 3 * pos)
+    case = _random_flat_case(rng, 12, 19, perm, pos)
+    om, T, dT, ph, dph, v, dv, inds, lens, shifts, perms, nT = case
+    outs = []
+    for fns in (P.port_lib(), P.ref_lib()):
+        T_, dT_ = T.copy(), (dT.copy() if mode == 1 else np.zeros_like(dT))
+        ph_, dph_ = ph.copy(), (dph.copy() if mode == 1 else np.zeros_like(dph))
+        v_, dv_ = v.copy(), dv.copy()
+        P.call(fns, T_, dT_, ph_, dph_, v_, dv_, inds, lens, shifts, perms, pos, mode, 1)
+        outs.append((v_, dv_, dT_, dph_))
+    for a, b in zip(*outs):
+        if a.size:
+            assert O.rel_err(a, b) < 1e-12
+
+
+def test_port_threads_race_free():
+    """Mode 2 with several threads equals one thread (private accumulators, ordered sum)."""
+    rng = np.random.default_rng(11)
+    om = O.random_mesh(rng, 32, "clements", "mzi", 0.02)
+    y = O.unit_columns(rng, 32, 200)
+    g = O.unit_columns(rng, 32, 200)
+    fns = P.port_lib()
+    G1, g1 = P.vjp(fns, om, y, g, threads=1, dtype=np.complex128)
+    G8, g8 = P.vjp(fns, om, y, g, threads=8, dtype=np.complex128)
+    assert O.rel_err(G8, G1) < 1e-13 and O.rel_err(g8, g1) < 1e-14
+
+
+def test_oracle_gradient_central_differences():
+    rng = np.random.default_rng(12)
+    for geo, cr in (("clements", "mzi"), ("reck", "sym"), ("fft", "mzi"), ("clements", "orth")):
+        om = O.random_mesh(rng, 8, geo, cr, 0.02)
+        real = cr == "orth"
+        x = O.unit_columns(rng, 8, 5, real=real)
+        t = O.unit_columns(rng, 8, 5, real=real)
+
+        def loss(p):
+            return float(np.sum(np.abs(O.propagate(om, x, p) - t) ** 2))
+
+        y, dp, _ = O.grad(om, x, lambda y: 2 * (y - t))
+        idx = np.flatnonzero(np.broadcast_to(om.active_mask()[..., None], om.p.shape))[:10]
+        fd = O.central_difference(loss, om.p.astype(np.float64), idx, h=1e-6)
+        assert np.allclose(dp.reshape(-1)[idx], fd, rtol=1e-6, atol=1e-8)
+
+
+def test_lossy_adjoint_matches_finite_differences():
+    """vjp_stored (activations kept) is exact for non-unitary crossings, vjp_unitary is not."""
+    rng = np.random.default_rng(13)
+    om = O.random_mesh(rng, 6, "clements", "mzi", 0.02)
+    T = om.T_grid() * np.exp(rng.normal(0, 0.05, (om.L, 3, 1, 1)))   # per-slot gain
+    lossy = O.OracleMesh(N=6, L=om.L, crossing="mzi", lens=om.lens, shifts=om.shifts, p=om.p, s=om.s, T_override=T)
+    x = O.unit_columns(rng, 6, 4)
+    g = O.unit_columns(rng, 6, 4)
+    G, gin = O.vjp_stored(lossy, x, g)
+    # dJ/dx* for J = Re<g, Ux>*2 is U^H g
+    U = O.matrix(lossy)
+    assert O.rel_err(gin, (U.conj().T @ g.T).T) < 1e-12
+    Gu, _, _ = O.vjp_unitary(lossy, O.propagate(lossy, x), g)
+    assert O.rel_err(Gu, G) > 1e-3
+
+
+def test_geometry_helpers_agree():
+    from meshes_gb300 import geometry as gm
+    for N in (2, 4, 8, 10, 64, 256):
+        assert gm.clements(N) == O.clements_geometry(N)
+        if N >= 3:
+            assert gm.reck(N) == O.reck_geometry(N)
+    for N in (2, 8, 64, 512):
+        assert gm.butterfly(N) == O.butterfly_strides(N)
+        assert gm.fft(N) == O.fft_strides(N)
+    with pytest.raises(ValueError):
+        gm.validate_nn(8, [4], [1])
+    with pytest.raises(ValueError):
+        gm.validate_fft(8, [3])
+
+
+def test_header_symbols_exported():
+    """Every entry point declared in include/meshes_gb300.h is exported by the library and bound in
+    meshes_gb300._lib (loading only; no compute call without a GPU)."""
+    from meshes_gb300 import _lib
+    from meshes_gb300.build import build
+    build()
+    hdr = open(os.path.join(ROOT, "include", "meshes_gb300.h")).read()
+    declared = set(re.findall(r"\b(mg_\w+)\s*\(", hdr))
+    lib = _lib.load()
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert declared == set(_lib.exported_symbols())
+    assert lib.mg_version().decode().startswith("meshes_gb300")
