@@ -249,6 +249,14 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.synchronize(dev)
         return [a.elapsed_time(b) * 1e-3 for a, b in evs]
 
+    if args.profile:
+        # one warm-up step and one profiled step, no timing (for ncu captures: -s 2 -c 2 on prop_kernel)
+        step(x, yt)
+        step(x, yt)
+        torch.cuda.synchronize(dev)
+        print(json.dumps({"profile_steps": 2, "status": lib.mg_read_status(ws_b.data_ptr(), 0, st)}))
+        return
+
     # ---- device-resident step (value)
     for _ in range(args.warmup):
         step(x, yt)
@@ -352,6 +360,7 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--profile", action="store_true", help="two untimed steps only (for ncu captures)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -50,6 +50,7 @@ int ilog2(int x) {
   return l;
 }
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
 struct DevInfo {
   int sms = 0;
@@ -80,6 +81,7 @@ bool instantiated(int op, int M, int V) {
 struct Plan {
   int op, N, L, B, crossing, geometry;
   bool real;
+  int gr;
   int M, V, W, CL, S, G, logG, R, np2, grid;
   unsigned lb, dlb;
   size_t smem;
@@ -97,6 +99,7 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   Plan& p = *P;
   p.op = op; p.N = N; p.L = L; p.B = B; p.crossing = crossing; p.geometry = geometry;
   p.real = crossing == CR_ORTH;
+  p.gr = (op != OP_BWD) ? 0 : (crossing == CR_MZI ? 1 : (crossing == CR_ORTH ? 2 : 0));
   const int Np = pow2ceil(N);
   int M = (cfg && cfg->M) ? cfg->M : std::max(std::min(8, Np), Np / 32);
   if (M < 2 || M > 16 || (M & (M - 1))) return fail(MG_E_CONFIG, "modes per lane M=%d not in {2,4,8,16}", M);
@@ -111,39 +114,47 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   if (!instantiated(op, M, V)) return fail(MG_E_CONFIG, "no kernel instantiated for op=%d M=%d V=%d", op, M, V);
   p.M = M; p.V = V; p.G = G; p.logG = ilog2(G); p.R = 32 / G; p.np2 = G * M / 2;
   const unsigned tslot = p.real ? 16 : 32;               // bytes per slot of a T tile
-  p.lb = (unsigned)(p.np2 * tslot * (op == OP_FWDDIFF ? 2 : 1));
-  p.dlb = (op == OP_BWD) ? (unsigned)(p.np2 * (p.real ? 16 : 64)) : 0;
-  const size_t gstl = (op == OP_BWD) ? (size_t)p.np2 * (p.real ? 16 : 32) : 0;
+  // layer tiles are copied by bulk TMA: every size and offset must be a multiple of 16 bytes
+  p.lb = (unsigned)align16((size_t)p.np2 * tslot * (op == OP_FWDDIFF ? 2 : 1) + (p.gr == 1 ? (size_t)p.np2 * 8 : 0));
+  p.dlb = (op == OP_BWD && p.gr == 0) ? (unsigned)(p.np2 * (p.real ? 16 : 64)) : 0;
+  const int gslot = (op != OP_BWD) ? 0 : (p.gr != 0 ? 8 : (p.real ? 16 : 32));
+  const size_t gstl = (size_t)p.np2 * gslot;
   const int maxw = prop_max_threads(op, M, V) / 32;
   int W = (cfg && cfg->W) ? cfg->W : 0;
   if (!W) {
+    // enough warps to cover the batch in one wave, rounded up to a multiple of 4 so the four
+    // schedulers of an SM carry equal work (measured: 8 warps on 128 SMs beat 7 warps on 147)
     const long per_warp = (long)p.R * V;
     const long warps = (B + per_warp - 1) / per_warp;
-    W = (int)std::min<long>(std::max<long>((warps + di.sms - 1) / di.sms, 1), std::min(8, maxw));
+    long w = std::max<long>((warps + di.sms - 1) / di.sms, 1);
+    if (w > 2) w = (w + 3) / 4 * 4;
+    W = (int)std::min<long>(w, std::min(8, maxw));
   }
   if (W < 1 || W > maxw) return fail(MG_E_CONFIG, "W=%d warps outside [1, %d]", W, maxw);
-  int S = (cfg && cfg->S) ? cfg->S : 3;
+  int S = (cfg && cfg->S) ? cfg->S : (op == OP_FWD ? 2 : 3);
   if (S < 1 || S > 8) return fail(MG_E_CONFIG, "S=%d stages outside [1, 8]", S);
   const size_t budget = (size_t)di.smem_optin - 1024;
   int CL = (cfg && cfg->CL) ? cfg->CL : 0;
   const size_t per_layer = (size_t)S * p.lb + p.dlb + W * gstl;
+  const size_t fixed = 8 * (size_t)(S + 1) + (L <= kMaxSmemKinds ? 4 * (size_t)L : 0);
   if (!CL) {
-    const size_t target = (op == OP_BWD) ? budget : std::min<size_t>(budget, 96 * 1024);
-    CL = (int)std::max<size_t>(1, std::min<size_t>(16, target / per_layer));
+    const size_t target = (op == OP_BWD) ? budget : std::min<size_t>(budget, 160 * 1024);
+    CL = (int)std::max<size_t>(1, std::min<size_t>(16, (target > fixed ? target - fixed : 0) / per_layer));
     if (L > 0) CL = std::min(CL, L);
   }
   if (CL < 1) return fail(MG_E_CONFIG, "CL=%d", CL);
   p.W = W; p.S = S; p.CL = CL;
-  p.smem = prop_smem_bytes(op, p.real, M, G, W, CL, S, p.lb, p.dlb);
+  p.smem = prop_smem_bytes(op, gslot, M, G, W, CL, S, p.lb, p.dlb, L);
   if (p.smem > budget)
     return fail(MG_E_CONFIG, "shared memory %zu B above the %zu B available (M=%d W=%d CL=%d S=%d)", p.smem, budget, M,
                 W, CL, S);
+  if (p.lb % 16 || p.dlb % 16) return fail(MG_E_CONFIG, "tile sizes %u/%u not multiples of 16 bytes", p.lb, p.dlb);
   if ((size_t)CL * p.lb >= (1u << 20) || (size_t)CL * p.dlb >= (1u << 20))
     return fail(MG_E_CONFIG, "one pipeline stage exceeds the 1 MB bulk-copy limit");
   const long per_cta = (long)W * p.R * V;
   p.grid = (int)((B + per_cta - 1) / per_cta);
   p.off_kinds = 256;
-  p.off_tiles = p.off_kinds + align256((size_t)std::max(L, 1) * 4);
+  p.off_tiles = p.off_kinds + align256((size_t)std::max(L, 1) * 12);   // kinds + (shift, len)
   p.off_dtiles = p.off_tiles + align256((size_t)L * p.lb);
   p.off_partial = p.off_dtiles + align256((size_t)L * p.dlb);
   p.total = p.off_partial + ((op == OP_BWD) ? align256((size_t)p.grid * L * p.np2 * 8) : 0);
@@ -186,6 +197,7 @@ int build_tiles(const Plan& P, const int* lens, const int* shifts, const int* st
   if (P.geometry == GEO_FFT && !strides) return fail(MG_E_ARG, "strides is NULL");
   CoefArgs a;
   a.N = P.N; a.L = P.L; a.crossing = P.crossing; a.geometry = P.geometry; a.op = P.op;
+  a.gr = P.gr;
   a.M = P.M; a.G = P.G;
   a.lens = lens; a.shifts = shifts; a.strides = strides;
   a.p = p; a.ldp = ldp; a.s = s; a.lds = lds; a.dp = dp;
@@ -219,14 +231,13 @@ int run_prop(const Plan& P, const void* in0, const void* in1, void* out0, void* 
   lc.smem = P.smem;
   lc.stream = st;
   cudaError_t e;
-  if (P.op == OP_FWD) e = launch_prop_fwd(P.real, P.M, P.V, lc, a);
-  else if (P.op == OP_FWDDIFF) e = launch_prop_fwddiff(P.real, P.M, P.V, lc, a);
-  else e = launch_prop_bwd(P.real, P.M, P.V, lc, a);
+  e = launch_prop(P.op, P.real, P.M, P.V, P.G == 32, P.gr, lc, a);
   if (e != cudaSuccess) return cuda_fail(e, "prop_kernel launch");
   if (P.op == OP_BWD && dp && P.L > 0) {
-    const int n = P.L * (P.N / 2);
-    dp_reduce_kernel<<<(n + 127) / 128, 128, 0, st>>>(a.partial, P.grid, P.L, P.np2, P.N, dp, ldp,
-                                                        crossing_np(P.crossing), accumulate);
+    const int n = P.L * P.np2;
+    dp_reduce_kernel<<<(n + 127) / 128, 128, 0, st>>>(a.partial, P.grid, P.L, P.np2, P.M, P.G, P.N, dp, ldp,
+                                                        crossing_np(P.crossing), accumulate,
+                                                        reinterpret_cast<const int*>(ws + P.off_kinds) + P.L);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "dp_reduce_kernel launch");
   }

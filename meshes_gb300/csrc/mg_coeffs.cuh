@@ -19,6 +19,7 @@ enum { GEO_NN = 0, GEO_FFT = 1 };
 
 struct CoefArgs {
   int N, L, crossing, geometry, op;
+  int gr;                // back-propagation gradient mode (0: dJ/dT + dT/dp tiles, 1: MZI direct, 2: orth direct)
   int M, G;
   const int* lens;
   const int* shifts;
@@ -34,7 +35,7 @@ struct CoefArgs {
   unsigned layer_bytes;
   unsigned char* dtiles; // BWD: [L][dlayer_bytes]
   unsigned dlayer_bytes;
-  int* kinds;            // [L]
+  int* kinds;            // [L] layer kinds, followed by [L][2] (shift, len) of the active slot range
   int* status;
 };
 
@@ -101,7 +102,21 @@ __global__ void coef_kernel(const CoefArgs a) {
   const int l = idx / np2, q = idx - l * np2;
   bool active = false;
   const int kind = layer_kind(a, l, q, &active);
-  if (q == 0) a.kinds[l] = kind;
+  if (q == 0) {
+    a.kinds[l] = kind;
+    int sh = 0, ln = 0;
+    if (a.geometry == GEO_NN) {
+      sh = __ldg(a.shifts + l);
+      ln = __ldg(a.lens + l);
+      if (sh < 0 || ln < 0 || sh + 2 * ln > a.N) sh = ln = 0;
+    } else {
+      bool any = false;
+      layer_kind(a, l, 0, &any);
+      ln = any ? a.N / 2 : 0;
+    }
+    a.kinds[a.L + 2 * l] = sh;
+    a.kinds[a.L + 2 * l + 1] = ln;
+  }
   const int M = a.M, G = a.G;
   const bool real = a.crossing == CR_ORTH;
   float4* tl = reinterpret_cast<float4*>(a.tiles + (size_t)l * a.layer_bytes);
@@ -116,12 +131,27 @@ __global__ void coef_kernel(const CoefArgs a) {
   if (!real) {
     C2x2 T, D0, D1;
     slot_T(a, l, q, active, T, D0, D1);
-    if (a.op == OP_BWD) {
-      float4* D = reinterpret_cast<float4*>(a.dtiles + (size_t)l * a.dlayer_bytes) + 4 * q;
+    if (a.op == OP_BWD && a.gr == 1) {   // (cos, sin)(pi/4 + beta) of the slot, for the direct MZI gradient
+      float2 csv = make_float2(0.f, 0.f);
+      if (active) {
+        const float be = a.s ? a.s[(size_t)l * a.lds + (size_t)q * 2 + 1] : 0.f;
+        double sb, cb;
+        sincos(0.78539816339744830962 + (double)be, &sb, &cb);
+        csv = make_float2((float)cb, (float)sb);
+      }
+      float2* cs = reinterpret_cast<float2*>(tl + M * G);
+      if (!xl) cs[e * G + j] = csv;
+      else {
+        const int d = (1 << (kind - KIND_XL)) / M;
+        cs[ma * (G / 2) + a_lane_index(la, d)] = csv;
+      }
+    }
+    if (a.op == OP_BWD && a.gr == 0) {   // planes [k][pos]: D0 row 0, D0 row 1, D1 row 0, D1 row 1
+      float4* D = reinterpret_cast<float4*>(a.dtiles + (size_t)l * a.dlayer_bytes) + slot_pos(q, M, G);
       D[0] = make_float4(D0.t00.x, D0.t00.y, D0.t01.x, D0.t01.y);
-      D[1] = make_float4(D0.t10.x, D0.t10.y, D0.t11.x, D0.t11.y);
-      D[2] = make_float4(D1.t00.x, D1.t00.y, D1.t01.x, D1.t01.y);
-      D[3] = make_float4(D1.t10.x, D1.t10.y, D1.t11.x, D1.t11.y);
+      D[np2] = make_float4(D0.t10.x, D0.t10.y, D0.t11.x, D0.t11.y);
+      D[2 * np2] = make_float4(D1.t00.x, D1.t00.y, D1.t01.x, D1.t01.y);
+      D[3 * np2] = make_float4(D1.t10.x, D1.t10.y, D1.t11.x, D1.t11.y);
     }
     C2x2 dT = c2x2_zero();
     if (a.op == OP_FWDDIFF && active && a.dp) {
@@ -155,8 +185,8 @@ __global__ void coef_kernel(const CoefArgs a) {
   } else {
     R2x2 T, D0;
     slot_R(a, l, q, active, T, D0);
-    if (a.op == OP_BWD) {
-      float4* D = reinterpret_cast<float4*>(a.dtiles + (size_t)l * a.dlayer_bytes) + q;
+    if (a.op == OP_BWD && a.gr == 0) {
+      float4* D = reinterpret_cast<float4*>(a.dtiles + (size_t)l * a.dlayer_bytes) + slot_pos(q, M, G);
       D[0] = make_float4(D0.t00, D0.t01, D0.t10, D0.t11);
     }
     R2x2 dT;
@@ -189,15 +219,28 @@ __global__ void coef_kernel(const CoefArgs a) {
   }
 }
 
-// dp[l][q][k] (= or +=) sum over the nC per-CTA partials, in CTA order (deterministic)
-__global__ void dp_reduce_kernel(const float2* __restrict__ partial, int nC, int L, int np2, int N, float* dp,
-                                 int ldp, int n_p, int accumulate) {
+// dp[l][q][k] (= or +=) sum over the nC per-CTA partials, in CTA order (deterministic).  Partials are
+// stored in the lane-major slot order pos (slot_pos); threads walk pos so the reads coalesce.
+// Inactive slots (outside a layer's lens/shifts range) get 0 (overwrite) or are left unchanged (accumulate).
+__global__ void dp_reduce_kernel(const float2* __restrict__ partial, int nC, int L, int np2, int M, int G, int N,
+                                 float* dp, int ldp, int n_p, int accumulate, const int* geo) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  const int half = N / 2;
-  if (idx >= L * half) return;
-  const int l = idx / half, q = idx - l * half;
+  if (idx >= L * np2) return;
+  const int l = idx / np2, pos = idx - l * np2;
+  const int q = pos_slot(pos, M, G);
+  if (q >= N / 2) return;
+  const int sh = geo[2 * l], ln = geo[2 * l + 1];
+  const bool active = q >= sh / 2 && q < sh / 2 + ln;
+  if (!active) {
+    if (!accumulate) {
+      float* o = dp + (size_t)l * ldp + (size_t)q * n_p;
+      o[0] = 0.f;
+      if (n_p > 1) o[1] = 0.f;
+    }
+    return;
+  }
   const size_t stride = (size_t)L * np2;
-  const float2* p = partial + (size_t)l * np2 + q;
+  const float2* p = partial + (size_t)l * np2 + pos;
   float sx = 0.f, sy = 0.f;
   int c = 0;
   for (; c + 4 <= nC; c += 4) {

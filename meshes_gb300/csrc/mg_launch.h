@@ -30,10 +30,10 @@ inline cudaError_t ensure_smem_attr(K kernel, std::atomic<unsigned long long>& d
   return cudaSuccess;
 }
 
-template <int OP, int M, int V, bool REAL>
+template <int OP, int M, int V, bool REAL, int GT, int GR>
 inline cudaError_t launch_one(const LaunchCfg& lc, const PropArgs& a) {
   static std::atomic<unsigned long long> done{0};
-  auto k = prop_kernel<OP, M, V, REAL>;
+  auto k = prop_kernel<OP, M, V, REAL, GT, GR>;
   cudaError_t e = ensure_smem_attr(k, done);
   if (e != cudaSuccess) return e;
   k<<<lc.grid, lc.block, lc.smem, lc.stream>>>(a);
@@ -41,11 +41,13 @@ inline cudaError_t launch_one(const LaunchCfg& lc, const PropArgs& a) {
 }
 
 // max threads per CTA the instantiation was compiled for
-inline int prop_max_threads(int op, int M, int V) { return (op == OP_FWD && M * V <= 16) ? 512 : 256; }
+inline int prop_max_threads(int op, int M, int V) {
+  return ((op == OP_FWD && M * V <= 16) || (op == OP_BWD && M * V <= 8)) ? 512 : 256;
+}
 
 // per-op dispatchers (one translation unit each, compiled in parallel)
-cudaError_t launch_prop_fwd(bool real, int M, int V, const LaunchCfg& lc, const PropArgs& a);
-cudaError_t launch_prop_fwddiff(bool real, int M, int V, const LaunchCfg& lc, const PropArgs& a);
-cudaError_t launch_prop_bwd(bool real, int M, int V, const LaunchCfg& lc, const PropArgs& a);
+// full: a vector fills the warp (G = 32), selecting the compile-time-G instantiation;
+// gr: back-propagation gradient mode (0 dJ/dT + dT/dp tiles, 1 MZI direct, 2 orth direct)
+cudaError_t launch_prop(int op, bool real, int M, int V, bool full, int gr, const LaunchCfg& lc, const PropArgs& a);
 
 }  // namespace mg

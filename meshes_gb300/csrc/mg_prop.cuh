@@ -97,6 +97,50 @@ __device__ __forceinline__ void x_bwd(const CT& t, F& a, F& b, F& ga, F& gb, CT&
   const F ngb = ccfma(t.t11, gb, ccmul(t.t01, ga));
   a = xa; b = xb; ga = nga; gb = ngb;
 }
+template <int OP, typename F, typename CT>
+__device__ __forceinline__ void xop(const CT& t, const CT& d, F& a, F& b, F& wa, F& wb, CT& acc) {
+  if constexpr (OP == OP_FWD) x_fwd(t, a, b);
+  else if constexpr (OP == OP_FWDDIFF) x_fwddiff(t, d, a, b, wa, wb);
+  else x_bwd(t, a, b, wa, wb, acc);
+}
+
+// Back-propagation with the parameter gradient taken directly (no 2x2 dJ/dT accumulator).
+// MZI (GR = 1), from T = S(beta) P(th) S(alpha) P(ph):
+//   dJ/dph = Re(i x_a conj(g_in,a))            (input-side field and gradient of mode a)
+//   dJ/dth = Re(i m conj(h)),  m = (S(beta)^H y)_a, h = (S(beta)^H g)_a,  (c, s) = cos, sin(pi/4 + beta)
+// orth (GR = 2): dJ/dth = (g_a y_b - g_b y_a) / 2 (the 1/2 is applied in the chunk reduction).
+__device__ __forceinline__ void x_bwd_direct(const C2x2& t, float2 cs, float2& a, float2& b, float2& ga, float2& gb,
+                                             float& ath, float& aph) {
+  const float c = cs.x, s = cs.y;
+  const float m0x = fmaf(c, a.x, s * b.y), m0y = fmaf(c, a.y, -s * b.x);
+  const float h0x = fmaf(c, ga.x, s * gb.y), h0y = fmaf(c, ga.y, -s * gb.x);
+  ath = fmaf(h0y, m0x, fmaf(-h0x, m0y, ath));
+  const float2 xa = ccfma(t.t10, b, ccmul(t.t00, a));
+  const float2 xb = ccfma(t.t11, b, ccmul(t.t01, a));
+  const float2 nga = ccfma(t.t10, gb, ccmul(t.t00, ga));
+  const float2 ngb = ccfma(t.t11, gb, ccmul(t.t01, ga));
+  aph = fmaf(nga.y, xa.x, fmaf(-nga.x, xa.y, aph));
+  a = xa; b = xb; ga = nga; gb = ngb;
+}
+__device__ __forceinline__ void x_bwd_direct(const R2x2& t, float2, float& a, float& b, float& ga, float& gb,
+                                             float& ath, float&) {
+  ath = fmaf(ga, b, fmaf(-gb, a, ath));
+  const float xa = fmaf(t.t10, b, t.t00 * a), xb = fmaf(t.t11, b, t.t01 * a);
+  const float nga = fmaf(t.t10, gb, t.t00 * ga), ngb = fmaf(t.t11, gb, t.t01 * ga);
+  a = xa; b = xb; ga = nga; gb = ngb;
+}
+// stage a warp's (dJ/dth, dJ/dph) of one slot position
+__device__ __forceinline__ void acc2_stage(float2* gl2, int pos, int G, int r, float ath, float aph, bool store) {
+  for (int off = G; off < 32; off <<= 1) {
+    ath += __shfl_xor_sync(0xffffffffu, ath, off, 32);
+    aph += __shfl_xor_sync(0xffffffffu, aph, off, 32);
+  }
+  if (store && r == 0) gl2[pos] = make_float2(ath, aph);
+}
+// float4 offset of the (c, s) splitter coefficients in a direct MZI back-propagation tile
+template <int M> __device__ __forceinline__ int cs_off(int G) { return M * G; }
+// compact index of an "a" lane (bit d clear) among the G/2 a-lanes of a cross-lane layer
+__device__ __forceinline__ int a_lane_index(int j, int d) { return ((j / (2 * d)) * d) | (j & (d - 1)); }
 
 __device__ __forceinline__ void acc_zero(C2x2& a) { a = c2x2_zero(); }
 __device__ __forceinline__ void acc_zero(R2x2& a) { a.t00 = a.t01 = a.t10 = a.t11 = 0.f; }
@@ -126,50 +170,60 @@ __device__ __forceinline__ void acc_stage(float4* gl, int e, int G, int j, int r
   if (r == 0) gl[e * G + j] = make_float4(a.t00, a.t01, a.t10, a.t11);
 }
 
-// ---- one crossing entry e of a layer, applied to all V vectors of the lane
-template <int OP, int V, bool REAL, typename F>
-__device__ __forceinline__ void entry(const float4* tl, int doff, int e, int G, int j, int r, F* pa[V], F* pb[V],
-                                      F* pga[V], F* pgb[V], float4* gl) {
+// Lane geometry of one launch.  With GT > 0 the group size is a compile-time constant (GT = 32: a
+// vector fills the warp) and every index, shuffle width and group reduction folds away.
+template <int GT>
+struct Lanes {
+  int G, j, r;
+  __device__ __forceinline__ Lanes(int g_runtime, int log_g) {
+    const int lane = threadIdx.x & 31;
+    G = GT ? GT : g_runtime;
+    j = lane & (G - 1);
+    r = GT ? (lane / (GT ? GT : 1)) : (lane >> log_g);
+  }
+};
+
+// ---- one crossing entry e of a layer (local modes a, b), applied to all V vectors of the lane
+template <int OP, int M, int V, bool REAL, int GR, typename F>
+__device__ __forceinline__ void entry(const float4* tl, int doff, int e, int a, int b, int G, int j, int r,
+                                      F (&u)[V][M], F (&w)[V][M], float4* gl) {
   using CT = typename Fld<REAL>::C;
-  CT t;
+  CT t, d, acc;
   ld_coef(tl, e, G, j, t);
-  if constexpr (OP == OP_FWD) {
+  if constexpr (OP == OP_BWD && GR != 0) {
+    float2 cs = make_float2(0.f, 0.f);
+    if constexpr (GR == 1) cs = reinterpret_cast<const float2*>(tl + cs_off<M>(G))[e * G + j];
+    float ath = 0.f, aph = 0.f;
 #pragma unroll
-    for (int v = 0; v < V; ++v) x_fwd(t, *pa[v], *pb[v]);
-  } else if constexpr (OP == OP_FWDDIFF) {
-    CT d;
-    ld_coef(tl + doff, e, G, j, d);
-#pragma unroll
-    for (int v = 0; v < V; ++v) x_fwddiff(t, d, *pa[v], *pb[v], *pga[v], *pgb[v]);
+    for (int v = 0; v < V; ++v) x_bwd_direct(t, cs, u[v][a], u[v][b], w[v][a], w[v][b], ath, aph);
+    acc2_stage(reinterpret_cast<float2*>(gl), e * G + j, G, r, ath, aph, true);
   } else {
-    CT acc;
-    acc_zero(acc);
+    if constexpr (OP == OP_FWDDIFF) ld_coef(tl + doff, e, G, j, d);
+    if constexpr (OP == OP_BWD) acc_zero(acc);
 #pragma unroll
-    for (int v = 0; v < V; ++v) x_bwd(t, *pa[v], *pb[v], *pga[v], *pgb[v], acc);
-    acc_stage(gl, e, G, j, r, acc);
+    for (int v = 0; v < V; ++v) xop<OP>(t, d, u[v][a], u[v][b], w[v][a], w[v][b], acc);
+    if constexpr (OP == OP_BWD) acc_stage(gl, e, G, j, r, acc);
   }
 }
 
 // ---- layer with all pairs inside the lane: (a, a+SS), a = 2*SS*(e/SS) + e%SS
-template <int OP, int M, int V, bool REAL, int SS, typename F>
+template <int OP, int M, int V, bool REAL, int GR, int SS, typename F>
 __device__ __forceinline__ void layer_local(const float4* tl, int G, int j, int r, F (&u)[V][M], F (&w)[V][M],
                                             float4* gl) {
   const int doff = dt_off<REAL, M>(G);
 #pragma unroll
   for (int e = 0; e < M / 2; ++e) {
-    const int a = 2 * SS * (e / SS) + (e % SS), b = a + SS;
-    F* pa[V]; F* pb[V]; F* pga[V]; F* pgb[V];
-#pragma unroll
-    for (int v = 0; v < V; ++v) { pa[v] = &u[v][a]; pb[v] = &u[v][b]; pga[v] = &w[v][a]; pgb[v] = &w[v][b]; }
-    entry<OP, V, REAL>(tl, doff, e, G, j, r, pa, pb, pga, pgb, gl);
+    const int a = 2 * SS * (e / SS) + (e % SS);
+    entry<OP, M, V, REAL, GR>(tl, doff, e, a, a + SS, G, j, r, u, w, gl);
   }
 }
 
 // ---- nearest-neighbour layer with odd shift: pairs (2e+1, 2e+2) and the lane-boundary pair
 // (mode M-1 of lane j, mode 0 of lane j+1) computed by lane j (reference gpu/fwdprop.cu:98-106)
-template <int OP, int M, int V, bool REAL, typename F>
+template <int OP, int M, int V, bool REAL, int GR, typename F>
 __device__ __forceinline__ void layer_mis(const float4* tl, int G, int j, int r, F (&u)[V][M], F (&w)[V][M],
                                           float4* gl) {
+  using CT = typename Fld<REAL>::C;
   const int doff = dt_off<REAL, M>(G);
   F nu[V], nw[V];
 #pragma unroll
@@ -178,19 +232,25 @@ __device__ __forceinline__ void layer_mis(const float4* tl, int G, int j, int r,
     if constexpr (OP != OP_FWD) nw[v] = shfl_down(w[v][0], 1, G);
   }
 #pragma unroll
-  for (int e = 0; e < M / 2 - 1; ++e) {
-    F* pa[V]; F* pb[V]; F* pga[V]; F* pgb[V];
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-      pa[v] = &u[v][2 * e + 1]; pb[v] = &u[v][2 * e + 2]; pga[v] = &w[v][2 * e + 1]; pgb[v] = &w[v][2 * e + 2];
-    }
-    entry<OP, V, REAL>(tl, doff, e, G, j, r, pa, pb, pga, pgb, gl);
-  }
+  for (int e = 0; e < M / 2 - 1; ++e) entry<OP, M, V, REAL, GR>(tl, doff, e, 2 * e + 1, 2 * e + 2, G, j, r, u, w, gl);
   {
-    F* pa[V]; F* pb[V]; F* pga[V]; F* pgb[V];
+    constexpr int e = M / 2 - 1;
+    CT t, d, acc;
+    ld_coef(tl, e, G, j, t);
+    if constexpr (OP == OP_BWD && GR != 0) {
+      float2 cs = make_float2(0.f, 0.f);
+      if constexpr (GR == 1) cs = reinterpret_cast<const float2*>(tl + cs_off<M>(G))[e * G + j];
+      float ath = 0.f, aph = 0.f;
 #pragma unroll
-    for (int v = 0; v < V; ++v) { pa[v] = &u[v][M - 1]; pb[v] = &nu[v]; pga[v] = &w[v][M - 1]; pgb[v] = &nw[v]; }
-    entry<OP, V, REAL>(tl, doff, M / 2 - 1, G, j, r, pa, pb, pga, pgb, gl);
+      for (int v = 0; v < V; ++v) x_bwd_direct(t, cs, u[v][M - 1], nu[v], w[v][M - 1], nw[v], ath, aph);
+      acc2_stage(reinterpret_cast<float2*>(gl), e * G + j, G, r, ath, aph, true);
+    } else {
+      if constexpr (OP == OP_FWDDIFF) ld_coef(tl + doff, e, G, j, d);
+      if constexpr (OP == OP_BWD) acc_zero(acc);
+#pragma unroll
+      for (int v = 0; v < V; ++v) xop<OP>(t, d, u[v][M - 1], nu[v], w[v][M - 1], nw[v], acc);
+      if constexpr (OP == OP_BWD) acc_stage(gl, e, G, j, r, acc);
+    }
   }
 #pragma unroll
   for (int v = 0; v < V; ++v) {
@@ -223,10 +283,12 @@ __device__ __forceinline__ void ld_xl(const float4* tl, int m, int G, int j, flo
   const float4 q = tl[(m >> 1) * G + j];
   if (m & 1) { cs = q.z; cp = q.w; } else { cs = q.x; cp = q.y; }
 }
-template <int OP, int M, int V, bool REAL, typename F>
+template <int OP, int M, int V, bool REAL, int GR, typename F>
 __device__ __forceinline__ void layer_xl(const float4* tl, int d, int G, int j, int r, F (&u)[V][M], F (&w)[V][M],
                                          float4* gl) {
   const int doff = dt_off<REAL, M>(G);
+  const bool is_a = (j & d) == 0;
+  const int ja = a_lane_index(j, d);
 #pragma unroll
   for (int m = 0; m < M; ++m) {
     F cs, cp;
@@ -247,6 +309,30 @@ __device__ __forceinline__ void layer_xl(const float4* tl, int d, int G, int j, 
         w[v][m] = cfma(dp, ru, cfma(ds, u[v][m], cfma(cp, rw, cmul(cs, w[v][m]))));
         u[v][m] = cfma(cp, ru, cmul(cs, u[v][m]));
       }
+    } else if constexpr (GR != 0) {
+      // coefficients of the BWD tile are the own row of T^H; a-lanes (bit d clear) own the slot's
+      // gradient (their mode is the slot's first mode), b-lanes compute and discard it
+      float2 sc = make_float2(0.f, 0.f);
+      if constexpr (GR == 1) sc = reinterpret_cast<const float2*>(tl + cs_off<M>(G))[m * (G / 2) + ja];
+      float ath = 0.f, aph = 0.f;
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        const F ry = shfl_xor(u[v][m], d, G);
+        const F rg = shfl_xor(w[v][m], d, G);
+        const F x = cfma(cp, ry, cmul(cs, u[v][m]));
+        const F ng = cfma(cp, rg, cmul(cs, w[v][m]));
+        if constexpr (GR == 1) {
+          const float m0x = fmaf(sc.x, u[v][m].x, sc.y * ry.y), m0y = fmaf(sc.x, u[v][m].y, -sc.y * ry.x);
+          const float h0x = fmaf(sc.x, w[v][m].x, sc.y * rg.y), h0y = fmaf(sc.x, w[v][m].y, -sc.y * rg.x);
+          ath = fmaf(h0y, m0x, fmaf(-h0x, m0y, ath));
+          aph = fmaf(ng.y, x.x, fmaf(-ng.x, x.y, aph));
+        } else {
+          ath = fmaf(w[v][m], ry, fmaf(-rg, u[v][m], ath));
+        }
+        w[v][m] = ng;
+        u[v][m] = x;
+      }
+      acc2_stage(reinterpret_cast<float2*>(gl), m * (G / 2) + ja, G, r, ath, aph, is_a);
     } else {
       // coefficients of the BWD tile are the own row of T^H
       F aoo = fzero<F>(), aop = fzero<F>();
@@ -267,6 +353,20 @@ __device__ __forceinline__ void layer_xl(const float4* tl, int d, int G, int j, 
       }
       if (r == 0) stage_xl(gl, m, G, j, aoo, aop);
     }
+  }
+}
+
+// ---- one layer of any kind
+template <int OP, int M, int V, bool REAL, int GR, typename F>
+__device__ __forceinline__ void layer_any(int kind, const float4* tl, int G, int j, int r, F (&u)[V][M],
+                                          F (&w)[V][M], float4* gl) {
+  switch (kind) {
+    case 0: layer_local<OP, M, V, REAL, GR, 1>(tl, G, j, r, u, w, gl); break;
+    case 1: if constexpr (M >= 4) layer_local<OP, M, V, REAL, GR, 2>(tl, G, j, r, u, w, gl); break;
+    case 2: if constexpr (M >= 8) layer_local<OP, M, V, REAL, GR, 4>(tl, G, j, r, u, w, gl); break;
+    case 3: if constexpr (M >= 16) layer_local<OP, M, V, REAL, GR, 8>(tl, G, j, r, u, w, gl); break;
+    case KIND_MIS: layer_mis<OP, M, V, REAL, GR>(tl, G, j, r, u, w, gl); break;
+    default: layer_xl<OP, M, V, REAL, GR>(tl, 1 << (kind - KIND_XL - ilog2_const(M)), G, j, r, u, w, gl);
   }
 }
 
@@ -319,41 +419,50 @@ __device__ __forceinline__ void store_fields(const F (&u)[V][M], void* dst, int 
   }
 }
 
+// Layer kinds are staged in shared memory when L is at most this (else read through the L1 cache).
+constexpr int kMaxSmemKinds = 4096;
+
 // Shared-memory footprint of one launch (host and device agree on this layout):
 //   [ring: S*CL*layer_bytes][BWD: dT/dp chunk CL*dlayer_bytes][BWD: per-warp dJ/dT W*CL*Np/2*gslot]
-//   [mbarriers: S+1]
-__host__ __device__ inline size_t prop_smem_bytes(int op, bool real, int M, int G, int W, int CL, int S,
-                                                  unsigned layer_bytes, unsigned dlayer_bytes) {
+//   [mbarriers: S+1][layer kinds: L ints when L <= kMaxSmemKinds]
+//   gslot: bytes staged per slot per warp in back-propagation (32 complex dJ/dT, 16 real dJ/dT,
+//   8 for the direct (dJ/dth, dJ/dph) modes); dlayer_bytes is 0 when no dT/dp tile is needed.
+__host__ __device__ inline size_t prop_smem_bytes(int op, int gslot, int M, int G, int W, int CL, int S,
+                                                  unsigned layer_bytes, unsigned dlayer_bytes, int L) {
   size_t b = (size_t)S * CL * layer_bytes;
   if (op == OP_BWD) {
     const size_t np2 = (size_t)G * M / 2;
-    b += (size_t)CL * dlayer_bytes + (size_t)W * CL * np2 * (real ? 16 : 32);
+    b += (size_t)CL * dlayer_bytes + (size_t)W * CL * np2 * gslot;
   }
-  return b + 8 * (size_t)(S + 1);
+  b += 8 * (size_t)(S + 1);
+  if (L <= kMaxSmemKinds) b += 4 * (size_t)L;
+  return b;
 }
+
+// Slot position of slot q in the lane-major order used by the dT/dp tiles and the gradient partials:
+// pos = e*G + j for q = j*(M/2) + e, so that consecutive threads of the chunk reduction touch
+// consecutive shared-memory words (no bank conflicts) and consecutive global addresses.
+__host__ __device__ inline int slot_pos(int q, int M, int G) { return (q % (M / 2)) * G + q / (M / 2); }
+__host__ __device__ inline int pos_slot(int pos, int M, int G) { return (pos % G) * (M / 2) + pos / G; }
 
 // ---- chunk-end gradient reduction (BWD): sum the W warps' staged dJ/dT of every slot of the chunk
 // in a fixed order, contract with dT/dp and write this CTA's partial (dJ/dp0, dJ/dp1).
 template <int M, bool REAL>
-__device__ __forceinline__ void chunk_reduce(const PropArgs& a, int lo, int nl, const unsigned char* gst,
-                                             const unsigned char* dbuf, int np2) {
-  const size_t gslot = REAL ? 16 : 32;
-  const size_t gst_layer = (size_t)np2 * gslot;
-  const int G = a.G;
+__device__ __forceinline__ void chunk_reduce(const PropArgs& a, const int* kinds, int lo, int nl,
+                                             const unsigned char* gst, const unsigned char* dbuf, int np2, int G) {
+  const size_t gst_layer = (size_t)np2 * (REAL ? 16 : 32);
   for (int idx = threadIdx.x; idx < nl * np2; idx += blockDim.x) {
-    const int li = idx / np2, q = idx - li * np2;
+    const int li = idx / np2, pos = idx - li * np2;
     const int l = lo + li;
-    const int kind = __ldg(a.kinds + l);
-    // locate the two staged rows of slot q: (lane, float4 index) for row 0 and row 1
-    int la, ia, lb, ib;   // lanes and entry indices
-    bool xl = kind >= KIND_XL;
-    int mrow_a = 0, mrow_b = 0;
+    const int kind = kinds[l];
+    const int e = pos / G, j = pos - e * G;
+    int la = j, lb = j, ia, ib, mrow_a = 0, mrow_b = 0;
+    const bool xl = kind >= KIND_XL;
     if (!xl) {
-      la = lb = q / (M / 2);
-      const int e = q - la * (M / 2);
       ia = REAL ? e : 2 * e;
       ib = REAL ? e : 2 * e + 1;
     } else {
+      const int q = j * (M / 2) + e;
       const int st = 1 << (kind - KIND_XL);
       const int ma = 2 * st * (q / st) + (q % st), mb = ma + st;
       la = ma / M; lb = mb / M;
@@ -361,38 +470,29 @@ __device__ __forceinline__ void chunk_reduce(const PropArgs& a, int lo, int nl, 
       ia = REAL ? (mrow_a >> 1) : mrow_a;
       ib = REAL ? (mrow_b >> 1) : mrow_b;
     }
-    float dth = 0.f, dph = 0.f;
-    if constexpr (!REAL) {
-      float4 ra = make_float4(0.f, 0.f, 0.f, 0.f), rb = ra;
-      for (int w = 0; w < a.W; ++w) {
-        const float4* gl = reinterpret_cast<const float4*>(gst + ((size_t)w * a.CL + li) * gst_layer);
-        const float4 x = gl[ia * G + la], y = gl[ib * G + lb];
-        ra.x += x.x; ra.y += x.y; ra.z += x.z; ra.w += x.w;
+    float4 ra = make_float4(0.f, 0.f, 0.f, 0.f), rb = ra;
+    for (int w = 0; w < a.W; ++w) {
+      const float4* gl = reinterpret_cast<const float4*>(gst + ((size_t)w * a.CL + li) * gst_layer);
+      const float4 x = gl[ia * G + la];
+      ra.x += x.x; ra.y += x.y; ra.z += x.z; ra.w += x.w;
+      if (!REAL || xl) {
+        const float4 y = gl[ib * G + lb];
         rb.x += y.x; rb.y += y.y; rb.z += y.z; rb.w += y.w;
       }
-      // G = [[g00, g01], [g10, g11]]
-      float2 g00, g01, g10, g11;
-      if (!xl) {
-        g00 = make_float2(ra.x, ra.y); g01 = make_float2(ra.z, ra.w);
-        g10 = make_float2(rb.x, rb.y); g11 = make_float2(rb.z, rb.w);
-      } else {   // row a = (G_aa, G_ab), row b = (G_bb, G_ba)
-        g00 = make_float2(ra.x, ra.y); g01 = make_float2(ra.z, ra.w);
-        g11 = make_float2(rb.x, rb.y); g10 = make_float2(rb.z, rb.w);
-      }
-      const float4* D = reinterpret_cast<const float4*>(dbuf + (size_t)li * a.dlayer_bytes) + 4 * q;
-      const float4 d0r0 = D[0], d0r1 = D[1], d1r0 = D[2], d1r1 = D[3];
+    }
+    float dth = 0.f, dph = 0.f;
+    const float4* D = reinterpret_cast<const float4*>(dbuf + (size_t)li * a.dlayer_bytes);
+    if constexpr (!REAL) {
+      // G = [[g00, g01], [g10, g11]]; XL rows are a = (G_aa, G_ab), b = (G_bb, G_ba)
+      const float2 g00 = make_float2(ra.x, ra.y), g01 = make_float2(ra.z, ra.w);
+      const float2 g10 = xl ? make_float2(rb.z, rb.w) : make_float2(rb.x, rb.y);
+      const float2 g11 = xl ? make_float2(rb.x, rb.y) : make_float2(rb.z, rb.w);
+      const float4 d0r0 = D[pos], d0r1 = D[np2 + pos], d1r0 = D[2 * np2 + pos], d1r1 = D[3 * np2 + pos];
       dth = d0r0.x * g00.x - d0r0.y * g00.y + d0r0.z * g01.x - d0r0.w * g01.y +
             d0r1.x * g10.x - d0r1.y * g10.y + d0r1.z * g11.x - d0r1.w * g11.y;
       dph = d1r0.x * g00.x - d1r0.y * g00.y + d1r0.z * g01.x - d1r0.w * g01.y +
             d1r1.x * g10.x - d1r1.y * g10.y + d1r1.z * g11.x - d1r1.w * g11.y;
     } else {
-      float4 ra = make_float4(0.f, 0.f, 0.f, 0.f), rb = ra;
-      for (int w = 0; w < a.W; ++w) {
-        const float4* gl = reinterpret_cast<const float4*>(gst + ((size_t)w * a.CL + li) * gst_layer);
-        const float4 x = gl[ia * G + la], y = gl[ib * G + lb];
-        ra.x += x.x; ra.y += x.y; ra.z += x.z; ra.w += x.w;
-        rb.x += y.x; rb.y += y.y; rb.z += y.z; rb.w += y.w;
-      }
       float g00, g01, g10, g11;
       if (!xl) {
         g00 = ra.x; g01 = ra.y; g10 = ra.z; g11 = ra.w;
@@ -401,36 +501,106 @@ __device__ __forceinline__ void chunk_reduce(const PropArgs& a, int lo, int nl, 
         const float2 Bq = (mrow_b & 1) ? make_float2(rb.z, rb.w) : make_float2(rb.x, rb.y);
         g00 = A.x; g01 = A.y; g11 = Bq.x; g10 = Bq.y;
       }
-      const float4 D = reinterpret_cast<const float4*>(dbuf + (size_t)li * a.dlayer_bytes)[q];
-      dth = D.x * g00 + D.y * g01 + D.z * g10 + D.w * g11;
+      const float4 d = D[pos];
+      dth = d.x * g00 + d.y * g01 + d.z * g10 + d.w * g11;
     }
-    a.partial[((size_t)blockIdx.x * a.L + l) * np2 + q] = make_float2(dth, dph);
+    a.partial[((size_t)blockIdx.x * a.L + l) * np2 + pos] = make_float2(dth, dph);
+  }
+}
+
+// ---- chunk-end reduction of the direct modes: sum the W warps' (dJ/dth, dJ/dph) per slot
+template <int M, int GR>
+__device__ __forceinline__ void chunk_reduce_direct(const PropArgs& a, const int* kinds, int lo, int nl,
+                                                    const unsigned char* gst, int np2, int G) {
+  const size_t gst_layer = (size_t)np2 * 8;
+  for (int idx = threadIdx.x; idx < nl * np2; idx += blockDim.x) {
+    const int li = idx / np2, pos = idx - li * np2;
+    const int l = lo + li;
+    const int kind = kinds[l];
+    int sp = pos;
+    if (kind >= KIND_XL) {
+      const int q = pos_slot(pos, M, G);
+      const int st = 1 << (kind - KIND_XL);
+      const int ma = 2 * st * (q / st) + (q % st);
+      sp = (ma % M) * (G / 2) + a_lane_index(ma / M, st / M);
+    }
+    float sx = 0.f, sy = 0.f;
+    for (int w = 0; w < a.W; ++w) {
+      const float2 v = reinterpret_cast<const float2*>(gst + ((size_t)w * a.CL + li) * gst_layer)[sp];
+      sx += v.x;
+      sy += v.y;
+    }
+    a.partial[((size_t)blockIdx.x * a.L + l) * np2 + pos] = make_float2(GR == 2 ? 0.5f * sx : sx, sy);
   }
 }
 
 template <int OP, int M, int V, bool REAL>
 struct PropTraits {
-  static constexpr int kMaxThreads = (OP == OP_FWD && M * V <= 16) ? 512 : 256;
+  static constexpr int kMaxThreads = ((OP == OP_FWD && M * V <= 16) || (OP == OP_BWD && M * V <= 8)) ? 512 : 256;
 };
 
-template <int OP, int M, int V, bool REAL>
+// Layer loop body: fused (aligned, odd-shift) pairs of nearest-neighbour layers run as one
+// straight-line block (the compiler interleaves the two layers' crossings); other kinds one by one.
+template <int OP, int M, int V, bool REAL, int GR, typename F>
+__device__ __forceinline__ void run_chunk(const int* kinds, const unsigned char* st, unsigned layer_bytes, int lo,
+                                          int hi, unsigned char* gst_warp, size_t gst_layer, int G, int j, int r,
+                                          F (&u)[V][M], F (&w)[V][M]) {
+  const int nl = hi - lo;
+  int i = 0;
+  while (i < nl) {
+    const int l0 = (OP == OP_BWD) ? (hi - 1 - i) : (lo + i);
+    const int k0 = kinds[l0];
+    const float4* t0 = reinterpret_cast<const float4*>(st + (size_t)(l0 - lo) * layer_bytes);
+    float4* g0 = reinterpret_cast<float4*>(gst_warp + (size_t)(l0 - lo) * gst_layer);
+    if (i + 1 < nl && (k0 == 0 || k0 == KIND_MIS)) {
+      const int l1 = (OP == OP_BWD) ? (l0 - 1) : (l0 + 1);
+      const int k1 = kinds[l1];
+      const float4* t1 = reinterpret_cast<const float4*>(st + (size_t)(l1 - lo) * layer_bytes);
+      float4* g1 = reinterpret_cast<float4*>(gst_warp + (size_t)(l1 - lo) * gst_layer);
+      if (k0 == 0 && k1 == KIND_MIS) {
+        layer_local<OP, M, V, REAL, GR, 1>(t0, G, j, r, u, w, g0);
+        layer_mis<OP, M, V, REAL, GR>(t1, G, j, r, u, w, g1);
+        i += 2;
+        continue;
+      }
+      if (k0 == KIND_MIS && k1 == 0) {
+        layer_mis<OP, M, V, REAL, GR>(t0, G, j, r, u, w, g0);
+        layer_local<OP, M, V, REAL, GR, 1>(t1, G, j, r, u, w, g1);
+        i += 2;
+        continue;
+      }
+    }
+    layer_any<OP, M, V, REAL, GR>(k0, t0, G, j, r, u, w, g0);
+    i += 1;
+  }
+}
+
+template <int OP, int M, int V, bool REAL, int GT, int GR>
 __global__ void __launch_bounds__(PropTraits<OP, M, V, REAL>::kMaxThreads)
 prop_kernel(const PropArgs a) {
   using F = typename Fld<REAL>::T;
   extern __shared__ __align__(128) unsigned char smem[];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int G = a.G, j = lane & (G - 1), r = lane >> a.logG, R = 32 >> a.logG;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const Lanes<GT> ln(a.G, a.logG);
+  const int G = ln.G, j = ln.j, r = ln.r, R = 32 / G;
   const int np2 = (G * M) >> 1;
   const int vb0 = blockIdx.x * (a.W * R * V) + (warp * R + r) * V;
 
   const size_t ring_bytes = (size_t)a.S * a.CL * a.layer_bytes;
-  const size_t dbuf_bytes = (OP == OP_BWD) ? (size_t)a.CL * a.dlayer_bytes : 0;
-  const size_t gst_layer = (size_t)np2 * (REAL ? 16 : 32);
+  constexpr bool kDT = (OP == OP_BWD && GR == 0);          // dT/dp tiles needed
+  const size_t dbuf_bytes = kDT ? (size_t)a.CL * a.dlayer_bytes : 0;
+  const size_t gst_layer = (size_t)np2 * (GR != 0 ? 8 : (REAL ? 16 : 32));
   const size_t gst_bytes = (OP == OP_BWD) ? (size_t)a.W * a.CL * gst_layer : 0;
   unsigned char* ring = smem;
   unsigned char* dbuf = smem + ring_bytes;
   unsigned char* gst = dbuf + dbuf_bytes;
   uint64_t* bars = reinterpret_cast<uint64_t*>(gst + gst_bytes);   // [S] ring, [S] = dT/dp buffer
+  int* skinds = reinterpret_cast<int*>(bars + a.S + 1);
+  const int* kinds = a.kinds;
+  if (a.L <= kMaxSmemKinds) {
+    for (int l = tid; l < a.L; l += blockDim.x) skinds[l] = __ldg(a.kinds + l);
+    kinds = skinds;
+  }
 
   F u[V][M];
   F w[V][M];
@@ -465,6 +635,7 @@ prop_kernel(const PropArgs a) {
   if (tid == 0) {
     for (; issued < min(a.S, nch); ++issued) issue(issued);
   }
+  unsigned char* gst_warp = gst + (size_t)warp * a.CL * gst_layer;
 
   for (int c = 0; c < nch; ++c) {
     const int lo = chunk_lo(c), hi = chunk_hi(c);
@@ -477,31 +648,14 @@ prop_kernel(const PropArgs a) {
       }
       return;
     }
-    if constexpr (OP == OP_BWD) {
+    if constexpr (kDT) {
       if (tid == 0) issue_d(c);
     }
     const unsigned char* st = ring + (size_t)(c % a.S) * a.CL * a.layer_bytes;
-    const int nl = hi - lo;
-    for (int i = 0; i < nl; ++i) {
-      const int l = (OP == OP_BWD) ? (hi - 1 - i) : (lo + i);
-      const int li = l - lo;
-      const int kind = __ldg(a.kinds + l);
-      const float4* tl = reinterpret_cast<const float4*>(st + (size_t)li * a.layer_bytes);
-      float4* gl = reinterpret_cast<float4*>(gst + ((size_t)warp * a.CL + li) * gst_layer);
-      switch (kind) {
-        case 0: layer_local<OP, M, V, REAL, 1>(tl, G, j, r, u, w, gl); break;
-        case 1: if constexpr (M >= 4) layer_local<OP, M, V, REAL, 2>(tl, G, j, r, u, w, gl); break;
-        case 2: if constexpr (M >= 8) layer_local<OP, M, V, REAL, 4>(tl, G, j, r, u, w, gl); break;
-        case 3: if constexpr (M >= 16) layer_local<OP, M, V, REAL, 8>(tl, G, j, r, u, w, gl); break;
-        case KIND_MIS: layer_mis<OP, M, V, REAL>(tl, G, j, r, u, w, gl); break;
-        default: {
-          const int d = 1 << (kind - KIND_XL - ilog2_const(M));
-          layer_xl<OP, M, V, REAL>(tl, d, G, j, r, u, w, gl);
-        }
-      }
-    }
+    run_chunk<OP, M, V, REAL, GR>(kinds, st, a.layer_bytes, lo, hi, gst_warp, gst_layer, G, j, r, u, w);
     __syncthreads();
-    if constexpr (OP == OP_BWD) {
+    if constexpr (OP == OP_BWD && GR != 0) chunk_reduce_direct<M, GR>(a, kinds, lo, hi - lo, gst, np2, G);
+    if constexpr (kDT) {
       const bool okd = mbar_wait_bounded(smem_u32(bars + a.S), (uint32_t)(c & 1));
       if (__syncthreads_or(!okd)) {
         if (tid == 0) {
@@ -510,7 +664,7 @@ prop_kernel(const PropArgs a) {
         }
         return;
       }
-      chunk_reduce<M, REAL>(a, lo, nl, gst, dbuf, np2);
+      chunk_reduce<M, REAL>(a, kinds, lo, hi - lo, gst, dbuf, np2, G);
     }
     if (tid == 0 && issued < nch) issue(issued++);
   }
