@@ -118,6 +118,17 @@ int mg_backdiff_ft(int N, int L, int B, const int* strides, const float* p, floa
                    int lds, const void* u_out, const void* dJdu_out, void* u_in, void* dJdu_in, int ldu, int crossing,
                    int accumulate, void* workspace, size_t workspace_bytes, void* stream);
 
+/* Forward propagation like mg_fwdprop (nearest-neighbour geometry), for callers that cannot allocate
+ * device memory - code that runs inside a stream capture, plugin hosts that forbid allocations, loops
+ * that must not touch an allocator - and so cannot provide a workspace.  No counterpart in the
+ * reference.  The scratch is an 8 MiB array compiled into the library (held on every GPU that loads
+ * it until exit); problems needing more return MG_E_WORKSPACE without launching.  The first call on
+ * each device looks up the array's device address and should come before any stream capture.  All
+ * calls share the array, so calls that overlap on the GPU race: serialise them.  Kernel status codes
+ * are not reported by this entry point. */
+int mg_fwdprop_noalloc(int N, int L, int B, const int* lens, const int* shifts, const float* p, int ldp,
+                       const float* s, int lds, const void* u_in, void* u_out, int ldu, int crossing, void* stream);
+
 /* ---- programmed-mesh entry points (coefficients kept resident between calls) -----------------
  * mg_build_tiles runs only the coefficient precompute of `op` into the workspace; mg_propagate runs
  * only the propagation kernel on tiles built earlier with the same (op, N, L, crossing, geometry,

@@ -40,6 +40,8 @@ _SIGS = {
     "mg_default_config": (c_int, [c_int, c_int, c_int, c_int, POINTER(mg_config)]),
     "mg_fwdprop": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p,
                            c_void_p, c_int, c_int, c_void_p, c_size_t, c_void_p]),
+    "mg_fwdprop_noalloc": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int,
+                                   c_void_p, c_void_p, c_int, c_int, c_void_p]),
     "mg_fwdprop_ft": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p,
                               c_int, c_int, c_void_p, c_size_t, c_void_p]),
     "mg_fwddiff": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int,

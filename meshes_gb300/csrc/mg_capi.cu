@@ -339,6 +339,19 @@ __global__ void fma_probe_kernel(float* sink, int iters, float m) {
 
 }  // namespace
 
+namespace mg {
+// Record an error message for mg_last_error() from another translation unit of the library.
+int set_last_error(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+}  // namespace mg
+
 extern "C" {
 
 const char* mg_last_error(void) { return g_err.c_str(); }

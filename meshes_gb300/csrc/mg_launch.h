@@ -46,6 +46,9 @@ inline int prop_max_threads(int op, int M, int V) {
 }
 
 // per-op dispatchers (one translation unit each, compiled in parallel)
+// error message for mg_last_error(), set from any translation unit; returns `code`
+int set_last_error(int code, const char* fmt, ...);
+
 // full: a vector fills the warp (G = 32), selecting the compile-time-G instantiation;
 // gr: back-propagation gradient mode (0 dJ/dT + dT/dp tiles, 1 MZI direct, 2 orth direct)
 cudaError_t launch_prop(int op, bool real, int M, int V, bool full, int gr, const LaunchCfg& lc, const PropArgs& a);
