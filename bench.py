@@ -222,9 +222,21 @@ def run_ours(args, rank, world, local_rank):
     for w, n in ((ws_f, wsb_f), (ws_b, wsb_b)):
         _lib.check(lib.mg_workspace_init(w.data_ptr(), n, st), "mg_workspace_init")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # > 129 MB L2
-    launches_per_step = 5                                  # coef+prop (fwd), coef+prop+reduce (bwd)
+    launches_per_step = 4          # coefficient tiles, forward, back-propagation with fused L2, gradient reduce
 
     def step(xx, yy_t):
+        """One training step through the programmed-mesh C ABI: the back-propagation tiles are built once
+        and serve the forward pass too; dJ/dy* = 2 (y - y_t) is formed inside the backward kernel."""
+        _lib.check(lib.mg_build_tiles(2, N, L, 0, lens_d.data_ptr(), shifts_d.data_ptr(), None, 0, p_d.data_ptr(), ldp,
+                                      s_d.data_ptr(), lds, None, None, None, B, None, ws_b.data_ptr(), wsb_b, st),
+                   "mg_build_tiles")
+        _lib.check(lib.mg_propagate(3, N, L, B, 0, 0, xx.data_ptr(), None, y.data_ptr(), None, N, None, 0, 0, None,
+                                    ws_b.data_ptr(), wsb_b, st), "mg_propagate")
+        _lib.check(lib.mg_propagate_l2(N, L, B, 0, 0, y.data_ptr(), yy_t.data_ptr(), None, gin.data_ptr(), N,
+                                       dp.data_ptr(), ldp, 0, None, ws_b.data_ptr(), wsb_b, st), "mg_propagate_l2")
+
+    def step_dropin(xx, yy_t):
+        """The same step through the reference-shaped entry points (mg_fwdprop, mg_backdiff)."""
         _lib.check(lib.mg_fwdprop(N, L, B, lens_d.data_ptr(), shifts_d.data_ptr(), p_d.data_ptr(), ldp,
                                   s_d.data_ptr(), lds, xx.data_ptr(), y.data_ptr(), N, 0, ws_f.data_ptr(), wsb_f, st),
                    "mg_fwdprop")
@@ -265,6 +277,9 @@ def run_ours(args, rank, world, local_rank):
         times = timed(lambda: step(x, yt), args.steps)
         barrier()
     t_step = sum(times) / len(times)
+    for _ in range(3):
+        step_dropin(x, yt)
+    t_dropin = statistics.median(timed(lambda: step_dropin(x, yt), max(5, args.steps // 4)))
     status = max(lib.mg_read_status(ws_f.data_ptr(), 0, st), lib.mg_read_status(ws_b.data_ptr(), 0, st))
     if status != 0:
         raise RuntimeError("kernel status %d" % status)
@@ -273,18 +288,14 @@ def run_ours(args, rank, world, local_rank):
     x_pin = torch.from_numpy(x_h).pin_memory()
     yt_pin = torch.from_numpy(yt_h).pin_memory()
     dp_pin = torch.empty(dp.numel(), dtype=torch.float32).pin_memory()
-    loss_pin = torch.empty(1, dtype=torch.float32).pin_memory()
     xd = torch.empty_like(x)
     ytd = torch.empty_like(yt)
-    loss = torch.empty(1, dtype=torch.float32, device=dev)
 
     def e2e_step():
         xd.copy_(x_pin, non_blocking=True)
         ytd.copy_(yt_pin, non_blocking=True)
         step(xd, ytd)
-        loss.copy_((g.abs().square().sum() * 0.25).reshape(1))     # J = sum |y - y_t|^2
-        dp_pin.copy_(dp, non_blocking=True)
-        loss_pin.copy_(loss, non_blocking=True)
+        dp_pin.copy_(dp, non_blocking=True)                  # the step's result: dJ/dp
 
     for _ in range(max(1, args.warmup)):
         e2e_step()
@@ -293,7 +304,7 @@ def run_ours(args, rank, world, local_rank):
     barrier()
     t_e2e = sum(times_e2e) / len(times_e2e)
     h2d = 2 * x.numel() * 8
-    d2h = dp.numel() * 4 + 4
+    d2h = dp.numel() * 4
 
     # ---- roofline of the dominant kernel: the back-propagation kernel alone (tiles built once)
     def bwd_kernel():
@@ -340,6 +351,9 @@ def run_ours(args, rank, world, local_rank):
                    "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas" if world > 1 else "1 GPU"},
         "pct_fp32_peak": 100 * value / world * (FLOP_FWD + FLOP_BWD) / peak,
         "fp32_peak_tflops": peak / 1e12,
+        "step": "programmed mesh: mg_build_tiles(bwd) + mg_propagate(fwd from bwd tiles) + mg_propagate_l2",
+        "drop_in_step": {"ms": t_dropin * 1e3, "mzi_per_s": units / world / t_dropin,
+                         "path": "mg_fwdprop + 2(y - y_t) + mg_backdiff (reference-shaped entry points)"},
         "kernels": {"fwd_prop_ms": t_fwd * 1e3, "bwd_prop_ms": t_bwd * 1e3,
                     "fwd_mzi_per_s": n_mzi * B / t_fwd, "bwd_mzi_per_s": n_mzi * B / t_bwd},
         "roofline": {"kernel": "prop_kernel<BWD> (back-propagation)", "bound": "fp32", "achieved": achieved / 1e12,
@@ -354,6 +368,194 @@ def run_ours(args, rank, world, local_rank):
     print(json.dumps(line))
 
 
+def make_batched_problem(seed=1003, n_meshes=512):
+    """512 meshes drawn 1:1:1 from Clements-mzi, Reck-mzi (native 2N-3 layers) and Clements-orth,
+    N uniform in {8, ..., 256}, batch uniform in [1, 2048], phases U[0, 2pi), splitters N(0, 0.01)."""
+    from meshes_gb300 import geometry as gm
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_meshes):
+        kind = ("clements-mzi", "reck-mzi", "clements-orth")[i % 3]
+        N = int(rng.choice([8, 16, 32, 64, 128, 256]))
+        B = int(rng.integers(1, 2049))
+        lens, shifts = gm.reck(N) if kind.startswith("reck") else gm.clements(N)
+        L = len(lens)
+        mask = gm.active_mask_nn(N, lens, shifts)
+        cr = "orth" if kind.endswith("orth") else "mzi"
+        n_p = 1 if cr == "orth" else 2
+        p = rng.uniform(0, 2 * np.pi, (L, N // 2, n_p)).astype(np.float32)
+        p[~mask] = 0
+        s = None
+        if cr == "mzi":
+            s = rng.normal(0, 0.01, (L, N // 2, 2)).astype(np.float32)
+            s[~mask] = 0
+        x = rng.standard_normal((B, N)) + (0 if cr == "orth" else 1j * rng.standard_normal((B, N)))
+        x = (x / np.linalg.norm(x, axis=1, keepdims=True)).astype(np.float32 if cr == "orth" else np.complex64)
+        out.append(dict(kind=kind, N=N, B=B, L=L, lens=lens, shifts=shifts, cr=cr, p=p, s=s, x=x,
+                        n_mzi=int(mask.sum())))
+    return out
+
+
+def run_batched(args):
+    """Batched uneven meshes: the one-mesh-per-call drop-in (mg_fwdprop / mg_backdiff per mesh) against
+    the persistent multi-mesh launch replayed from a CUDA graph; forward and forward + backward."""
+    import torch
+    from meshes_gb300 import MeshNetworkGPU, _lib
+    from meshes_gb300.batched import BatchedMeshes
+    lib = _lib.load()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    st = torch.cuda.current_stream().cuda_stream
+    prob = make_batched_problem()
+    meshes, bufs = [], []
+    for d in prob:
+        m = MeshNetworkGPU(d["N"], d["L"], d["lens"], d["shifts"], d["p"].reshape(-1), d["s"], d["cr"],
+                           is_phase=False, device=dev)
+        meshes.append(m)
+        x = torch.from_numpy(d["x"]).to(dev)
+        nbf = lib.mg_workspace_bytes(0, d["N"], d["L"], d["B"], m.crossing, 0, None)
+        nbb = lib.mg_workspace_bytes(2, d["N"], d["L"], d["B"], m.crossing, 0, None)
+        wf = torch.empty(nbf, dtype=torch.uint8, device=dev)
+        wb = torch.empty(nbb, dtype=torch.uint8, device=dev)
+        lib.mg_workspace_init(wf.data_ptr(), nbf, st)
+        lib.mg_workspace_init(wb.data_ptr(), nbb, st)
+        bufs.append(dict(x=x, y=torch.empty_like(x), g=torch.randn_like(x) if x.is_complex() else torch.randn_like(x),
+                         gi=torch.empty_like(x), dp=torch.empty(m.p_phase.numel(), device=dev),
+                         wf=(wf, nbf), wb=(wb, nbb)))
+    units = sum(d["n_mzi"] * d["B"] for d in prob)
+
+    def plain(backward):
+        for d, m, b in zip(prob, meshes, bufs):
+            sp = m.p_splitter
+            sptr = sp.data_ptr() if sp.numel() else None
+            ldp, lds = d["N"] // 2 * m.X_np, d["N"] // 2 * m.X_ns
+            _lib.check(lib.mg_fwdprop(d["N"], d["L"], d["B"], m.lens.data_ptr(), m.shifts.data_ptr(),
+                                      m.p_phase.data_ptr(), ldp, sptr, lds, b["x"].data_ptr(), b["y"].data_ptr(),
+                                      d["N"], m.crossing, b["wf"][0].data_ptr(), b["wf"][1], st), "mg_fwdprop")
+            if backward:
+                _lib.check(lib.mg_backdiff(d["N"], d["L"], d["B"], m.lens.data_ptr(), m.shifts.data_ptr(),
+                                           m.p_phase.data_ptr(), b["dp"].data_ptr(), ldp, sptr, lds,
+                                           b["y"].data_ptr(), b["g"].data_ptr(), None, b["gi"].data_ptr(), d["N"],
+                                           m.crossing, 0, b["wb"][0].data_ptr(), b["wb"][1], st), "mg_backdiff")
+
+    bm = BatchedMeshes(meshes, [d["B"] for d in prob])
+    for stt, b in zip(bm.states, bufs):
+        stt.x.copy_(b["x"])
+        stt.gy.copy_(b["g"])
+    g_f = BatchedMeshes.capture(bm, backward=False)
+    bm2 = bm
+    g_fb = torch.cuda.CUDAGraph()
+    bm2.step(True)
+    torch.cuda.synchronize()
+    with torch.cuda.graph(g_fb):
+        bm2.step(True)
+
+    def t_of(fn, k):
+        for _ in range(max(2, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(k):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) * 1e-3 / k
+
+    k = max(3, min(args.steps, 20))
+    t_plain_f = t_of(lambda: plain(False), k)
+    t_plain_fb = t_of(lambda: plain(True), k)
+    t_bat_f = t_of(g_f.replay, k)
+    t_bat_fb = t_of(g_fb.replay, k)
+    status = bm.check_status()
+    line = {"metric": "MZI-apps/s (batched uneven meshes, fwd+bwd)", "value": units / t_bat_fb, "unit": "MZI-apps/s",
+            "n_gpus": 1, "steps": k, "warmup": args.warmup, "ms_per_step": t_bat_fb * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64/f32", "data": "synthetic (seeded)",
+            "config": {"workload": "batched_512_meshes_clements_reck_orth_N8-256_B1-2048", "meshes": len(prob),
+                       "mzi_apps_per_pass": units, "items": bm.n_items, "graph": True},
+            "batched": {"fwd_mzi_per_s": units / t_bat_f, "fwdbwd_mzi_per_s": units / t_bat_fb,
+                        "fwd_ms": t_bat_f * 1e3, "fwdbwd_ms": t_bat_fb * 1e3},
+            "plain_one_mesh_per_call": {"fwd_mzi_per_s": units / t_plain_f, "fwdbwd_mzi_per_s": units / t_plain_fb,
+                                        "fwd_ms": t_plain_f * 1e3, "fwdbwd_ms": t_plain_fb * 1e3},
+            "speedup_batched_vs_plain": {"fwd": t_plain_f / t_bat_f, "fwdbwd": t_plain_fb / t_bat_fb},
+            "status": status}
+    print(json.dumps(line))
+
+
+def run_serve(args):
+    """Served mixed traffic: 64 resident meshes (Clements / log-depth butterfly, N in {16..512}, splitters
+    N(0, 0.02)), Poisson arrivals at 20k req/s, uniform mesh choice, batch log-uniform in [1, 512],
+    80% forward / 20% gradient requests; p50/p99 latency from arrival to result and MZI-apps/s."""
+    import torch
+    from meshes_gb300 import MeshNetworkGPU
+    from meshes_gb300 import geometry as gm
+    from meshes_gb300.serve import MeshServer
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(1005)
+    meshes, pools = [], []
+    for i in range(64):
+        N = int(rng.choice([16, 32, 64, 128, 256, 512]))
+        if i % 2 == 0:
+            lens, shifts = gm.clements(N)
+            L, strides = len(lens), None
+            mask = gm.active_mask_nn(N, lens, shifts)
+        else:
+            strides = gm.fft(N)
+            lens = shifts = None
+            L = len(strides)
+            mask = np.ones((L, N // 2), bool)
+        p = rng.uniform(0, 2 * np.pi, (L, N // 2, 2)).astype(np.float32)
+        s = rng.normal(0, 0.02, (L, N // 2, 2)).astype(np.float32)
+        p[~mask] = 0
+        s[~mask] = 0
+        meshes.append(MeshNetworkGPU(N, L, lens, shifts, p.reshape(-1), s, "mzi", is_phase=False, strides=strides,
+                                     device=dev))
+        x = rng.standard_normal((512, N)) + 1j * rng.standard_normal((512, N))
+        pools.append((x / np.linalg.norm(x, axis=1, keepdims=True)).astype(np.complex64))
+    srv = MeshServer(meshes, mem_budget=512 << 20)
+    n_mzi = [(sum(m.lens_h) if m.strides is None else m.L * (m.N // 2)) for m in meshes]
+    rate, duration = 20000.0, float(args.duration)
+    n_req = int(rate * duration)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    mesh_ids = rng.integers(0, 64, n_req)
+    bsz = np.clip(np.round(np.exp(rng.uniform(0, np.log(512), n_req))), 1, 512).astype(int)
+    grad = rng.random(n_req) < 0.2
+    srv.start()
+    # warm-up: one request per mesh
+    for i in range(64):
+        srv.submit(i, pools[i][:4]).result(60)
+    futs = []
+    t0 = time.perf_counter()
+    k = 0
+    while k < n_req:
+        now = time.perf_counter() - t0
+        while k < n_req and arrivals[k] <= now:
+            i, b = int(mesh_ids[k]), int(bsz[k])
+            x = pools[i][:b]
+            f = srv.submit(i, x, gy=x if grad[k] else None)
+            futs.append((k, f))
+            k += 1
+        time.sleep(20e-6)
+    for _, f in futs:
+        f.result(120)
+    t_end = max(f.t_done for _, f in futs)
+    srv.stop()
+    # latency of each request: result available on the host minus its scheduled arrival time
+    lat = np.array([f.t_done - (t0 + arrivals[kk]) for kk, f in futs])
+    apps = sum(n_mzi[int(mesh_ids[kk])] * int(bsz[kk]) * (2 if grad[kk] else 1) for kk, _ in futs)
+    span = t_end - t0
+    line = {"metric": "serve p50/p99 latency (ms) and MZI-apps/s", "value": float(np.percentile(lat, 50) * 1e3),
+            "unit": "ms (p50 latency)", "n_gpus": 1, "steps": len(futs), "warmup": 64, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded Poisson stream)",
+            "config": {"workload": "serve_64_meshes_clements_butterfly_N16-512_20k_req_s", "rate_req_s": rate,
+                       "duration_s": duration, "requests": len(futs), "grad_fraction": float(grad.mean())},
+            "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "throughput_mzi_apps_per_s": apps / span, "served_req_per_s": len(futs) / span, "ticks": srv.ticks,
+            "status": srv.kernel_status()}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -361,12 +563,20 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--profile", action="store_true", help="two untimed steps only (for ncu captures)")
+    ap.add_argument("--workload", default="clements256", choices=["clements256", "batched", "serve"],
+                    help="clements256: the headline fwd+bwd step; batched: 512 uneven meshes, plain vs "
+                         "persistent; serve: Poisson request stream on 64 resident meshes")
+    ap.add_argument("--duration", type=float, default=10.0, help="serve workload: seconds of traffic")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.workload in ("batched", "serve"):
+        if rank == 0:
+            (run_batched if args.workload == "batched" else run_serve)(args)
         return
     if world > 1:
         import torch

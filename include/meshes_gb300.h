@@ -36,6 +36,7 @@ extern "C" {
 #define MG_OP_FWD 0
 #define MG_OP_FWDDIFF 1
 #define MG_OP_BWD 2
+#define MG_OP_FWD_BWDTILES 3   /* mg_propagate only: forward reading back-propagation tiles */
 #define MG_GEO_NN 0
 #define MG_GEO_FFT 1
 
@@ -77,6 +78,11 @@ int mg_workspace_init(void* workspace, size_t workspace_bytes, void* stream);
 
 /* Synchronise `stream`, return the workspace's status word (MG_ST_*), clear it if `clear`. */
 int mg_read_status(void* workspace, int clear, void* stream);
+
+/* Register a measured configuration for (op, crossing, geometry, N) and batch sizes B in [B_lo, B_hi];
+ * calls that pass no config then use it instead of the heuristic.  cfg = NULL removes the entries of
+ * that (op, crossing, geometry, N) (N = 0: all N).  Filled by meshes_gb300.autotune. */
+int mg_set_tuned(int op, int crossing, int geometry, int N, int B_lo, int B_hi, const mg_config* cfg);
 
 /* The configuration the heuristic picks (filled into *out). */
 int mg_default_config(int op, int N, int B, int crossing, mg_config* out);
@@ -139,9 +145,65 @@ int mg_build_tiles(int op, int N, int L, int geometry, const int* lens, const in
                    int crossing, const float* p, int ldp, const float* s, int lds, const float* dp, const void* Tgen,
                    const void* Dgen, int B, const mg_config* cfg, void* workspace, size_t workspace_bytes, void* stream);
 
+/* op MG_OP_FWD_BWDTILES runs the forward kernel on tiles built for MG_OP_BWD (nearest-neighbour
+ * geometry), so one coefficient pass serves a forward propagation and its back-propagation. */
 int mg_propagate(int op, int N, int L, int B, int crossing, int geometry, const void* in0, const void* in1, void* out0,
                  void* out1, int ldu, float* dp, int ldp, int accumulate, const mg_config* cfg, void* workspace,
                  size_t workspace_bytes, void* stream);
+
+/* Plan of one launch (for hosts that manage tiles themselves, e.g. the batched engine). */
+typedef struct mg_plan_info {
+  int M, V, W, CL, S, G, grid;
+  unsigned layer_bytes, dlayer_bytes;
+  size_t smem, off_kinds, off_tiles, off_dtiles, off_partial, total;
+} mg_plan_info;
+int mg_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_config* cfg, mg_plan_info* out);
+
+/* ---- batched meshes: one persistent launch over a (mesh, batch-tile) work queue ----------------
+ * Each mesh's coefficient tiles are built beforehand with mg_build_tiles into its own workspace, with
+ * the tile configuration of its kernel class and W = 8 (the persistent CTA width):
+ *   MG_BCLS_C8  : complex64, M = 8,  N <= 256   (fwd V = 4, bwd V = 4, mzi)
+ *   MG_BCLS_C16 : complex64, M = 16, N <= 512   (fwd V = 2, bwd V = 2, mzi)
+ *   MG_BCLS_R8  : float32,   M = 8,  N <= 256   (fwd V = 4, bwd V = 4, orth)
+ * Work items cover vectors [v0, vend) of one mesh; CTAs take items from a device counter (`head`,
+ * zeroed by the caller before each launch, e.g. a memset node of a captured CUDA graph) in array
+ * order, so items sorted longest-first balance the load.  Back-propagation items write partials
+ * at mesh.partial + part * L * Np/2 (float2); mg_batched_reduce sums them in order into mesh.dp. */
+#define MG_BCLS_C8 0
+#define MG_BCLS_C16 1
+#define MG_BCLS_R8 2
+typedef struct mg_batch_mesh {
+  int N, L, B, ldu;
+  int cls, G, CL, S;
+  unsigned layer_bytes;
+  int n_items, ldp, n_p;
+  const void* tiles;     /* workspace + off_tiles of the mesh's mg_build_tiles */
+  const int* kinds;      /* workspace + off_kinds */
+  const void* in0;       /* fwd: x; bwd: y */
+  const void* in1;       /* bwd: dJ/dy* */
+  void* out0;            /* fwd: y; bwd: x (may be NULL) */
+  void* out1;            /* bwd: dJ/dx* */
+  float* dp;             /* bwd: dJ/dp (L, N/2, n_p), overwritten by mg_batched_reduce */
+  void* partial;         /* bwd: n_items * L * Np/2 float2 */
+} mg_batch_mesh;
+typedef struct mg_batch_item {
+  int mesh, v0, vend, part;
+} mg_batch_item;
+
+/* Persistent launch of `grid` CTAs of 256 threads with `smem` bytes of dynamic shared memory (the
+ * maximum mg_plan_info.smem of the meshes' W = 8 plans).  op is MG_OP_FWD or MG_OP_BWD.  Kernel
+ * status (bad work item, expired wait) goes to *status (device int, zeroed by the caller). */
+int mg_batched_propagate(int op, const mg_batch_mesh* meshes, int n_meshes, const mg_batch_item* items, int n_items,
+                         int* head, int grid, size_t smem, int* status, void* stream);
+/* Deterministic sum of the back-propagation partials of every mesh into its dp. */
+int mg_batched_reduce(const mg_batch_mesh* meshes, int n_meshes, void* stream);
+
+/* Back-propagation with the L2 loss to a target fused into the kernel: dJ/dy* = 2 (y - target) is
+ * formed on load (J = sum |y - target|^2), then as mg_propagate(MG_OP_BWD) with tiles built earlier.
+ * The reference computes this gradient in a separate pass (gpu/mesh.py:176-181, 219-221). */
+int mg_propagate_l2(int N, int L, int B, int crossing, int geometry, const void* y, const void* target, void* x_out,
+                    void* g_out, int ldu, float* dp, int ldp, int accumulate, const mg_config* cfg, void* workspace,
+                    size_t workspace_bytes, void* stream);
 
 /* ---- measurement helpers -------------------------------------------------------------------- */
 

@@ -12,3 +12,15 @@ from . import geometry  # noqa: F401
 from .mesh import MeshNetworkGPU, from_structured  # noqa: F401
 
 __version__ = "0.1.0"
+
+
+def _load_tuning():
+    """Load the committed autotuning table into the library (silently skipped without the library)."""
+    try:
+        from .autotune import load_table
+        load_table()
+    except (MeshLibraryError, OSError):
+        pass
+
+
+_load_tuning()

@@ -8,13 +8,13 @@ from __future__ import annotations
 import ctypes
 import os
 import threading
-from ctypes import POINTER, Structure, c_char_p, c_int, c_size_t, c_void_p
+from ctypes import POINTER, Structure, c_char_p, c_int, c_size_t, c_uint, c_void_p
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libmeshes_gb300.so")
 
 MZI, SYM, ORTH, GENERIC = 0, 1, 2, 3
-OP_FWD, OP_FWDDIFF, OP_BWD = 0, 1, 2
+OP_FWD, OP_FWDDIFF, OP_BWD, OP_FWD_BWDTILES = 0, 1, 2, 3
 GEO_NN, GEO_FFT = 0, 1
 CROSSING_CODES = {"mzi": MZI, "sym": SYM, "orth": ORTH, "generic": GENERIC}
 STATUS_NAMES = {0: "ok", 1: "timeout", 2: "bad geometry", 3: "bad work item"}
@@ -31,6 +31,24 @@ class mg_config(Structure):
         return (self.M, self.V, self.W, self.CL, self.S)
 
 
+class mg_plan_info(Structure):
+    _fields_ = [("M", c_int), ("V", c_int), ("W", c_int), ("CL", c_int), ("S", c_int), ("G", c_int),
+                ("grid", c_int), ("layer_bytes", c_uint), ("dlayer_bytes", c_uint), ("smem", c_size_t),
+                ("off_kinds", c_size_t), ("off_tiles", c_size_t), ("off_dtiles", c_size_t),
+                ("off_partial", c_size_t), ("total", c_size_t)]
+
+
+class mg_batch_mesh(Structure):
+    _fields_ = [("N", c_int), ("L", c_int), ("B", c_int), ("ldu", c_int), ("cls", c_int), ("G", c_int),
+                ("CL", c_int), ("S", c_int), ("layer_bytes", c_uint), ("n_items", c_int), ("ldp", c_int),
+                ("n_p", c_int), ("tiles", c_void_p), ("kinds", c_void_p), ("in0", c_void_p), ("in1", c_void_p),
+                ("out0", c_void_p), ("out1", c_void_p), ("dp", c_void_p), ("partial", c_void_p)]
+
+
+class mg_batch_item(Structure):
+    _fields_ = [("mesh", c_int), ("v0", c_int), ("vend", c_int), ("part", c_int)]
+
+
 _SIGS = {
     "mg_last_error": (c_char_p, []),
     "mg_version": (c_char_p, []),
@@ -38,6 +56,7 @@ _SIGS = {
     "mg_workspace_init": (c_int, [c_void_p, c_size_t, c_void_p]),
     "mg_read_status": (c_int, [c_void_p, c_int, c_void_p]),
     "mg_default_config": (c_int, [c_int, c_int, c_int, c_int, POINTER(mg_config)]),
+    "mg_set_tuned": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, POINTER(mg_config)]),
     "mg_fwdprop": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p,
                            c_void_p, c_int, c_int, c_void_p, c_size_t, c_void_p]),
     "mg_fwdprop_noalloc": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int,
@@ -58,7 +77,14 @@ _SIGS = {
                                c_size_t, c_void_p]),
     "mg_propagate": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
                              c_void_p, c_int, c_int, POINTER(mg_config), c_void_p, c_size_t, c_void_p]),
+    "mg_propagate_l2": (c_int, [c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
+                                c_void_p, c_int, c_int, POINTER(mg_config), c_void_p, c_size_t, c_void_p]),
     "mg_fma_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
+    "mg_plan": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, POINTER(mg_config), POINTER(mg_plan_info)]),
+    # mesh and item arrays live in device memory: passed as raw addresses
+    "mg_batched_propagate": (c_int, [c_int, c_void_p, c_int, c_void_p, c_int, c_void_p, c_int, c_size_t, c_void_p,
+                                     c_void_p]),
+    "mg_batched_reduce": (c_int, [c_void_p, c_int, c_void_p]),
 }
 
 _lock = threading.Lock()

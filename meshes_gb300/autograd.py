@@ -1,0 +1,122 @@
+"""torch.autograd integration: y = U(p) x through the sm_103a kernels.
+
+``mesh_apply(mesh, x, p)`` propagates a batch ``x`` (B, N) (rows are vectors, complex64; float32 for
+orth meshes) through ``mesh`` (a MeshNetworkGPU giving the geometry, the crossing and the splitter
+errors) with phases ``p`` (L, N/2, n_p) and returns y (B, N).  Gradients flow to x and p.
+
+Complex convention: PyTorch's gradient of a real loss with respect to a complex tensor is
+2 dL/dz*, the reference's dJ/dv convention (gpu/mesh.py:176-181, mesh.py:376), so the backward
+passes ``grad_output`` to the back-propagation kernel unchanged and returns its input gradient as is.
+
+Lossless crossings (mzi, sym, orth) store nothing for the backward pass but the output y: the kernel
+rebuilds each layer's input with T^H, as the reference's backdiff does.  For nearest-neighbour meshes
+the forward pass already builds the back-propagation coefficient tiles (one coefficient pass per
+training step) and the backward pass reuses them unless another call rebuilt them meanwhile.
+"""
+from __future__ import annotations
+
+from typing import Optional
+
+import torch
+
+from . import _lib
+from ._lib import GEO_NN, OP_BWD, OP_FWD, OP_FWD_BWDTILES, check, load
+from .mesh import MeshNetworkGPU, _stream
+
+
+class _Plan:
+    """Workspace cache of one (mesh, op, batch) combination."""
+
+    def __init__(self, mesh: MeshNetworkGPU, op: int):
+        self.mesh, self.op = mesh, op
+        self.buf: Optional[torch.Tensor] = None
+
+    def workspace(self, B: int):
+        m = self.mesh
+        nb = load().mg_workspace_bytes(self.op, m.N, m.L, B, m.crossing, m.geometry,
+                                       _lib.cfg_ptr(m.config.get(self.op)))
+        if nb == 0:
+            check(-1, "mg_workspace_bytes")
+        if self.buf is None or self.buf.numel() < nb:
+            self.buf = torch.empty(nb, dtype=torch.uint8, device=m.device)
+            check(load().mg_workspace_init(self.buf.data_ptr(), nb, _stream(m.device)), "mg_workspace_init")
+        return self.buf.data_ptr(), self.buf.numel()
+
+
+def _plans(mesh: MeshNetworkGPU):
+    p = getattr(mesh, "_autograd_plans", None)
+    if p is None:
+        p = {OP_FWD: _Plan(mesh, OP_FWD), OP_BWD: _Plan(mesh, OP_BWD)}
+        mesh._autograd_plans = p
+    return p
+
+
+def _build(mesh: MeshNetworkGPU, op: int, p: torch.Tensor, B: int):
+    """Build op's tiles for phases p into the mesh's cached workspace; returns (ws, bytes, version)."""
+    lib = load()
+    plan_ = _plans(mesh)[op]
+    ws, nb = plan_.workspace(B)
+    plan_.version = getattr(plan_, "version", 0) + 1
+    s = mesh.p_splitter
+    geo = ((None, None, mesh.strides.data_ptr()) if mesh.strides is not None
+           else (mesh.lens.data_ptr(), mesh.shifts.data_ptr(), None))
+    check(lib.mg_build_tiles(op, mesh.N, mesh.L, mesh.geometry, *geo, mesh.crossing, p.data_ptr(),
+                             mesh.N // 2 * mesh.X_np, s.data_ptr() if s.numel() else None, mesh.N // 2 * mesh.X_ns,
+                             None, None, None, B, _lib.cfg_ptr(mesh.config.get(op)), ws, nb, _stream(mesh.device)),
+          "mg_build_tiles")
+    return ws, nb, plan_.version
+
+
+class MeshFunction(torch.autograd.Function):
+    """y = U(p) x for a lossless mesh; backward returns (dL/dx*·2, dL/dp)."""
+
+    @staticmethod
+    def forward(ctx, x: torch.Tensor, p: torch.Tensor, mesh: MeshNetworkGPU):
+        lib = load()
+        x = x.contiguous()
+        p = p.detach().to(torch.float32).contiguous()
+        B, N = x.shape
+        assert N == mesh.N, "x must be (B, N) with N=%d" % mesh.N
+        y = torch.empty_like(x)
+        shared = mesh.geometry == GEO_NN
+        if shared:      # back-propagation tiles serve the forward kernel and, later, the backward
+            ws, nb, ver = _build(mesh, OP_BWD, p, B)
+            op, cfg = OP_FWD_BWDTILES, mesh.config.get(OP_BWD)
+        else:
+            ws, nb, ver = _build(mesh, OP_FWD, p, B)
+            op, cfg = OP_FWD, mesh.config.get(OP_FWD)
+        check(lib.mg_propagate(op, N, mesh.L, B, mesh.crossing, mesh.geometry, x.data_ptr(), None, y.data_ptr(),
+                               None, N, None, 0, 0, _lib.cfg_ptr(cfg), ws, nb, _stream(mesh.device)), "mg_propagate")
+        ctx.mesh = mesh
+        ctx.tiles_version = ver if shared else None
+        ctx.save_for_backward(y, p)
+        return y
+
+    @staticmethod
+    def backward(ctx, gy: torch.Tensor):
+        lib = load()
+        y, p = ctx.saved_tensors
+        mesh = ctx.mesh
+        B, N = y.shape
+        gy = gy.contiguous()
+        plan_ = _plans(mesh)[OP_BWD]
+        if ctx.tiles_version is not None and getattr(plan_, "version", None) == ctx.tiles_version:
+            ws, nb = plan_.workspace(B)               # tiles of this forward are still in place
+        else:
+            ws, nb, _ = _build(mesh, OP_BWD, p, B)
+        gx = torch.empty_like(gy)
+        dp = torch.empty(p.numel(), dtype=torch.float32, device=y.device)
+        check(lib.mg_propagate(OP_BWD, N, mesh.L, B, mesh.crossing, mesh.geometry, y.data_ptr(), gy.data_ptr(), None,
+                               gx.data_ptr(), N, dp.data_ptr(), N // 2 * mesh.X_np, 0,
+                               _lib.cfg_ptr(mesh.config.get(OP_BWD)), ws, nb, _stream(mesh.device)), "mg_propagate")
+        return gx, dp.view_as(p), None
+
+
+def mesh_apply(mesh: MeshNetworkGPU, x: torch.Tensor, p: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """Differentiable y = U(p) x; x (B, N), p (L, N/2, n_p) (defaults to the mesh's own phases)."""
+    if p is None:
+        p = mesh.p_crossing
+    dtype = mesh.dtype
+    if x.dtype != dtype:
+        x = x.to(dtype)
+    return MeshFunction.apply(x, p, mesh)

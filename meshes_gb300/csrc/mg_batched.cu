@@ -1,0 +1,131 @@
+// Persistent multi-mesh propagation: one launch drains a (mesh, batch-tile) work queue.
+//
+// Every CTA (256 threads, one per SM) repeatedly takes the next work item from a device counter and
+// runs the same per-tile body as the one-mesh kernel (prop_body) on it: the item's mesh descriptor
+// gives N, L, the coefficient tiles (built beforehand and kept resident) and the field pointers; the
+// item gives the vector range.  Meshes of different N and depth share one launch; the kernel class
+// of a mesh (complex M = 8, complex M = 16, real M = 8) selects the compiled body, the lane count
+// G = N/M is a run-time value.  Items are taken in array order, so a host that sorts them
+// longest-first gets longest-processing-time scheduling.
+#include <cuda_runtime.h>
+
+#include "../../include/meshes_gb300.h"
+#include "mg_launch.h"
+
+namespace mg {
+namespace {
+
+constexpr int kBatchWarps = 8;
+
+__device__ __forceinline__ int cls_M(int cls) { return cls == MG_BCLS_C16 ? 16 : 8; }
+
+template <int OP>
+__global__ void __launch_bounds__(kBatchWarps * 32, 1)
+batched_kernel(const mg_batch_mesh* __restrict__ meshes, int n_meshes, const mg_batch_item* __restrict__ items,
+               int n_items, int* head, int* status) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ int s_item;
+  for (;;) {
+    __syncthreads();                       // previous item fully done (barriers, smem reuse)
+    if (threadIdx.x == 0) s_item = atomicAdd(head, 1);
+    __syncthreads();
+    const int i = s_item;
+    if (i >= n_items) return;
+    const mg_batch_item it = items[i];
+    if (it.mesh < 0 || it.mesh >= n_meshes) {
+      if (threadIdx.x == 0) set_status(status, ST_BAD_WORK);
+      continue;
+    }
+    const mg_batch_mesh md = meshes[it.mesh];
+    const int M = cls_M(md.cls);
+    if (md.G < 1 || md.G > 32 || (md.G & (md.G - 1)) || md.G * M < md.N || it.v0 < 0 || it.vend > md.B) {
+      if (threadIdx.x == 0) set_status(status, ST_BAD_WORK);
+      continue;
+    }
+    PropArgs a;
+    a.N = md.N; a.L = md.L; a.B = md.B; a.ldu = md.ldu;
+    a.G = md.G; a.logG = 31 - __clz(md.G); a.W = kBatchWarps; a.CL = md.CL; a.S = md.S;
+    a.layer_bytes = md.layer_bytes; a.dlayer_bytes = 0;
+    a.tiles = static_cast<const unsigned char*>(md.tiles); a.dtiles = nullptr;
+    a.kinds = md.kinds;
+    a.in0 = md.in0; a.in1 = md.in1; a.out0 = md.out0; a.out1 = md.out1;
+    a.partial = (OP == OP_BWD) ? static_cast<float2*>(md.partial) + (size_t)it.part * md.L * (md.G * M / 2) : nullptr;
+    a.status = status;
+    a.v0 = it.v0; a.vend = it.vend;
+    a.target = nullptr;
+    switch (md.cls) {
+      case MG_BCLS_C8: prop_body<OP, 8, 4, false, 0, (OP == OP_BWD ? 1 : 0)>(a, smem); break;
+      case MG_BCLS_C16: prop_body<OP, 16, 2, false, 0, (OP == OP_BWD ? 1 : 0)>(a, smem); break;
+      case MG_BCLS_R8: prop_body<OP, 8, 4, true, 0, (OP == OP_BWD ? 2 : 0)>(a, smem); break;
+      default:
+        if (threadIdx.x == 0) set_status(status, ST_BAD_WORK);
+    }
+  }
+}
+
+// one CTA per mesh: dp[l][q][k] = sum over the mesh's items (in order) of the partials
+__global__ void batched_reduce_kernel(const mg_batch_mesh* __restrict__ meshes) {
+  const mg_batch_mesh md = meshes[blockIdx.x];
+  if (!md.dp || !md.partial || md.n_items <= 0) return;
+  const int M = cls_M(md.cls), G = md.G, np2 = G * M / 2, L = md.L, N = md.N;
+  const int* geo = md.kinds + L;
+  const float2* part = static_cast<const float2*>(md.partial);
+  const size_t stride = (size_t)L * np2;
+  for (int idx = threadIdx.x; idx < L * np2; idx += blockDim.x) {
+    const int l = idx / np2, pos = idx - l * np2;
+    const int q = pos_slot(pos, M, G);
+    if (q >= N / 2) continue;
+    const int sh = geo[2 * l], ln = geo[2 * l + 1];
+    float sx = 0.f, sy = 0.f;
+    if (q >= sh / 2 && q < sh / 2 + ln) {
+      const float2* p = part + (size_t)l * np2 + pos;
+      for (int k = 0; k < md.n_items; ++k) {
+        const float2 v = p[(size_t)k * stride];
+        sx += v.x;
+        sy += v.y;
+      }
+    }
+    float* o = md.dp + (size_t)l * md.ldp + (size_t)q * md.n_p;
+    o[0] = sx;
+    if (md.n_p > 1) o[1] = sy;
+  }
+}
+
+}  // namespace
+}  // namespace mg
+
+using namespace mg;
+
+extern "C" int mg_batched_propagate(int op, const mg_batch_mesh* meshes, int n_meshes, const mg_batch_item* items,
+                                    int n_items, int* head, int grid, size_t smem, int* status, void* stream) {
+  if (op != MG_OP_FWD && op != MG_OP_BWD) return set_last_error(MG_E_ARG, "batched op must be fwd or bwd");
+  if (!meshes || n_meshes < 0 || (!items && n_items > 0) || !head || grid < 1)
+    return set_last_error(MG_E_ARG, "batched launch: bad arguments");
+  if (n_items == 0) return MG_OK;
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (smem + 1024 > (size_t)optin) return set_last_error(MG_E_CONFIG, "batched smem %zu above %d", smem, optin);
+  (void)cudaGetLastError();   // start from a clean error state: launch errors below are this call's
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  if (op == MG_OP_FWD) {
+    static std::atomic<unsigned long long> done{0};
+    e = ensure_smem_attr(batched_kernel<OP_FWD>, done);
+    if (e == cudaSuccess) batched_kernel<OP_FWD><<<grid, kBatchWarps * 32, smem, st>>>(meshes, n_meshes, items, n_items, head, status);
+  } else {
+    static std::atomic<unsigned long long> done{0};
+    e = ensure_smem_attr(batched_kernel<OP_BWD>, done);
+    if (e == cudaSuccess) batched_kernel<OP_BWD><<<grid, kBatchWarps * 32, smem, st>>>(meshes, n_meshes, items, n_items, head, status);
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  return e == cudaSuccess ? MG_OK : set_last_error(MG_E_CUDA, "batched_kernel: %s", cudaGetErrorString(e));
+}
+
+extern "C" int mg_batched_reduce(const mg_batch_mesh* meshes, int n_meshes, void* stream) {
+  if (!meshes || n_meshes < 0) return set_last_error(MG_E_ARG, "batched reduce: bad arguments");
+  if (n_meshes == 0) return MG_OK;
+  batched_reduce_kernel<<<n_meshes, 256, 0, static_cast<cudaStream_t>(stream)>>>(meshes);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MG_OK : set_last_error(MG_E_CUDA, "batched_reduce_kernel: %s", cudaGetErrorString(e));
+}

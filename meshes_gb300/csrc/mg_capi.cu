@@ -14,6 +14,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/meshes_gb300.h"
 #include "mg_coeffs.cuh"
@@ -78,6 +79,24 @@ bool instantiated(int op, int M, int V) {
   return false;
 }
 
+// Tuning table: configurations measured by the autotuner, used when a call passes no config.
+struct Tuned {
+  int op, crossing, geometry, N, Blo, Bhi;
+  mg_config cfg;
+};
+std::mutex g_tuned_mu;
+std::vector<Tuned> g_tuned;
+
+bool lookup_tuned(int op, int crossing, int geometry, int N, int B, mg_config* out) {
+  std::lock_guard<std::mutex> lk(g_tuned_mu);
+  for (const Tuned& t : g_tuned)
+    if (t.op == op && t.crossing == crossing && t.geometry == geometry && t.N == N && B >= t.Blo && B <= t.Bhi) {
+      *out = t.cfg;
+      return true;
+    }
+  return false;
+}
+
 struct Plan {
   int op, N, L, B, crossing, geometry;
   bool real;
@@ -96,6 +115,8 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   if (N > 512) return fail(MG_E_ARG, "N=%d above the supported maximum 512", N);
   if (L < 0 || B < 0) return fail(MG_E_ARG, "L=%d, B=%d must be non-negative", L, B);
   const DevInfo di = dev_info();
+  mg_config tuned;
+  if (!cfg && lookup_tuned(op, crossing, geometry, N, B, &tuned)) cfg = &tuned;
   Plan& p = *P;
   p.op = op; p.N = N; p.L = L; p.B = B; p.crossing = crossing; p.geometry = geometry;
   p.real = crossing == CR_ORTH;
@@ -214,9 +235,10 @@ int build_tiles(const Plan& P, const int* lens, const int* shifts, const int* st
 }
 
 int run_prop(const Plan& P, const void* in0, const void* in1, void* out0, void* out1, int ldu, float* dp, int ldp,
-             int accumulate, unsigned char* ws, cudaStream_t st) {
+             int accumulate, unsigned char* ws, cudaStream_t st, const void* target = nullptr) {
   if (P.B == 0) return MG_OK;
   PropArgs a;
+  a.target = target;
   a.N = P.N; a.L = P.L; a.B = P.B; a.ldu = ldu;
   a.G = P.G; a.logG = P.logG; a.W = P.W; a.CL = P.CL; a.S = P.S;
   a.layer_bytes = P.lb; a.dlayer_bytes = P.dlb;
@@ -235,7 +257,8 @@ int run_prop(const Plan& P, const void* in0, const void* in1, void* out0, void* 
   if (e != cudaSuccess) return cuda_fail(e, "prop_kernel launch");
   if (P.op == OP_BWD && dp && P.L > 0) {
     const int n = P.L * P.np2;
-    dp_reduce_kernel<<<(n + 127) / 128, 128, 0, st>>>(a.partial, P.grid, P.L, P.np2, P.M, P.G, P.N, dp, ldp,
+    dp_reduce_kernel<<<(n + kReduceCols - 1) / kReduceCols, kReduceCols * kReduceRows, 0, st>>>(
+        a.partial, P.grid, P.L, P.np2, P.M, P.G, P.N, dp, ldp,
                                                         crossing_np(P.crossing), accumulate,
                                                         reinterpret_cast<const int*>(ws + P.off_kinds) + P.L);
     e = cudaGetLastError();
@@ -449,6 +472,31 @@ int mg_propagate(int op, int N, int L, int B, int crossing, int geometry, const 
                  void* out1, int ldu, float* dp, int ldp, int accumulate, const mg_config* cfg, void* ws, size_t wsb,
                  void* stream) {
   g_err.clear();
+  if (op == MG_OP_FWD_BWDTILES) {
+    // forward propagation reading the tiles mg_build_tiles(MG_OP_BWD) wrote: the layer stride and the
+    // workspace layout are the back-propagation plan's, the kernel is the forward one
+    if (geometry != GEO_NN) return fail(MG_E_ARG, "forward from back-propagation tiles needs nearest-neighbour geometry");
+    Plan Pb, Pf;
+    TRY(make_plan(OP_BWD, N, L, B, crossing, geometry, cfg, &Pb));
+    TRY(check_ws(Pb, ws, wsb));
+    mg_config cf = {Pb.M, 0, 0, 0, 0};
+    TRY(make_plan(OP_FWD, N, L, B, crossing, geometry, &cf, &Pf));
+    Pf.lb = Pb.lb;
+    Pf.off_kinds = Pb.off_kinds;
+    Pf.off_tiles = Pb.off_tiles;
+    const size_t budget = (size_t)dev_info().smem_optin - 1024;
+    for (;;) {
+      Pf.smem = prop_smem_bytes(OP_FWD, 0, Pf.M, Pf.G, Pf.W, Pf.CL, Pf.S, Pf.lb, 0, L);
+      if (Pf.smem <= budget && (size_t)Pf.CL * Pf.lb < (1u << 20)) break;
+      if (Pf.CL == 1) return fail(MG_E_CONFIG, "no pipeline depth fits shared memory");
+      Pf.CL = std::max(1, Pf.CL / 2);
+    }
+    TRY(check_ldu(Pf, ldu));
+    TRY(check_field(in0, "in0", Pf.real, B > 0));
+    TRY(check_field(out0, "out0", Pf.real, B > 0));
+    return run_prop(Pf, in0, nullptr, out0, nullptr, ldu, nullptr, 0, 0, static_cast<unsigned char*>(ws),
+                    static_cast<cudaStream_t>(stream));
+  }
   Plan P;
   TRY(make_plan(op, N, L, B, crossing, geometry, cfg, &P));
   TRY(check_ws(P, ws, wsb));
@@ -460,6 +508,56 @@ int mg_propagate(int op, int N, int L, int B, int crossing, int geometry, const 
   if (op == OP_BWD && dp && ldp < N / 2 * crossing_np(crossing)) return fail(MG_E_ARG, "ldp too small");
   return run_prop(P, in0, in1, out0, out1, ldu, dp, ldp, accumulate, static_cast<unsigned char*>(ws),
                   static_cast<cudaStream_t>(stream));
+}
+
+int mg_set_tuned(int op, int crossing, int geometry, int N, int B_lo, int B_hi, const mg_config* cfg) {
+  g_err.clear();
+  std::lock_guard<std::mutex> lk(g_tuned_mu);
+  if (!cfg) {   // clear every entry of this (op, crossing, geometry, N)
+    std::vector<Tuned> keep;
+    for (const Tuned& t : g_tuned)
+      if (!(t.op == op && t.crossing == crossing && t.geometry == geometry && (N == 0 || t.N == N))) keep.push_back(t);
+    g_tuned.swap(keep);
+    return MG_OK;
+  }
+  if (op < 0 || op > 2 || N < 2 || B_lo > B_hi) return fail(MG_E_ARG, "bad tuning entry");
+  for (Tuned& t : g_tuned)
+    if (t.op == op && t.crossing == crossing && t.geometry == geometry && t.N == N && t.Blo == B_lo && t.Bhi == B_hi) {
+      t.cfg = *cfg;
+      return MG_OK;
+    }
+  g_tuned.push_back(Tuned{op, crossing, geometry, N, B_lo, B_hi, *cfg});
+  return MG_OK;
+}
+
+int mg_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_config* cfg, mg_plan_info* out) {
+  g_err.clear();
+  Plan P;
+  TRY(make_plan(op, N, L, B, crossing, geometry, cfg, &P));
+  if (out) {
+    out->M = P.M; out->V = P.V; out->W = P.W; out->CL = P.CL; out->S = P.S; out->G = P.G; out->grid = P.grid;
+    out->layer_bytes = P.lb; out->dlayer_bytes = P.dlb; out->smem = P.smem;
+    out->off_kinds = P.off_kinds; out->off_tiles = P.off_tiles; out->off_dtiles = P.off_dtiles;
+    out->off_partial = P.off_partial; out->total = P.total;
+  }
+  return MG_OK;
+}
+
+int mg_propagate_l2(int N, int L, int B, int crossing, int geometry, const void* y, const void* target, void* x_out,
+                    void* g_out, int ldu, float* dp, int ldp, int accumulate, const mg_config* cfg, void* ws, size_t wsb,
+                    void* stream) {
+  g_err.clear();
+  Plan P;
+  TRY(make_plan(OP_BWD, N, L, B, crossing, geometry, cfg, &P));
+  TRY(check_ws(P, ws, wsb));
+  TRY(check_ldu(P, ldu));
+  TRY(check_field(y, "y", P.real, B > 0));
+  TRY(check_field(target, "target", P.real, B > 0));
+  TRY(check_field(x_out, "x_out", P.real, false));
+  TRY(check_field(g_out, "g_out", P.real, B > 0));
+  if (dp && ldp < N / 2 * crossing_np(crossing)) return fail(MG_E_ARG, "ldp too small");
+  return run_prop(P, y, nullptr, x_out, g_out, ldu, dp, ldp, accumulate, static_cast<unsigned char*>(ws),
+                  static_cast<cudaStream_t>(stream), target);
 }
 
 int mg_fma_probe(float* sink, int blocks, int threads, int iters, void* stream) {

@@ -219,40 +219,54 @@ __global__ void coef_kernel(const CoefArgs a) {
   }
 }
 
-// dp[l][q][k] (= or +=) sum over the nC per-CTA partials, in CTA order (deterministic).  Partials are
-// stored in the lane-major slot order pos (slot_pos); threads walk pos so the reads coalesce.
-// Inactive slots (outside a layer's lens/shifts range) get 0 (overwrite) or are left unchanged (accumulate).
-__global__ void dp_reduce_kernel(const float2* __restrict__ partial, int nC, int L, int np2, int M, int G, int N,
-                                 float* dp, int ldp, int n_p, int accumulate, const int* geo) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= L * np2) return;
+// dp[l][q][k] (= or +=) sum over the nC per-CTA partials, deterministic.  Partials are stored in the
+// lane-major slot order pos (slot_pos).  A block of 256 threads owns 32 consecutive positions; its 8
+// thread rows sum the CTAs c = row, row+8, ... (many independent loads in flight), then the 8 row
+// sums are combined in a fixed order through shared memory.
+constexpr int kReduceCols = 32, kReduceRows = 8;
+__global__ void __launch_bounds__(kReduceCols * kReduceRows)
+dp_reduce_kernel(const float2* __restrict__ partial, int nC, int L, int np2, int M, int G, int N, float* dp, int ldp,
+                 int n_p, int accumulate, const int* geo) {
+  __shared__ float2 acc[kReduceRows][kReduceCols];
+  const int col = threadIdx.x % kReduceCols, row = threadIdx.x / kReduceCols;
+  const int idx = blockIdx.x * kReduceCols + col;
+  const bool valid = idx < L * np2;
+  const size_t stride = (size_t)L * np2;
+  float sx = 0.f, sy = 0.f;
+  if (valid) {
+    const float2* p = partial + idx;
+    int c = row;
+    for (; c + 3 * kReduceRows < nC; c += 4 * kReduceRows) {
+      const float2 a0 = __ldg(p + (size_t)c * stride), a1 = __ldg(p + (size_t)(c + kReduceRows) * stride);
+      const float2 a2 = __ldg(p + (size_t)(c + 2 * kReduceRows) * stride);
+      const float2 a3 = __ldg(p + (size_t)(c + 3 * kReduceRows) * stride);
+      sx += a0.x; sy += a0.y; sx += a1.x; sy += a1.y; sx += a2.x; sy += a2.y; sx += a3.x; sy += a3.y;
+    }
+    for (; c < nC; c += kReduceRows) {
+      const float2 a0 = __ldg(p + (size_t)c * stride);
+      sx += a0.x; sy += a0.y;
+    }
+  }
+  acc[row][col] = make_float2(sx, sy);
+  __syncthreads();
+  if (row != 0 || !valid) return;
+  for (int r = 1; r < kReduceRows; ++r) {
+    sx += acc[r][col].x;
+    sy += acc[r][col].y;
+  }
   const int l = idx / np2, pos = idx - l * np2;
   const int q = pos_slot(pos, M, G);
   if (q >= N / 2) return;
   const int sh = geo[2 * l], ln = geo[2 * l + 1];
   const bool active = q >= sh / 2 && q < sh / 2 + ln;
+  float* o = dp + (size_t)l * ldp + (size_t)q * n_p;
   if (!active) {
     if (!accumulate) {
-      float* o = dp + (size_t)l * ldp + (size_t)q * n_p;
       o[0] = 0.f;
       if (n_p > 1) o[1] = 0.f;
     }
     return;
   }
-  const size_t stride = (size_t)L * np2;
-  const float2* p = partial + (size_t)l * np2 + pos;
-  float sx = 0.f, sy = 0.f;
-  int c = 0;
-  for (; c + 4 <= nC; c += 4) {
-    const float2 a0 = p[(size_t)c * stride], a1 = p[(size_t)(c + 1) * stride];
-    const float2 a2 = p[(size_t)(c + 2) * stride], a3 = p[(size_t)(c + 3) * stride];
-    sx += a0.x; sy += a0.y; sx += a1.x; sy += a1.y; sx += a2.x; sy += a2.y; sx += a3.x; sy += a3.y;
-  }
-  for (; c < nC; ++c) {
-    const float2 a0 = p[(size_t)c * stride];
-    sx += a0.x; sy += a0.y;
-  }
-  float* o = dp + (size_t)l * ldp + (size_t)q * n_p;
   if (accumulate) {
     o[0] += sx;
     if (n_p > 1) o[1] += sy;

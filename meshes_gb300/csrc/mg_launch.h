@@ -24,8 +24,15 @@ inline cudaError_t ensure_smem_attr(K kernel, std::atomic<unsigned long long>& d
   int optin = 0;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  // the dynamic limit is the opt-in maximum less the kernel's static shared memory
+  cudaFuncAttributes fa;
+  e = cudaFuncGetAttributes(&fa, kernel);
   if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();   // do not leave the failure for the next launch check to report
+    return e;
+  }
   done.fetch_or(bit, std::memory_order_acq_rel);
   return cudaSuccess;
 }

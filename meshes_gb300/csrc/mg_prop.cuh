@@ -52,8 +52,10 @@ struct PropArgs {
   const void* in1;               // FWDDIFF: du_in (may be null = 0)   BWD: dJ/du_out*
   void* out0;                    // FWD/FWDDIFF: u_out     BWD: u_in (may be null)
   void* out1;                    // FWDDIFF: du_out        BWD: dJ/du_in*
-  float2* partial;               // BWD: [gridDim.x][L][Np/2] (dJ/dp0, dJ/dp1) per CTA
+  float2* partial;               // BWD: (dJ/dp0, dJ/dp1) partials of this CTA/item, [L][Np/2]
   int* status;
+  int v0, vend;                  // vectors [v0, vend) are handled by this CTA/item
+  const void* target;            // BWD: when set, dJ/du_out* = 2 (u_out - target) replaces in1
 };
 
 template <bool REAL> struct Fld { using T = float2; using C = C2x2; };
@@ -97,10 +99,21 @@ __device__ __forceinline__ void x_bwd(const CT& t, F& a, F& b, F& ga, F& gb, CT&
   const F ngb = ccfma(t.t11, gb, ccmul(t.t01, ga));
   a = xa; b = xb; ga = nga; gb = ngb;
 }
-template <int OP, typename F, typename CT>
+// back-propagation through one layer whose INPUT x is given (stored activation of a lossy mesh):
+// G += conj(g) x^T, g <- T^H g; x is left unchanged
+template <typename F, typename CT>
+__device__ __forceinline__ void x_bwd_stored(const CT& t, F& xa, F& xb, F& ga, F& gb, CT& acc) {
+  acc.t00 = ccfma(ga, xa, acc.t00); acc.t01 = ccfma(ga, xb, acc.t01);
+  acc.t10 = ccfma(gb, xa, acc.t10); acc.t11 = ccfma(gb, xb, acc.t11);
+  const F nga = ccfma(t.t10, gb, ccmul(t.t00, ga));
+  const F ngb = ccfma(t.t11, gb, ccmul(t.t01, ga));
+  ga = nga; gb = ngb;
+}
+template <int OP, int GR, typename F, typename CT>
 __device__ __forceinline__ void xop(const CT& t, const CT& d, F& a, F& b, F& wa, F& wb, CT& acc) {
   if constexpr (OP == OP_FWD) x_fwd(t, a, b);
   else if constexpr (OP == OP_FWDDIFF) x_fwddiff(t, d, a, b, wa, wb);
+  else if constexpr (GR == 4) x_bwd_stored(t, a, b, wa, wb, acc);
   else x_bwd(t, a, b, wa, wb, acc);
 }
 
@@ -141,6 +154,9 @@ __device__ __forceinline__ void acc2_stage(float2* gl2, int pos, int G, int r, f
 template <int M> __device__ __forceinline__ int cs_off(int G) { return M * G; }
 // compact index of an "a" lane (bit d clear) among the G/2 a-lanes of a cross-lane layer
 __device__ __forceinline__ int a_lane_index(int j, int d) { return ((j / (2 * d)) * d) | (j & (d - 1)); }
+
+__device__ __forceinline__ float2 l2_grad(float2 y, float2 t) { return make_float2(2.f * (y.x - t.x), 2.f * (y.y - t.y)); }
+__device__ __forceinline__ float l2_grad(float y, float t) { return 2.f * (y - t); }
 
 __device__ __forceinline__ void acc_zero(C2x2& a) { a = c2x2_zero(); }
 __device__ __forceinline__ void acc_zero(R2x2& a) { a.t00 = a.t01 = a.t10 = a.t11 = 0.f; }
@@ -190,7 +206,7 @@ __device__ __forceinline__ void entry(const float4* tl, int doff, int e, int a, 
   using CT = typename Fld<REAL>::C;
   CT t, d, acc;
   ld_coef(tl, e, G, j, t);
-  if constexpr (OP == OP_BWD && GR != 0) {
+  if constexpr (OP == OP_BWD && (GR == 1 || GR == 2)) {
     float2 cs = make_float2(0.f, 0.f);
     if constexpr (GR == 1) cs = reinterpret_cast<const float2*>(tl + cs_off<M>(G))[e * G + j];
     float ath = 0.f, aph = 0.f;
@@ -201,7 +217,7 @@ __device__ __forceinline__ void entry(const float4* tl, int doff, int e, int a, 
     if constexpr (OP == OP_FWDDIFF) ld_coef(tl + doff, e, G, j, d);
     if constexpr (OP == OP_BWD) acc_zero(acc);
 #pragma unroll
-    for (int v = 0; v < V; ++v) xop<OP>(t, d, u[v][a], u[v][b], w[v][a], w[v][b], acc);
+    for (int v = 0; v < V; ++v) xop<OP, GR>(t, d, u[v][a], u[v][b], w[v][a], w[v][b], acc);
     if constexpr (OP == OP_BWD) acc_stage(gl, e, G, j, r, acc);
   }
 }
@@ -237,7 +253,7 @@ __device__ __forceinline__ void layer_mis(const float4* tl, int G, int j, int r,
     constexpr int e = M / 2 - 1;
     CT t, d, acc;
     ld_coef(tl, e, G, j, t);
-    if constexpr (OP == OP_BWD && GR != 0) {
+    if constexpr (OP == OP_BWD && (GR == 1 || GR == 2)) {
       float2 cs = make_float2(0.f, 0.f);
       if constexpr (GR == 1) cs = reinterpret_cast<const float2*>(tl + cs_off<M>(G))[e * G + j];
       float ath = 0.f, aph = 0.f;
@@ -248,7 +264,7 @@ __device__ __forceinline__ void layer_mis(const float4* tl, int G, int j, int r,
       if constexpr (OP == OP_FWDDIFF) ld_coef(tl + doff, e, G, j, d);
       if constexpr (OP == OP_BWD) acc_zero(acc);
 #pragma unroll
-      for (int v = 0; v < V; ++v) xop<OP>(t, d, u[v][M - 1], nu[v], w[v][M - 1], nw[v], acc);
+      for (int v = 0; v < V; ++v) xop<OP, GR>(t, d, u[v][M - 1], nu[v], w[v][M - 1], nw[v], acc);
       if constexpr (OP == OP_BWD) acc_stage(gl, e, G, j, r, acc);
     }
   }
@@ -309,7 +325,7 @@ __device__ __forceinline__ void layer_xl(const float4* tl, int d, int G, int j, 
         w[v][m] = cfma(dp, ru, cfma(ds, u[v][m], cfma(cp, rw, cmul(cs, w[v][m]))));
         u[v][m] = cfma(cp, ru, cmul(cs, u[v][m]));
       }
-    } else if constexpr (GR != 0) {
+    } else if constexpr (GR == 1 || GR == 2) {
       // coefficients of the BWD tile are the own row of T^H; a-lanes (bit d clear) own the slot's
       // gradient (their mode is the slot's first mode), b-lanes compute and discard it
       float2 sc = make_float2(0.f, 0.f);
@@ -340,8 +356,9 @@ __device__ __forceinline__ void layer_xl(const float4* tl, int d, int G, int j, 
       for (int v = 0; v < V; ++v) {
         const F ry = shfl_xor(u[v][m], d, G);
         const F rg = shfl_xor(w[v][m], d, G);
-        const F x = cfma(cp, ry, cmul(cs, u[v][m]));
-        const F rx = shfl_xor(x, d, G);
+        // GR 4: u already holds the layer input (stored); otherwise rebuild it with T^H
+        const F x = (GR == 4) ? u[v][m] : cfma(cp, ry, cmul(cs, u[v][m]));
+        const F rx = (GR == 4) ? ry : shfl_xor(x, d, G);
         aoo = ccfma(w[v][m], x, aoo);
         aop = ccfma(w[v][m], rx, aop);
         w[v][m] = cfma(cp, rg, cmul(cs, w[v][m]));
@@ -504,7 +521,7 @@ __device__ __forceinline__ void chunk_reduce(const PropArgs& a, const int* kinds
       const float4 d = D[pos];
       dth = d.x * g00 + d.y * g01 + d.z * g10 + d.w * g11;
     }
-    a.partial[((size_t)blockIdx.x * a.L + l) * np2 + pos] = make_float2(dth, dph);
+    a.partial[(size_t)l * np2 + pos] = make_float2(dth, dph);
   }
 }
 
@@ -530,7 +547,42 @@ __device__ __forceinline__ void chunk_reduce_direct(const PropArgs& a, const int
       sx += v.x;
       sy += v.y;
     }
-    a.partial[((size_t)blockIdx.x * a.L + l) * np2 + pos] = make_float2(GR == 2 ? 0.5f * sx : sx, sy);
+    a.partial[(size_t)l * np2 + pos] = make_float2(GR == 2 ? 0.5f * sx : sx, sy);
+  }
+}
+
+// ---- chunk-end reduction of the raw dJ/dT modes (generic crossings): sum the W warps' staged
+// dJ/dT_ij of every slot in a fixed order; partial layout [l][k][pos] float2, k = (00, 01, 10, 11)
+template <int M>
+__device__ __forceinline__ void chunk_reduce_raw(const PropArgs& a, const int* kinds, int lo, int nl,
+                                                 const unsigned char* gst, int np2, int G) {
+  const size_t gst_layer = (size_t)np2 * 32;
+  for (int idx = threadIdx.x; idx < nl * np2; idx += blockDim.x) {
+    const int li = idx / np2, pos = idx - li * np2;
+    const int l = lo + li;
+    const int kind = kinds[l];
+    const int e = pos / G, j = pos - e * G;
+    int la = j, lb = j, ia = 2 * e, ib = 2 * e + 1;
+    const bool xl = kind >= KIND_XL;
+    if (xl) {
+      const int q = j * (M / 2) + e;
+      const int st = 1 << (kind - KIND_XL);
+      const int ma = 2 * st * (q / st) + (q % st), mb = ma + st;
+      la = ma / M; lb = mb / M;
+      ia = ma % M; ib = mb % M;
+    }
+    float4 ra = make_float4(0.f, 0.f, 0.f, 0.f), rb = ra;
+    for (int w = 0; w < a.W; ++w) {
+      const float4* gl = reinterpret_cast<const float4*>(gst + ((size_t)w * a.CL + li) * gst_layer);
+      const float4 x = gl[ia * G + la], y = gl[ib * G + lb];
+      ra.x += x.x; ra.y += x.y; ra.z += x.z; ra.w += x.w;
+      rb.x += y.x; rb.y += y.y; rb.z += y.z; rb.w += y.w;
+    }
+    float2* o = a.partial + (size_t)l * 4 * np2 + pos;
+    o[0] = make_float2(ra.x, ra.y);                                        // G00 (XL: G_aa)
+    o[np2] = make_float2(ra.z, ra.w);                                      // G01 (XL: G_ab)
+    o[2 * np2] = xl ? make_float2(rb.z, rb.w) : make_float2(rb.x, rb.y);   // G10 (XL: G_ba)
+    o[3 * np2] = xl ? make_float2(rb.x, rb.y) : make_float2(rb.z, rb.w);   // G11 (XL: G_bb)
   }
 }
 
@@ -575,21 +627,22 @@ __device__ __forceinline__ void run_chunk(const int* kinds, const unsigned char*
   }
 }
 
+// One batch tile of one mesh: vectors [a.v0, a.vend), all L layers, by the W warps of the CTA.
+// Shared by the one-mesh kernel (prop_kernel) and the persistent multi-mesh kernel (mg_batched.cu).
 template <int OP, int M, int V, bool REAL, int GT, int GR>
-__global__ void __launch_bounds__(PropTraits<OP, M, V, REAL>::kMaxThreads)
-prop_kernel(const PropArgs a) {
+__device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem) {
   using F = typename Fld<REAL>::T;
-  extern __shared__ __align__(128) unsigned char smem[];
   const int tid = threadIdx.x, warp = tid >> 5;
   const Lanes<GT> ln(a.G, a.logG);
   const int G = ln.G, j = ln.j, r = ln.r, R = 32 / G;
   const int np2 = (G * M) >> 1;
-  const int vb0 = blockIdx.x * (a.W * R * V) + (warp * R + r) * V;
+  const int vb0 = a.v0 + (warp * R + r) * V;
 
   const size_t ring_bytes = (size_t)a.S * a.CL * a.layer_bytes;
   constexpr bool kDT = (OP == OP_BWD && GR == 0);          // dT/dp tiles needed
   const size_t dbuf_bytes = kDT ? (size_t)a.CL * a.dlayer_bytes : 0;
-  const size_t gst_layer = (size_t)np2 * (GR != 0 ? 8 : (REAL ? 16 : 32));
+  constexpr bool kDirect = (GR == 1 || GR == 2);
+  const size_t gst_layer = (size_t)np2 * (kDirect ? 8 : (REAL ? 16 : 32));
   const size_t gst_bytes = (OP == OP_BWD) ? (size_t)a.W * a.CL * gst_layer : 0;
   unsigned char* ring = smem;
   unsigned char* dbuf = smem + ring_bytes;
@@ -604,8 +657,20 @@ prop_kernel(const PropArgs a) {
 
   F u[V][M];
   F w[V][M];
-  load_fields<M, V, REAL>(u, a.in0, vb0, a.B, a.N, a.ldu, j);
-  if constexpr (OP != OP_FWD) load_fields<M, V, REAL>(w, a.in1, vb0, a.B, a.N, a.ldu, j);
+  load_fields<M, V, REAL>(u, a.in0, vb0, a.vend, a.N, a.ldu, j);
+  if constexpr (OP == OP_BWD) {
+    if (a.target) {   // fused L2 loss to a target: g = 2 (y - t)
+      load_fields<M, V, REAL>(w, a.target, vb0, a.vend, a.N, a.ldu, j);
+#pragma unroll
+      for (int v = 0; v < V; ++v)
+#pragma unroll
+        for (int m = 0; m < M; ++m) w[v][m] = l2_grad(u[v][m], w[v][m]);
+    } else {
+      load_fields<M, V, REAL>(w, a.in1, vb0, a.vend, a.N, a.ldu, j);
+    }
+  } else if constexpr (OP != OP_FWD) {
+    load_fields<M, V, REAL>(w, a.in1, vb0, a.vend, a.N, a.ldu, j);
+  }
 
   const int nch = (a.L + a.CL - 1) / a.CL;
   if (tid == 0) {
@@ -654,7 +719,8 @@ prop_kernel(const PropArgs a) {
     const unsigned char* st = ring + (size_t)(c % a.S) * a.CL * a.layer_bytes;
     run_chunk<OP, M, V, REAL, GR>(kinds, st, a.layer_bytes, lo, hi, gst_warp, gst_layer, G, j, r, u, w);
     __syncthreads();
-    if constexpr (OP == OP_BWD && GR != 0) chunk_reduce_direct<M, GR>(a, kinds, lo, hi - lo, gst, np2, G);
+    if constexpr (OP == OP_BWD && kDirect) chunk_reduce_direct<M, GR>(a, kinds, lo, hi - lo, gst, np2, G);
+    if constexpr (OP == OP_BWD && (GR == 3 || GR == 4)) chunk_reduce_raw<M>(a, kinds, lo, hi - lo, gst, np2, G);
     if constexpr (kDT) {
       const bool okd = mbar_wait_bounded(smem_u32(bars + a.S), (uint32_t)(c & 1));
       if (__syncthreads_or(!okd)) {
@@ -669,8 +735,20 @@ prop_kernel(const PropArgs a) {
     if (tid == 0 && issued < nch) issue(issued++);
   }
   (void)R;
-  store_fields<M, V, REAL>(u, a.out0, vb0, a.B, a.N, a.ldu, j);
-  if constexpr (OP != OP_FWD) store_fields<M, V, REAL>(w, a.out1, vb0, a.B, a.N, a.ldu, j);
+  store_fields<M, V, REAL>(u, a.out0, vb0, a.vend, a.N, a.ldu, j);
+  if constexpr (OP != OP_FWD) store_fields<M, V, REAL>(w, a.out1, vb0, a.vend, a.N, a.ldu, j);
+}
+
+template <int OP, int M, int V, bool REAL, int GT, int GR>
+__global__ void __launch_bounds__(PropTraits<OP, M, V, REAL>::kMaxThreads)
+prop_kernel(const PropArgs a0) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  PropArgs a = a0;
+  const int G = GT ? GT : a.G;
+  a.v0 = blockIdx.x * (a.W * (32 / G) * V);
+  a.vend = a.B;
+  if (OP == OP_BWD) a.partial = a0.partial + (size_t)blockIdx.x * a.L * ((G * M) >> 1);
+  prop_body<OP, M, V, REAL, GT, GR>(a, smem);
 }
 
 }  // namespace mg

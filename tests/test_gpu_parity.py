@@ -246,3 +246,43 @@ def test_argument_errors():
     assert "even" in _lib.last_error()
     assert lib.mg_fwdprop(1024, 1, 1, None, None, None, 0, None, 0, None, None, 1024, 0, None, 0, st) == -1
     assert lib.mg_fwdprop(8, 1, 1, None, None, None, 0, None, 0, None, None, 8, 0, None, 0, st) == -2
+
+
+@pytest.mark.parametrize("cr,N,B", [("mzi", 128, 77), ("orth", 64, 40), ("sym", 32, 9), ("mzi", 512, 5)])
+def test_shared_tiles_and_fused_l2_target(cr, N, B):
+    """One coefficient pass (back-propagation tiles) serves the forward kernel (op 3); the L2 gradient
+    2 (y - t) is formed inside the backward kernel (mg_propagate_l2)."""
+    from meshes_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(N + B)
+    om = O.random_mesh(rng, N, "clements", cr, 0.02)
+    real = cr == "orth"
+    x = O.unit_columns(rng, N, B, real=real)
+    t = O.unit_columns(rng, N, B, real=real)
+    m = gpu_mesh(om)
+    dt = torch.float32 if real else torch.complex64
+    xd = torch.tensor(x, dtype=dt, device="cuda")
+    td = torch.tensor(t, dtype=dt, device="cuda")
+    y = torch.empty_like(xd)
+    gx = torch.empty_like(xd)
+    dp = torch.empty(m.p_phase.numel(), device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    nb = lib.mg_workspace_bytes(2, N, om.L, B, m.crossing, 0, None)
+    ws = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    assert lib.mg_workspace_init(ws.data_ptr(), nb, st) == 0
+    s = m.p_splitter
+    ldp, lds = N // 2 * m.X_np, N // 2 * m.X_ns
+    assert lib.mg_build_tiles(2, N, om.L, 0, m.lens.data_ptr(), m.shifts.data_ptr(), None, m.crossing,
+                              m.p_phase.data_ptr(), ldp, s.data_ptr() if s.numel() else None, lds, None, None, None,
+                              B, None, ws.data_ptr(), nb, st) == 0
+    assert lib.mg_propagate(3, N, om.L, B, m.crossing, 0, xd.data_ptr(), None, y.data_ptr(), None, N, None, 0, 0,
+                            None, ws.data_ptr(), nb, st) == 0, _lib.last_error()
+    assert lib.mg_propagate_l2(N, om.L, B, m.crossing, 0, y.data_ptr(), td.data_ptr(), None, gx.data_ptr(), N,
+                               dp.data_ptr(), ldp, 0, None, ws.data_ptr(), nb, st) == 0, _lib.last_error()
+    y_ref = O.propagate(om, x)
+    G, _, gin = O.vjp_unitary(om, y_ref, 2 * (y_ref - t))
+    n_p = O.CROSSINGS[cr][0]
+    assert O.rel_err(y.cpu().numpy(), y_ref) < TOL
+    assert O.rel_err(gx.cpu().numpy(), gin) < TOL
+    assert O.rel_err(dp.cpu().numpy().reshape(om.L, N // 2, n_p), O.contract_dp(om, G)) < TOL
+    assert lib.mg_read_status(ws.data_ptr(), 0, st) == 0
