@@ -37,6 +37,7 @@ extern "C" {
 #define MG_OP_FWDDIFF 1
 #define MG_OP_BWD 2
 #define MG_OP_FWD_BWDTILES 3   /* mg_propagate only: forward reading back-propagation tiles */
+#define MG_OP_BWD_STORED 4     /* back-propagation from stored layer inputs (lossy crossings) */
 #define MG_GEO_NN 0
 #define MG_GEO_FFT 1
 
@@ -204,6 +205,25 @@ int mg_batched_reduce(const mg_batch_mesh* meshes, int n_meshes, void* stream);
 int mg_propagate_l2(int N, int L, int B, int crossing, int geometry, const void* y, const void* target, void* x_out,
                     void* g_out, int ldu, float* dp, int ldp, int accumulate, const mg_config* cfg, void* workspace,
                     size_t workspace_bytes, void* stream);
+
+/* ---- lossy meshes: layer ranges and stored activations ----------------------------------------
+ * The reference back-propagates by inverting each layer with T^H (c/dot.cpp:75-80, gpu/backprop.cu),
+ * which is exact only for unitary crossings; for lossy ones (crossing.py:444-508, gains g_ij) that
+ * gradient is wrong.  These calls back-propagate from stored layer inputs instead, for checkpointed
+ * adjoints that keep one input every ~sqrt(L) layers and recompute the rest segment by segment.
+ * Both run layers [l0, l1) of tiles built earlier by mg_build_tiles for the same (N, L, B, crossing,
+ * geometry, cfg): op MG_OP_FWD with tiles of MG_OP_FWD, op MG_OP_BWD_STORED with tiles of
+ * MG_OP_BWD_STORED (complex crossings only; MG_GENERIC takes T per slot from Tgen and needs no Dgen).
+ *   MG_OP_FWD:        in0 = input of layer l0, out0 = output of layer l1-1 (may be NULL); when act is
+ *                     not NULL the input of every layer l of the range is also written to
+ *                     act + (l - l0) * B * ldu (complex64 elements).
+ *   MG_OP_BWD_STORED: act holds those inputs; in1 = 2 dJ/du* at the output of layer l1-1, out1 =
+ *                     2 dJ/du* at the input of layer l0; dT (complex64 [L][N/2][2][2], same slot grid
+ *                     as Tgen) receives, for the layers of the range, sum_b g_i conj(x_j) = 2 dJ/dT_ij*
+ *                     (0 on inactive slots), overwritten or, with accumulate, added. */
+int mg_propagate_range(int op, int N, int L, int l0, int l1, int B, int crossing, int geometry, const void* in0,
+                       const void* in1, void* out0, void* out1, int ldu, void* act, void* dT, int accumulate,
+                       const mg_config* cfg, void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---- measurement helpers -------------------------------------------------------------------- */
 

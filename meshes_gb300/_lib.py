@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libmeshes_gb300.so")
 
 MZI, SYM, ORTH, GENERIC = 0, 1, 2, 3
-OP_FWD, OP_FWDDIFF, OP_BWD, OP_FWD_BWDTILES = 0, 1, 2, 3
+OP_FWD, OP_FWDDIFF, OP_BWD, OP_FWD_BWDTILES, OP_BWD_STORED = 0, 1, 2, 3, 4
 GEO_NN, GEO_FFT = 0, 1
 CROSSING_CODES = {"mzi": MZI, "sym": SYM, "orth": ORTH, "generic": GENERIC}
 STATUS_NAMES = {0: "ok", 1: "timeout", 2: "bad geometry", 3: "bad work item"}
@@ -79,6 +79,9 @@ _SIGS = {
                              c_void_p, c_int, c_int, POINTER(mg_config), c_void_p, c_size_t, c_void_p]),
     "mg_propagate_l2": (c_int, [c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
                                 c_void_p, c_int, c_int, POINTER(mg_config), c_void_p, c_size_t, c_void_p]),
+    "mg_propagate_range": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p,
+                                   c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_int, POINTER(mg_config), c_void_p,
+                                   c_size_t, c_void_p]),
     "mg_fma_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
     "mg_plan": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, POINTER(mg_config), POINTER(mg_plan_info)]),
     # mesh and item arrays live in device memory: passed as raw addresses

@@ -107,8 +107,28 @@ struct Plan {
   size_t off_kinds, off_tiles, off_dtiles, off_partial, total;
 };
 
+// (M, V) instantiated for the stored-activation kernels (GR 4), by op (FWD writes, BWD reads)
+bool instantiated_stored(int op, int M, int V) {
+  static const int fwd[][2] = {{2, 8}, {4, 8}, {8, 4}, {16, 2}};
+  static const int bwd[][2] = {{2, 4}, {4, 4}, {8, 4}, {16, 2}};
+  for (int i = 0; i < 4; ++i) {
+    const int* t = (op == OP_FWD) ? fwd[i] : bwd[i];
+    if (t[0] == M && t[1] == V) return true;
+  }
+  return false;
+}
+int stored_default_v(int op, int M) { return op == OP_FWD ? (M <= 4 ? 8 : (M == 8 ? 4 : 2)) : (M <= 8 ? 4 : 2); }
+
+// op MG_OP_BWD_STORED plans the back-propagation kernel in its stored-activation mode (GR 4): T tiles
+// only, 32-byte dJ/dT staging per slot, raw partials of 4 complex per slot.
 int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_config* cfg, Plan* P) {
-  if (op < 0 || op > 2) return fail(MG_E_ARG, "op %d not in {0,1,2}", op);
+  const bool stored = op == MG_OP_BWD_STORED;
+  if (stored) {
+    if (crossing == CR_ORTH) return fail(MG_E_ARG, "stored-activation back-propagation needs a complex crossing");
+    op = OP_BWD;
+  } else if (op < 0 || op > 2) {
+    return fail(MG_E_ARG, "op %d not in {0,1,2,4}", op);
+  }
   if (crossing < 0 || crossing > 3) return fail(MG_E_ARG, "crossing %d not in {0,1,2,3}", crossing);
   if (geometry < 0 || geometry > 1) return fail(MG_E_ARG, "geometry %d not in {0,1}", geometry);
   if (N < 2 || N % 2) return fail(MG_E_ARG, "N=%d must be even and >= 2 (reference gpu/mesh.py:67)", N);
@@ -120,7 +140,7 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   Plan& p = *P;
   p.op = op; p.N = N; p.L = L; p.B = B; p.crossing = crossing; p.geometry = geometry;
   p.real = crossing == CR_ORTH;
-  p.gr = (op != OP_BWD) ? 0 : (crossing == CR_MZI ? 1 : (crossing == CR_ORTH ? 2 : 0));
+  p.gr = stored ? 4 : (op != OP_BWD) ? 0 : (crossing == CR_MZI ? 1 : (crossing == CR_ORTH ? 2 : 0));
   const int Np = pow2ceil(N);
   int M = (cfg && cfg->M) ? cfg->M : std::max(std::min(8, Np), Np / 32);
   if (M < 2 || M > 16 || (M & (M - 1))) return fail(MG_E_CONFIG, "modes per lane M=%d not in {2,4,8,16}", M);
@@ -130,15 +150,16 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   int V = (cfg && cfg->V) ? cfg->V : 0;
   if (!V) {
     static const int vd[3][5] = {{8, 8, 4, 2, 0}, {4, 4, 2, 1, 0}, {4, 4, 4, 2, 0}};   // by ilog2(M)-1
-    V = vd[op][ilog2(M) - 1];
+    V = stored ? stored_default_v(OP_BWD, M) : vd[op][ilog2(M) - 1];
   }
-  if (!instantiated(op, M, V)) return fail(MG_E_CONFIG, "no kernel instantiated for op=%d M=%d V=%d", op, M, V);
+  if (stored ? !instantiated_stored(OP_BWD, M, V) : !instantiated(op, M, V))
+    return fail(MG_E_CONFIG, "no kernel instantiated for op=%d M=%d V=%d", stored ? MG_OP_BWD_STORED : op, M, V);
   p.M = M; p.V = V; p.G = G; p.logG = ilog2(G); p.R = 32 / G; p.np2 = G * M / 2;
   const unsigned tslot = p.real ? 16 : 32;               // bytes per slot of a T tile
   // layer tiles are copied by bulk TMA: every size and offset must be a multiple of 16 bytes
   p.lb = (unsigned)align16((size_t)p.np2 * tslot * (op == OP_FWDDIFF ? 2 : 1) + (p.gr == 1 ? (size_t)p.np2 * 8 : 0));
   p.dlb = (op == OP_BWD && p.gr == 0) ? (unsigned)(p.np2 * (p.real ? 16 : 64)) : 0;
-  const int gslot = (op != OP_BWD) ? 0 : (p.gr != 0 ? 8 : (p.real ? 16 : 32));
+  const int gslot = (op != OP_BWD) ? 0 : ((p.gr == 1 || p.gr == 2) ? 8 : (p.real ? 16 : 32));
   const size_t gstl = (size_t)p.np2 * gslot;
   const int maxw = prop_max_threads(op, M, V) / 32;
   int W = (cfg && cfg->W) ? cfg->W : 0;
@@ -178,7 +199,7 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   p.off_tiles = p.off_kinds + align256((size_t)std::max(L, 1) * 12);   // kinds + (shift, len)
   p.off_dtiles = p.off_tiles + align256((size_t)L * p.lb);
   p.off_partial = p.off_dtiles + align256((size_t)L * p.dlb);
-  p.total = p.off_partial + ((op == OP_BWD) ? align256((size_t)p.grid * L * p.np2 * 8) : 0);
+  p.total = p.off_partial + ((op == OP_BWD) ? align256((size_t)p.grid * L * p.np2 * (p.gr == 4 ? 32 : 8)) : 0);
   return MG_OK;
 }
 
@@ -239,6 +260,8 @@ int run_prop(const Plan& P, const void* in0, const void* in1, void* out0, void* 
   if (P.B == 0) return MG_OK;
   PropArgs a;
   a.target = target;
+  a.act = nullptr;
+  a.act_plane = 0;
   a.N = P.N; a.L = P.L; a.B = P.B; a.ldu = ldu;
   a.G = P.G; a.logG = P.logG; a.W = P.W; a.CL = P.CL; a.S = P.S;
   a.layer_bytes = P.lb; a.dlayer_bytes = P.dlb;
@@ -497,6 +520,7 @@ int mg_propagate(int op, int N, int L, int B, int crossing, int geometry, const 
     return run_prop(Pf, in0, nullptr, out0, nullptr, ldu, nullptr, 0, 0, static_cast<unsigned char*>(ws),
                     static_cast<cudaStream_t>(stream));
   }
+  if (op == MG_OP_BWD_STORED) return fail(MG_E_ARG, "stored-activation back-propagation runs through mg_propagate_range");
   Plan P;
   TRY(make_plan(op, N, L, B, crossing, geometry, cfg, &P));
   TRY(check_ws(P, ws, wsb));
@@ -558,6 +582,90 @@ int mg_propagate_l2(int N, int L, int B, int crossing, int geometry, const void*
   if (dp && ldp < N / 2 * crossing_np(crossing)) return fail(MG_E_ARG, "ldp too small");
   return run_prop(P, y, nullptr, x_out, g_out, ldu, dp, ldp, accumulate, static_cast<unsigned char*>(ws),
                   static_cast<cudaStream_t>(stream), target);
+}
+
+int mg_propagate_range(int op, int N, int L, int l0, int l1, int B, int crossing, int geometry, const void* in0,
+                       const void* in1, void* out0, void* out1, int ldu, void* act, void* dT, int accumulate,
+                       const mg_config* cfg, void* ws, size_t wsb, void* stream) {
+  g_err.clear();
+  if (op != OP_FWD && op != MG_OP_BWD_STORED) return fail(MG_E_ARG, "op %d not in {MG_OP_FWD, MG_OP_BWD_STORED}", op);
+  if (l0 < 0 || l1 < l0 || l1 > L) return fail(MG_E_ARG, "layer range [%d, %d) outside [0, %d)", l0, l1, L);
+  Plan P;
+  TRY(make_plan(op, N, L, B, crossing, geometry, cfg, &P));
+  TRY(check_ws(P, ws, wsb));
+  TRY(check_ldu(P, ldu));
+  const bool bwd = op == MG_OP_BWD_STORED;
+  if (P.real && act) return fail(MG_E_ARG, "stored activations need a complex crossing");
+  if (bwd && !act && B > 0 && l1 > l0) return fail(MG_E_ARG, "stored-activation back-propagation needs act");
+  TRY(check_field(act, "act", P.real, false));
+  TRY(check_field(in0, "in0", P.real, !bwd && B > 0));
+  TRY(check_field(out0, "out0", P.real, false));
+  TRY(check_field(in1, "in1", P.real, bwd && B > 0));
+  TRY(check_field(out1, "out1", P.real, bwd && B > 0));
+  if (bwd && !dT && B > 0 && l1 > l0) return fail(MG_E_ARG, "dT is NULL");
+  if (dT && (reinterpret_cast<uintptr_t>(dT) & 7)) return fail(MG_E_ARG, "dT not 8-byte aligned");
+  if (act && !bwd) {   // the forward kernel's store mode has its own (M, V) instantiations
+    if (!(cfg && cfg->V)) P.V = stored_default_v(OP_FWD, P.M);
+    if (!instantiated_stored(OP_FWD, P.M, P.V))
+      return fail(MG_E_CONFIG, "no activation-storing forward kernel for M=%d V=%d", P.M, P.V);
+    const long per_cta = (long)P.W * P.R * P.V;
+    P.grid = (int)((B + per_cta - 1) / per_cta);
+  }
+  const int nl = l1 - l0;
+  if (B == 0 || nl == 0) {
+    if (bwd && B == 0 && dT && !accumulate && nl > 0) {   // no vectors: dJ/dT of the range is 0
+      cudaError_t e = cudaMemsetAsync(static_cast<float2*>(dT) + (size_t)l0 * (N / 2) * 4, 0,
+                                      (size_t)nl * (N / 2) * 32, static_cast<cudaStream_t>(stream));
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(dT)");
+    }
+    if (nl == 0 && B > 0) {   // empty range: the field passes through
+      const size_t el = P.real ? 4 : 8;
+      const void* src = bwd ? in1 : in0;
+      void* dst = bwd ? out1 : out0;
+      if (dst && dst != src) {
+        cudaError_t e = cudaMemcpy2DAsync(dst, (size_t)ldu * el, src, (size_t)ldu * el, (size_t)N * el, B,
+                                          cudaMemcpyDeviceToDevice, static_cast<cudaStream_t>(stream));
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy2DAsync");
+      }
+    }
+    return MG_OK;
+  }
+  // the launch sees layers [l0, l1) as its own layers [0, nl): tiles and kinds start at l0
+  unsigned char* w = static_cast<unsigned char*>(ws);
+  const int* kinds_full = reinterpret_cast<const int*>(w + P.off_kinds);
+  P.smem = prop_smem_bytes(P.op, bwd ? 32 : 0, P.M, P.G, P.W, P.CL, P.S, P.lb, P.dlb, nl);
+  PropArgs a;
+  a.target = nullptr;
+  a.N = N; a.L = nl; a.B = B; a.ldu = ldu;
+  a.G = P.G; a.logG = P.logG; a.W = P.W; a.CL = P.CL; a.S = P.S;
+  a.layer_bytes = P.lb; a.dlayer_bytes = 0;
+  a.tiles = w + P.off_tiles + (size_t)l0 * P.lb;
+  a.dtiles = nullptr;
+  a.kinds = kinds_full + l0;
+  a.in0 = bwd ? nullptr : in0;
+  a.in1 = bwd ? in1 : nullptr;
+  a.out0 = bwd ? nullptr : out0;
+  a.out1 = bwd ? out1 : nullptr;
+  a.partial = reinterpret_cast<float2*>(w + P.off_partial);
+  a.status = reinterpret_cast<int*>(w);
+  a.act = act;
+  a.act_plane = (size_t)B * ldu;
+  LaunchCfg lc;
+  lc.grid = dim3(P.grid);
+  lc.block = dim3(32 * P.W);
+  lc.smem = P.smem;
+  lc.stream = static_cast<cudaStream_t>(stream);
+  cudaError_t e = launch_prop(P.op, P.real, P.M, P.V, P.G == 32, act ? 4 : 0, lc, a);
+  if (e != cudaSuccess) return cuda_fail(e, "prop_kernel launch");
+  if (bwd) {
+    const int n = nl * P.np2;
+    raw_reduce_kernel<<<(n + 255) / 256, 256, 0, lc.stream>>>(a.partial, P.grid, nl, P.np2, P.M, P.G, N,
+                                                             static_cast<float2*>(dT) + (size_t)l0 * (N / 2) * 4,
+                                                             accumulate, kinds_full + L + 2 * l0);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "raw_reduce_kernel launch");
+  }
+  return MG_OK;
 }
 
 int mg_fma_probe(float* sink, int blocks, int threads, int iters, void* stream) {

@@ -56,6 +56,8 @@ struct PropArgs {
   int* status;
   int v0, vend;                  // vectors [v0, vend) are handled by this CTA/item
   const void* target;            // BWD: when set, dJ/du_out* = 2 (u_out - target) replaces in1
+  void* act;                     // GR 4: per-layer inputs [L][act_plane] (FWD writes them, BWD reads them)
+  size_t act_plane;              // elements between the stored inputs of consecutive layers
 };
 
 template <bool REAL> struct Fld { using T = float2; using C = C2x2; };
@@ -593,11 +595,24 @@ struct PropTraits {
 
 // Layer loop body: fused (aligned, odd-shift) pairs of nearest-neighbour layers run as one
 // straight-line block (the compiler interleaves the two layers' crossings); other kinds one by one.
+// GR 4 (stored activations, for lossy crossings) goes layer by layer: the forward pass writes each
+// layer's input to a.act before applying it, back-propagation reloads it in place of T^H reconstruction.
 template <int OP, int M, int V, bool REAL, int GR, typename F>
-__device__ __forceinline__ void run_chunk(const int* kinds, const unsigned char* st, unsigned layer_bytes, int lo,
-                                          int hi, unsigned char* gst_warp, size_t gst_layer, int G, int j, int r,
-                                          F (&u)[V][M], F (&w)[V][M]) {
+__device__ __forceinline__ void run_chunk(const PropArgs& pa, int vb0, const int* kinds, const unsigned char* st,
+                                          unsigned layer_bytes, int lo, int hi, unsigned char* gst_warp,
+                                          size_t gst_layer, int G, int j, int r, F (&u)[V][M], F (&w)[V][M]) {
   const int nl = hi - lo;
+  if constexpr (GR == 4) {
+    for (int i = 0; i < nl; ++i) {
+      const int l = (OP == OP_BWD) ? (hi - 1 - i) : (lo + i);
+      F* plane = static_cast<F*>(pa.act) + (size_t)l * pa.act_plane;
+      if constexpr (OP == OP_BWD) load_fields<M, V, REAL>(u, plane, vb0, pa.vend, pa.N, pa.ldu, j);
+      else store_fields<M, V, REAL>(u, plane, vb0, pa.vend, pa.N, pa.ldu, j);
+      layer_any<OP, M, V, REAL, GR>(kinds[l], reinterpret_cast<const float4*>(st + (size_t)(l - lo) * layer_bytes), G,
+                                    j, r, u, w, reinterpret_cast<float4*>(gst_warp + (size_t)(l - lo) * gst_layer));
+    }
+    return;
+  }
   int i = 0;
   while (i < nl) {
     const int l0 = (OP == OP_BWD) ? (hi - 1 - i) : (lo + i);
@@ -717,10 +732,10 @@ __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem
       if (tid == 0) issue_d(c);
     }
     const unsigned char* st = ring + (size_t)(c % a.S) * a.CL * a.layer_bytes;
-    run_chunk<OP, M, V, REAL, GR>(kinds, st, a.layer_bytes, lo, hi, gst_warp, gst_layer, G, j, r, u, w);
+    run_chunk<OP, M, V, REAL, GR>(a, vb0, kinds, st, a.layer_bytes, lo, hi, gst_warp, gst_layer, G, j, r, u, w);
     __syncthreads();
     if constexpr (OP == OP_BWD && kDirect) chunk_reduce_direct<M, GR>(a, kinds, lo, hi - lo, gst, np2, G);
-    if constexpr (OP == OP_BWD && (GR == 3 || GR == 4)) chunk_reduce_raw<M>(a, kinds, lo, hi - lo, gst, np2, G);
+    if constexpr (OP == OP_BWD && GR == 4) chunk_reduce_raw<M>(a, kinds, lo, hi - lo, gst, np2, G);
     if constexpr (kDT) {
       const bool okd = mbar_wait_bounded(smem_u32(bars + a.S), (uint32_t)(c & 1));
       if (__syncthreads_or(!okd)) {
@@ -747,7 +762,7 @@ prop_kernel(const PropArgs a0) {
   const int G = GT ? GT : a.G;
   a.v0 = blockIdx.x * (a.W * (32 / G) * V);
   a.vend = a.B;
-  if (OP == OP_BWD) a.partial = a0.partial + (size_t)blockIdx.x * a.L * ((G * M) >> 1);
+  if (OP == OP_BWD) a.partial = a0.partial + (size_t)blockIdx.x * a.L * ((G * M) >> 1) * (GR == 4 ? 4 : 1);
   prop_body<OP, M, V, REAL, GT, GR>(a, smem);
 }
 

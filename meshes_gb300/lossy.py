@@ -1,0 +1,193 @@
+"""Lossy meshes: generic 2x2 crossings with a checkpointed adjoint on the sm_103a kernels.
+
+The lossless path back-propagates by inverting each layer with T^H (the reference's c/dot.cpp:75-80 and
+gpu/backprop.cu do the same), which needs no stored activations but is exact only for unitary crossings.
+A lossy crossing - the generic MZI of crossing.py:444-488, with phase errors and gains g_ij - breaks it.
+Here the adjoint keeps the mesh input of every segment of ``segment`` = ceil(sqrt(L)) layers during the
+forward pass; back-propagation then walks the segments in reverse, recomputes each segment's layer inputs
+from its checkpoint (one forward launch that writes them to a (segment, B, N) buffer) and back-propagates
+through the segment from those stored inputs (one launch plus a deterministic reduction).  Memory is
+about 2 sqrt(L) fields instead of L; work is one extra forward pass.
+
+The crossing is given as its transfer matrices ``T`` (L, N/2, 2, 2), complex, in the reference's slot
+grid (gpu/mesh.py:77-81); ``mzi_generic_T`` builds them from (theta, phi) and the 14 error parameters
+with differentiable torch operations, so gradients reach the phases (or any other parameterisation)
+through PyTorch's own autograd of T.  The kernel returns dJ/dT as sum_b g_i conj(x_j) = 2 dJ/dT_ij*,
+PyTorch's gradient convention for complex tensors.
+"""
+from __future__ import annotations
+
+import math
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import geometry as geom
+from ._lib import GENERIC, GEO_FFT, GEO_NN, OP_BWD_STORED, OP_FWD, check, load
+from .mesh import _stream
+
+
+def mzi_generic_T(p: torch.Tensor, s: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """(..., 2, 2) complex T of the lossy generic MZI, T = S(beta) D2 S(alpha) D1 (crossing.py:466-488).
+
+    p (..., 2) = (theta, phi); s (..., 14) = (alpha, beta, fabrication phase errors e11, e21, e12, e22,
+    crosstalk phase errors x11, x21, x12, x22, log-gains g11, g21, g12, g22);
+    D1 = diag(exp(i(phi + e11 + x11) + g11/2), exp(i(e21 + x21) + g21/2)),
+    D2 = diag(exp(i(theta + e12 + x12) + g12/2), exp(i(e22 + x22) + g22/2)),
+    S(a) = [[cos(pi/4 + a), i sin(pi/4 + a)], [i sin(pi/4 + a), cos(pi/4 + a)]].
+    """
+    if s is None:
+        s = p.new_zeros(p.shape[:-1] + (14,))
+    th, ph = p[..., 0], p[..., 1]
+
+    def ep(phase, gain):                       # exp(i phase + gain / 2)
+        return torch.exp(torch.complex(gain / 2, phase))
+
+    d1a, d1b = ep(ph + s[..., 2] + s[..., 6], s[..., 10]), ep(s[..., 3] + s[..., 7], s[..., 11])
+    d2a, d2b = ep(th + s[..., 4] + s[..., 8], s[..., 12]), ep(s[..., 5] + s[..., 9], s[..., 13])
+    ca, sa = torch.cos(math.pi / 4 + s[..., 0]), torch.sin(math.pi / 4 + s[..., 0])
+    cb, sb = torch.cos(math.pi / 4 + s[..., 1]), torch.sin(math.pi / 4 + s[..., 1])
+    # D2 S(alpha) D1
+    n00, n01 = d2a * ca * d1a, d2a * (1j * sa) * d1b
+    n10, n11 = d2b * (1j * sa) * d1a, d2b * ca * d1b
+    # S(beta) (D2 S(alpha) D1)
+    t00, t01 = cb * n00 + (1j * sb) * n10, cb * n01 + (1j * sb) * n11
+    t10, t11 = (1j * sb) * n00 + cb * n10, (1j * sb) * n01 + cb * n11
+    return torch.stack([torch.stack([t00, t01], -1), torch.stack([t10, t11], -1)], -2)
+
+
+class LossyMesh:
+    """Geometry of a mesh of generic (possibly lossy) crossings; ``mesh(x, T)`` is y = U(T) x.
+
+    Nearest-neighbour geometry (``lens``, ``shifts``, as gpu/mesh.py:50-60) or butterfly/FFT strides.
+    ``segment`` is the checkpoint spacing of the adjoint (default ceil(sqrt(L))).
+    """
+
+    def __init__(self, N: int, lens=None, shifts=None, strides=None, device=None, segment: Optional[int] = None):
+        load()
+        assert N % 2 == 0
+        self.N = int(N)
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        if strides is not None:
+            self.geometry = GEO_FFT
+            self.strides_h = [int(v) for v in np.asarray(strides).reshape(-1)]
+            geom.validate_fft(N, self.strides_h)
+            self.L = len(self.strides_h)
+            self.strides = torch.tensor(self.strides_h, dtype=torch.int32, device=self.device)
+            self.lens = self.shifts = None
+            active = np.ones((self.L, N // 2), dtype=bool)
+        else:
+            self.geometry = GEO_NN
+            self.lens_h = [int(v) for v in np.asarray(lens).reshape(-1)]
+            self.shifts_h = [int(v) for v in np.asarray(shifts).reshape(-1)]
+            geom.validate_nn(N, self.lens_h, self.shifts_h)
+            self.L = len(self.lens_h)
+            self.lens = torch.tensor(self.lens_h, dtype=torch.int32, device=self.device)
+            self.shifts = torch.tensor(self.shifts_h, dtype=torch.int32, device=self.device)
+            self.strides = None
+            active = np.zeros((self.L, N // 2), dtype=bool)
+            for l, (ln, sh) in enumerate(zip(self.lens_h, self.shifts_h)):
+                active[l, sh // 2: sh // 2 + ln] = True
+        self.active = torch.as_tensor(active, device=self.device)
+        self.segment = int(segment) if segment else max(1, math.ceil(math.sqrt(max(self.L, 1))))
+        self._ws = {}
+
+    # ---- plumbing
+    def _geo(self):
+        if self.geometry == GEO_FFT:
+            return None, None, self.strides.data_ptr()
+        return self.lens.data_ptr(), self.shifts.data_ptr(), None
+
+    def _workspace(self, op: int, B: int):
+        lib = load()
+        nb = lib.mg_workspace_bytes(op, self.N, self.L, B, GENERIC, self.geometry, None)
+        if nb == 0:
+            check(-1, "mg_workspace_bytes")
+        buf = self._ws.get(op)
+        if buf is None or buf.numel() < nb:
+            buf = torch.empty(nb, dtype=torch.uint8, device=self.device)
+            check(lib.mg_workspace_init(buf.data_ptr(), nb, _stream(self.device)), "mg_workspace_init")
+            self._ws[op] = buf
+        return buf.data_ptr(), buf.numel()
+
+    def _build(self, op: int, Tc: torch.Tensor, B: int):
+        ws, nb = self._workspace(op, B)
+        check(load().mg_build_tiles(op, self.N, self.L, self.geometry, *self._geo(), GENERIC, None, 0, None, 0, None,
+                                    Tc.data_ptr(), None, B, None, ws, nb, _stream(self.device)), "mg_build_tiles")
+        return ws, nb
+
+    def _range(self, op, l0, l1, B, in0, in1, out0, out1, act, dT, ws, nb):
+        ptr = (lambda t: None if t is None else t.data_ptr())
+        check(load().mg_propagate_range(op, self.N, self.L, l0, l1, B, GENERIC, self.geometry, ptr(in0), ptr(in1),
+                                        ptr(out0), ptr(out1), self.N, ptr(act), ptr(dT), 0, None, ws, nb,
+                                        _stream(self.device)), "mg_propagate_range")
+
+    def status(self, clear: bool = True) -> int:
+        """Kernel status word of the last launches (0 = ok); reads both workspaces."""
+        lib = load()
+        st = 0
+        for buf in self._ws.values():
+            r = lib.mg_read_status(buf.data_ptr(), int(clear), _stream(self.device))
+            if r < 0:
+                check(r, "mg_read_status")
+            st = st or r
+        return st
+
+    # ---- user API
+    def T(self, p: torch.Tensor, s: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """Lossy generic-MZI transfer matrices (L, N/2, 2, 2) from p (L, N/2, 2) and s (L, N/2, 14)."""
+        return mzi_generic_T(p, s)
+
+    def __call__(self, x: torch.Tensor, T: torch.Tensor) -> torch.Tensor:
+        return LossyMeshFunction.apply(x, T, self)
+
+
+class LossyMeshFunction(torch.autograd.Function):
+    """y = U(T) x for x (B, N) complex, T (L, N/2, 2, 2) complex; gradients to x and T."""
+
+    @staticmethod
+    def forward(ctx, x: torch.Tensor, T: torch.Tensor, mesh: LossyMesh):
+        assert x.dim() == 2 and x.shape[1] == mesh.N, "x must be (B, N) with N=%d" % mesh.N
+        assert tuple(T.shape) == (mesh.L, mesh.N // 2, 2, 2), "T must be (L, N/2, 2, 2)"
+        x = x.detach().to(device=mesh.device, dtype=torch.complex64).contiguous()
+        Tc = T.detach().to(device=mesh.device, dtype=torch.complex64).contiguous()
+        B, L, seg = x.shape[0], mesh.L, mesh.segment
+        ckpts = [x]
+        cur = x
+        if B > 0 and L > 0:
+            ws, nb = mesh._build(OP_FWD, Tc, B)
+            for l0 in range(0, L, seg):
+                out = torch.empty_like(x)
+                mesh._range(OP_FWD, l0, min(L, l0 + seg), B, cur, None, out, None, None, None, ws, nb)
+                if l0 + seg < L:
+                    ckpts.append(out)
+                cur = out
+        y = cur.clone() if cur is x else cur
+        ctx.mesh = mesh
+        ctx.T_dtype = T.dtype
+        ctx.save_for_backward(Tc, *ckpts)
+        return y
+
+    @staticmethod
+    def backward(ctx, gy: torch.Tensor):
+        mesh = ctx.mesh
+        Tc, *ckpts = ctx.saved_tensors
+        B, N, L, seg = ckpts[0].shape[0], mesh.N, mesh.L, mesh.segment
+        g = gy.detach().to(torch.complex64).contiguous()
+        dT = torch.zeros((L, N // 2, 2, 2), dtype=torch.complex64, device=mesh.device)
+        if B > 0 and L > 0:
+            wsf, nbf = mesh._build(OP_FWD, Tc, B)
+            wsb, nbb = mesh._build(OP_BWD_STORED, Tc, B)
+            act = torch.empty((seg, B, N), dtype=torch.complex64, device=mesh.device)
+            starts = list(range(0, L, seg))
+            for k in range(len(starts) - 1, -1, -1):
+                l0, l1 = starts[k], min(L, starts[k] + seg)
+                # the inputs of layers l0..l1-1, recomputed from the segment's checkpoint
+                mesh._range(OP_FWD, l0, l1, B, ckpts[k], None, None, None, act, None, wsf, nbf)
+                gn = torch.empty_like(g)
+                mesh._range(OP_BWD_STORED, l0, l1, B, None, g, None, gn, act, dT, wsb, nbb)
+                g = gn
+        gx = g if ctx.needs_input_grad[0] else None
+        gT = dT.to(ctx.T_dtype) if ctx.needs_input_grad[1] else None
+        return gx, gT, None

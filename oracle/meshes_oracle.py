@@ -38,7 +38,8 @@ from typing import Optional, Sequence
 
 import numpy as np
 
-CROSSINGS = {"mzi": (2, 2), "sym": (2, 1), "orth": (1, 0)}   # (n_p, n_s), gpu/mesh.py:72-73
+# (n_p, n_s): gpu/mesh.py:72-73; the lossy generic MZI has 14 splitter entries (crossing.py:448-452)
+CROSSINGS = {"mzi": (2, 2), "sym": (2, 1), "orth": (1, 0), "mzi_generic": (2, 14)}
 
 
 # ----------------------------------------------------------------------------------------------
@@ -157,8 +158,61 @@ def dT_orth(p, s=None):
     return 0.5 * np.array([[[C, S], [-S, C]]])
 
 
-T_FN = {"mzi": T_mzi, "sym": T_sym, "orth": T_orth}
-DT_FN = {"mzi": dT_mzi, "sym": dT_sym, "orth": dT_orth}
+def T_mzi_generic(p, s=None):
+    """(2, 2, k) complex128: lossy MZI with phase and gain errors; crossing.py:466-488 (out_phase False).
+
+    p (k, 2) = (theta, phi); s (k, 14) = (alpha, beta, fab phase errors e11, e21, e12, e22, crosstalk
+    phase errors x11, x21, x12, x22, log-gains g11, g21, g12, g22).  T = S(beta) D2 S(alpha) D1 with
+    D1 = diag(exp(i(phi + e11 + x11) + g11/2), exp(i(e21 + x21) + g21/2)),
+    D2 = diag(exp(i(theta + e12 + x12) + g12/2), exp(i(e22 + x22) + g22/2)),
+    S(a) = [[cos(pi/4 + a), i sin(pi/4 + a)], [i sin(pi/4 + a), cos(pi/4 + a)]].
+    """
+    p = np.asarray(p, dtype=np.float64).reshape(-1, 2)
+    k = p.shape[0]
+    s = np.zeros((k, 14)) if s is None else np.asarray(s, dtype=np.float64).reshape(-1, 14)
+    th, ph = p[:, 0], p[:, 1]
+    a, b = s[:, 0], s[:, 1]
+    e11, e21, e12, e22 = s[:, 2], s[:, 3], s[:, 4], s[:, 5]
+    x11, x21, x12, x22 = s[:, 6], s[:, 7], s[:, 8], s[:, 9]
+    g11, g21, g12, g22 = s[:, 10], s[:, 11], s[:, 12], s[:, 13]
+    d1 = (np.exp(1j * (ph + e11 + x11) + g11 / 2), np.exp(1j * (e21 + x21) + g21 / 2))
+    d2 = (np.exp(1j * (th + e12 + x12) + g12 / 2), np.exp(1j * (e22 + x22) + g22 / 2))
+
+    def split(al):
+        c, sn = np.cos(np.pi / 4 + al), np.sin(np.pi / 4 + al)
+        return np.array([[c, 1j * sn], [1j * sn, c]])
+
+    T = split(a) * np.array([d1[0], d1[1]])[None, :, :]                 # S(alpha) D1
+    T = np.array([d2[0], d2[1]])[:, None, :] * T                         # D2 S(alpha) D1
+    return np.einsum("ijk,jlk->ilk", split(b), T)                        # S(beta) D2 S(alpha) D1
+
+
+def dT_mzi_generic(p, s=None):
+    """(2, 2, 2, k): derivative of T_mzi_generic with respect to (theta, phi).
+
+    theta enters D2 and phi enters D1 through exp(i.) on their first diagonal entries, so
+    dT/dtheta = S(beta) diag(i, 0) D2 S(alpha) D1 and dT/dphi = T diag(i, 0).
+    """
+    p = np.asarray(p, dtype=np.float64).reshape(-1, 2)
+    T = T_mzi_generic(p, s)
+    dph = T.copy()
+    dph[:, 0] *= 1j
+    dph[:, 1] = 0
+    # S(beta)^-1 T = D2 S(alpha) D1; scale its first row by i, multiply back by S(beta)
+    k = p.shape[0]
+    ss = np.zeros((k, 14)) if s is None else np.asarray(s, dtype=np.float64).reshape(-1, 14)
+    c, sn = np.cos(np.pi / 4 + ss[:, 1]), np.sin(np.pi / 4 + ss[:, 1])
+    Sb = np.array([[c, 1j * sn], [1j * sn, c]])
+    Sb_inv = np.array([[c, -1j * sn], [-1j * sn, c]])                   # S(b)^H = S(b)^-1 (real angle)
+    inner = np.einsum("ijk,jlk->ilk", Sb_inv, T)
+    inner[1] = 0
+    inner[0] *= 1j
+    dth = np.einsum("ijk,jlk->ilk", Sb, inner)
+    return np.array([dth, dph])
+
+
+T_FN = {"mzi": T_mzi, "sym": T_sym, "orth": T_orth, "mzi_generic": T_mzi_generic}
+DT_FN = {"mzi": dT_mzi, "sym": dT_sym, "orth": dT_orth, "mzi_generic": dT_mzi_generic}
 
 
 # ----------------------------------------------------------------------------------------------

@@ -159,6 +159,30 @@ def main(ref_path):
          p=p_cr.reshape(L, N // 2, 2), s=bf.p_splitter.reshape(L, N // 2, 2), x=x, y=y, g=g,
          dJdp=dJdp[:n_cr * 2].reshape(L, N // 2, 2), g_in=dJdv.T)
 
+    # Lossy generic MZI (crossing.py:444-488: phase errors and gains g_ij < 0) on a Clements mesh: the
+    # reference's forward dot only.  Its dot_vjp raises NotImplementedError for this crossing (no dT),
+    # so the lossy gradient is pinned by complex128 central differences in the tests instead.
+    from meshes.crossing import MZICrossingGeneric
+    N = 8
+    n_cr = N * (N - 1) // 2
+    sp = np.zeros((n_cr, 14))
+    sp[:, :2] = rng.normal(0, 0.02, (n_cr, 2))
+    sp[:, 2:10] = rng.normal(0, 0.05, (n_cr, 8))
+    sp[:, 10:] = -np.abs(rng.normal(0.1, 0.05, (n_cr, 4)))
+    sp = sp.astype(np.float32).astype(np.float64)
+    net = ClementsNetwork(N=N, is_phase=False, phi_out=None, X=MZICrossingGeneric(), p_splitter=sp)
+    lens, shifts = list(map(int, net.lens)), list(map(int, net.shifts))
+    p_cr = rng.uniform(0, 2 * np.pi, (n_cr, 2)).astype(np.float32).astype(np.float64)
+    net.p_phase[:n_cr * 2] = p_cr.reshape(-1)
+    B = 5
+    x = (rng.standard_normal((B, N)) + 1j * rng.standard_normal((B, N)))
+    x /= np.linalg.norm(x, axis=1, keepdims=True)
+    y = net.dot(x.T).T
+    T = np.moveaxis(np.asarray(net.X.T(p_cr, sp)), -1, 0)                # (n_cr, 2, 2)
+    save("clements_mzigeneric_N8_lossy", N=N, L=len(lens), crossing="mzi_generic", lens=np.array(lens),
+         shifts=np.array(shifts), p=flat_to_grid(p_cr, lens, shifts, N, 2), s=flat_to_grid(sp, lens, shifts, N, 14),
+         T=flat_to_grid(T.reshape(n_cr, 4), lens, shifts, N, 4).reshape(len(lens), N // 2, 2, 2), x=x, y=y)
+
     print("wrote", *written, sep="\n  ")
 
 

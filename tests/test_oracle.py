@@ -134,6 +134,50 @@ def test_lossy_adjoint_matches_finite_differences():
     assert O.rel_err(Gu, G) > 1e-3
 
 
+def _lossy_mesh(rng, N, gain=0.1):
+    """Clements mesh of lossy generic MZIs: phase errors and log-gains g_ij ~ -|N(gain, gain/2)|."""
+    om = O.random_mesh(rng, N, "clements", "mzi_generic", 0.02)
+    s = np.zeros((om.L, N // 2, 14))
+    s[..., :10] = rng.normal(0, 0.03, (om.L, N // 2, 10))
+    s[..., 10:] = -np.abs(rng.normal(gain, gain / 2, (om.L, N // 2, 4)))
+    s[~om.active_mask()] = 0
+    om.s = s
+    return om
+
+
+def test_lossy_crossing_matches_reference_fixture():
+    """T of the lossy generic MZI and the forward through a lossy Clements mesh, against the reference."""
+    f = np.load(os.path.join(GOLDEN, "clements_mzigeneric_N8_lossy.npz"))
+    om = O.OracleMesh(N=int(f["N"]), L=int(f["L"]), crossing="mzi_generic", lens=list(f["lens"]),
+                      shifts=list(f["shifts"]), p=f["p"], s=f["s"])
+    mask = om.active_mask()
+    assert np.abs(om.T_grid()[mask] - f["T"][mask]).max() < 1e-14
+    y = O.propagate(om, f["x"])
+    assert O.rel_err(y, f["y"]) < 1e-13
+    assert np.linalg.norm(y) < 0.9 * np.linalg.norm(f["x"])          # the mesh loses power
+
+
+def test_lossy_generic_gradient_central_differences():
+    """dJ/dp of a lossy mesh from stored activations (vjp_stored + dT_mzi_generic) equals complex128
+    central differences; the T^H-inversion adjoint of the unitary path does not."""
+    rng = np.random.default_rng(14)
+    om = _lossy_mesh(rng, 8)
+    x = O.unit_columns(rng, 8, 5)
+    t = O.unit_columns(rng, 8, 5)
+
+    def loss(p):
+        return float(np.sum(np.abs(O.propagate(om, x, p) - t) ** 2))
+
+    y = O.propagate(om, x)
+    G, _ = O.vjp_stored(om, x, 2 * (y - t))
+    dp = O.contract_dp(om, G)
+    idx = np.flatnonzero(np.broadcast_to(om.active_mask()[..., None], om.p.shape))
+    fd = O.central_difference(loss, om.p.astype(np.float64), idx, h=1e-6)
+    assert np.allclose(dp.reshape(-1)[idx], fd, rtol=1e-6, atol=1e-9)
+    Gu, _, _ = O.vjp_unitary(om, y, 2 * (y - t))
+    assert O.rel_err(O.contract_dp(om, Gu).reshape(-1)[idx], fd) > 1e-2
+
+
 def test_geometry_helpers_agree():
     from meshes_gb300 import geometry as gm
     for N in (2, 4, 8, 10, 64, 256):
