@@ -225,6 +225,17 @@ int mg_propagate_range(int op, int N, int L, int l0, int l1, int B, int crossing
                        const void* in1, void* out0, void* out1, int ldu, void* act, void* dT, int accumulate,
                        const mg_config* cfg, void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- phase screen (the reference's is_phase / phi_pos, c/dot.cpp:97-143; its GPU API forbids it) -----
+ * mg_phase_screen: u_out = exp(i sgn ph) u_in elementwise per mode (ph: N floats; fields complex64 (B, N)
+ * with leading dimension ldu; u_out may alias u_in); with du_out, also du_out = exp(i sgn ph) du_in +
+ * i dph u_out (du_in and dph may be NULL = 0), the forward-mode derivative of the screen.
+ * mg_phase_screen_grad: dph[k] (= or, with accumulate, +=) sum_b Re(conj(g_bk) i u_bk) for the field u
+ * after the screen and g = 2 dJ/du* there; deterministic. */
+int mg_phase_screen(int N, int B, const float* ph, const float* dph, int sgn, const void* u_in, void* u_out,
+                    const void* du_in, void* du_out, int ldu, void* stream);
+int mg_phase_screen_grad(int N, int B, const void* u, const void* g, int ldu, float* dph, int accumulate,
+                         void* stream);
+
 /* ---- measurement helpers -------------------------------------------------------------------- */
 
 /* FP32 FMA throughput probe: `blocks` x `threads` threads each run `iters` iterations of 64

@@ -82,6 +82,9 @@ _SIGS = {
     "mg_propagate_range": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p,
                                    c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_int, POINTER(mg_config), c_void_p,
                                    c_size_t, c_void_p]),
+    "mg_phase_screen": (c_int, [c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
+                                c_void_p]),
+    "mg_phase_screen_grad": (c_int, [c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p]),
     "mg_fma_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
     "mg_plan": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, POINTER(mg_config), POINTER(mg_plan_info)]),
     # mesh and item arrays live in device memory: passed as raw addresses

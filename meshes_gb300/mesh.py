@@ -54,8 +54,11 @@ class MeshNetworkGPU:
 
     def __init__(self, N: int, L: int, lens=None, shifts=None, p_phase=None, p_splitter=None, X: str = "mzi",
                  phi_pos: str = "out", is_phase: bool = True, strides=None, device=None):
-        assert not is_phase, "is_phase=True is not supported (reference gpu/mesh.py:65)"
         assert X in ["mzi", "sym", "orth"]
+        assert phi_pos in ["in", "out"]
+        # the reference GPU API forbids the phase screen (gpu/mesh.py:65); here it is supported for complex
+        # crossings as the reference CPU path defines it (c/dot.cpp:97-143)
+        assert not (is_phase and X == "orth"), "a phase screen needs a complex crossing"
         assert N % 2 == 0
         load()
         self._N, self._L, self.X = int(N), int(L), X
@@ -168,6 +171,14 @@ class MeshNetworkGPU:
 
     # ---- forward / forward-mode derivative (gpu/mesh.py:147-174)
     def dot(self, v, p_phase=None, p_splitter=None, dp=None, dv=None, out=None, dout=None):
+        """y = U v (v (N, B)); with dp and/or dv also the forward-mode derivative dy (gpu/mesh.py:147-174).
+        With is_phase, the N screen phases (the tail of p_phase) act before (phi_pos 'in') or after
+        ('out') the mesh."""
+        if not self.is_phase:
+            return self._dot_mesh(v, p_phase, p_splitter, dp, dv, out, dout)
+        return self._dot_screened(v, p_phase, p_splitter, dp, dv, out, dout)
+
+    def _dot_mesh(self, v, p_phase=None, p_splitter=None, dp=None, dv=None, out=None, dout=None):
         lib = load()
         v, ldu_in = self._field(v)
         p, s = self._defaults(p_phase, p_splitter)
@@ -201,7 +212,7 @@ class MeshNetworkGPU:
                 dv = dv.t().contiguous().t()
             o2, _ = self._out(None, B)
             d2, _ = self._out(None, B)
-            self.dot(v, p, s, dp=dpp, dv=dv, out=o2, dout=d2)
+            self._dot_mesh(v, p, s, dp=dpp, dv=dv, out=o2, dout=d2)
             out.copy_(o2)
             dout.copy_(d2)
             return out, dout
@@ -243,12 +254,17 @@ class MeshNetworkGPU:
         a caller-zeroed array); otherwise a fresh array is returned.  Unlike the reference, the input
         array ``v`` is never overwritten with the reconstructed input field.
         """
-        assert not self.is_phase
         assert vpos in ["in", "out"]
+        if self.is_phase:
+            return self._grad_screened(v, dJdv, p_phase, p_splitter, out_dp, out_dJdv, vpos)
+        return self._grad_mesh(v, dJdv, p_phase, p_splitter, out_dp, out_dJdv, vpos)
+
+    def _grad_mesh(self, v, dJdv, p_phase=None, p_splitter=None, out_dp=None, out_dJdv=None, vpos="in",
+                   out_vin=None):
         lib = load()
         p, s = self._defaults(p_phase, p_splitter)
         if vpos == "in":
-            v = self.dot(v, p_phase, p_splitter)
+            v = self._dot_mesh(v, p_phase, p_splitter)
         else:
             v, _ = self._field(v)
         if callable(dJdv):
@@ -262,7 +278,7 @@ class MeshNetworkGPU:
             g = g.t().contiguous().t()
             ldu = self.N
             if ldu_o != ldu:
-                res = self.grad_phi(v2, g, p, s, out_dp=out_dp, vpos="out")
+                res = self._grad_mesh(v2, g, p, s, out_dp=out_dp, vpos="out", out_vin=out_vin)
                 out_dJdv.copy_(res[1])
                 return res[0], out_dJdv
         else:
@@ -276,10 +292,93 @@ class MeshNetworkGPU:
         wsb = lib.mg_workspace_bytes(OP_BWD, self.N, self.L, B, self.crossing, self.geometry, None)
         ws, wsn = self._ws[OP_BWD].get(wsb)
         fn = lib.mg_backdiff_ft if self.geometry == GEO_FFT else lib.mg_backdiff
+        if out_vin is not None:
+            assert out_vin.shape == (self.N, B) and out_vin.stride(0) == 1 and (B == 1 or out_vin.stride(1) == ldu)
         check(fn(self.N, self.L, B, *self._geo_args(), pptr, out_dp.data_ptr(), ldp, sptr, lds, v2.data_ptr(),
-                 g.data_ptr(), None, out_dJdv.data_ptr(), ldu, self.crossing, accumulate, ws, wsn,
-                 _stream(self.device)), fn.__name__)
+                 g.data_ptr(), None if out_vin is None else out_vin.data_ptr(), out_dJdv.data_ptr(), ldu,
+                 self.crossing, accumulate, ws, wsn, _stream(self.device)), fn.__name__)
         return out_dp, out_dJdv
+
+    # ---- phase screen: is_phase with phi_pos 'in' (y = U D v) or 'out' (y = D U v), D = diag(exp(i ph)),
+    # the screen step of the reference CPU path (c/dot.cpp:97-143, mesh.py:335-341)
+    def _fresh(self, v) -> torch.Tensor:
+        """(N, B) field as a view of a (B, N) row-major tensor (leading dimension N)."""
+        v, ldu = self._field(v)
+        return v if (ldu == self.N and v.stride(0) == 1) else v.t().contiguous().t()
+
+    def _screen(self, ph, sign, u, du=None, dph=None, inplace=False):
+        """exp(i sign ph) u (and its derivative along dph) on fields with leading dimension N."""
+        B = u.shape[1]
+        out = u if inplace else self._out(None, B)[0]
+        dout = None
+        if du is not None or dph is not None:
+            dout = du if (inplace and du is not None) else self._out(None, B)[0]
+        ptr = (lambda t: None if t is None else t.data_ptr())
+        check(load().mg_phase_screen(self.N, B, ph.data_ptr(), ptr(dph), sign, u.data_ptr(), out.data_ptr(), ptr(du),
+                                     ptr(dout), self.N, _stream(self.device)), "mg_phase_screen")
+        return out, dout
+
+    def _dot_screened(self, v, p_phase, p_splitter, dp, dv, out, dout):
+        p, s = self._defaults(p_phase, p_splitter)
+        ph = p[self.n_cr * self.X_np:]
+        dpp = None if dp is None else self._param(dp).reshape(-1)
+        if dpp is not None and dpp.numel() == 0:
+            dpp = None
+        if dpp is not None:
+            assert dpp.numel() == p.numel()
+        dph = None if dpp is None else dpp[self.n_cr * self.X_np:]
+        diff = dpp is not None or dv is not None
+        if self.phi_pos == "in":
+            u, du = self._screen(ph, 1, self._fresh(v), None if dv is None else self._fresh(dv), dph)
+            if diff:
+                return self._dot_mesh(u, p, s, dp=dpp, dv=du, out=out, dout=dout)
+            return self._dot_mesh(u, p, s, out=out)
+        if diff:
+            y, dy = self._dot_mesh(v, p, s, dp=dpp, dv=dv)
+            y, dy = self._screen(ph, 1, y, dy, dph, inplace=True)
+        else:
+            y, dy = self._screen(ph, 1, self._dot_mesh(v, p, s), inplace=True)
+        if out is not None:
+            out.copy_(y)
+            y = out
+        if diff and dout is not None:
+            dout.copy_(dy)
+            dy = dout
+        return (y, dy) if diff else y
+
+    def _grad_screened(self, v, dJdv, p_phase, p_splitter, out_dp, out_dJdv, vpos):
+        lib = load()
+        p, s = self._defaults(p_phase, p_splitter)
+        ncp = self.n_cr * self.X_np
+        ph = p[ncp:]
+        y = self._dot_screened(v, p, s, None, None, None, None) if vpos == "in" else self._fresh(v)
+        if callable(dJdv):
+            dJdv = dJdv(y)
+        g = self._fresh(dJdv)
+        B = y.shape[1]
+        accumulate = 1 if out_dp is not None else 0
+        if out_dp is None:
+            out_dp = torch.zeros(p.numel(), dtype=torch.float32, device=self.device)
+        else:
+            assert isinstance(out_dp, torch.Tensor) and out_dp.numel() == p.numel() and out_dp.is_contiguous()
+        dph = out_dp[ncp:]
+        stream = _stream(self.device)
+        if self.phi_pos == "out":
+            check(lib.mg_phase_screen_grad(self.N, B, y.data_ptr(), g.data_ptr(), self.N, dph.data_ptr(), accumulate,
+                                           stream), "mg_phase_screen_grad")
+            ym, _ = self._screen(ph, -1, y)
+            gm, _ = self._screen(ph, -1, g)
+            _, gx = self._grad_mesh(ym, gm, p, s, out_dp=out_dp, vpos="out")
+        else:
+            vin = self._out(None, B)[0]
+            _, gm = self._grad_mesh(y, g, p, s, out_dp=out_dp, vpos="out", out_vin=vin)
+            check(lib.mg_phase_screen_grad(self.N, B, vin.data_ptr(), gm.data_ptr(), self.N, dph.data_ptr(),
+                                           accumulate, stream), "mg_phase_screen_grad")
+            gx, _ = self._screen(ph, -1, gm, inplace=True)
+        if out_dJdv is not None:
+            out_dJdv.copy_(gx)
+            gx = out_dJdv
+        return out_dp, gx
 
     def matrix(self, p_phase=None, p_splitter=None):
         return self.dot(torch.eye(self.N, dtype=self.dtype, device=self.device), p_phase, p_splitter)

@@ -425,6 +425,47 @@ def vjp_stored(mesh: OracleMesh, x: np.ndarray, g: np.ndarray, p=None):
     return G, np.ascontiguousarray(gg.T)
 
 
+# ----------------------------------------------------------------------------------------------
+# phase screen (is_phase / phi_pos; the screen step of c/dot.cpp:97-143): y = D U x for pos "out",
+# y = U D x for pos "in", D = diag(exp(i ph)) over the N modes
+# ----------------------------------------------------------------------------------------------
+def screen(v: np.ndarray, ph, sign: int = 1) -> np.ndarray:
+    """v (B, N) times exp(i sign ph) per mode."""
+    return np.asarray(v, dtype=np.complex128) * np.exp(1j * sign * np.asarray(ph, dtype=np.float64))[None, :]
+
+
+def propagate_screened(mesh: OracleMesh, x: np.ndarray, ph, pos: str, p=None) -> np.ndarray:
+    if pos == "in":
+        return propagate(mesh, screen(x, ph), p)
+    return screen(propagate(mesh, x, p), ph)
+
+
+def fwddiff_screened(mesh: OracleMesh, x, ph, pos: str, dp, dph, dx=None, p=None):
+    """(y, dy) along (dp, dph): the screen contributes d(exp(i ph) u) = exp(i ph) du + i dph exp(i ph) u."""
+    dph = np.asarray(dph, dtype=np.float64)
+    dx = np.zeros_like(np.asarray(x, dtype=np.complex128)) if dx is None else np.asarray(dx, np.complex128)
+    if pos == "in":
+        u = screen(x, ph)
+        du = screen(dx, ph) + 1j * dph[None, :] * u
+        return fwddiff(mesh, u, dp, du, p)
+    y, dy = fwddiff(mesh, x, dp, dx, p)
+    y2 = screen(y, ph)
+    return y2, screen(dy, ph) + 1j * dph[None, :] * y2
+
+
+def grad_screened(mesh: OracleMesh, y, g, ph, pos: str, p=None):
+    """From the outputs (y, g = 2 dJ/dy*): (dJ/dp grid, dJ/dph, g_in), unitary mesh.
+    dJ/dph_k = sum_b Re(conj(g_k) i u_k) with (u, g) taken just after the screen."""
+    def dph_of(u, gg):
+        return np.real(np.sum(np.conj(gg) * 1j * u, axis=0))
+    if pos == "out":
+        dph = dph_of(y, g)
+        G, _, gin = vjp_unitary(mesh, screen(y, ph, -1), screen(g, ph, -1), p)
+        return contract_dp(mesh, G, p), dph, gin
+    G, u, gin_m = vjp_unitary(mesh, y, g, p)
+    return contract_dp(mesh, G, p), dph_of(u, gin_m), screen(gin_m, ph, -1)
+
+
 def contract_dp(mesh: OracleMesh, G: np.ndarray, p=None) -> np.ndarray:
     """dJ/dp (L, N//2, n_p) = Re sum_ij dT_ij/dp G_ij; crossing.py:146-163.  Inactive slots are 0."""
     D = mesh.dT_grid(p)

@@ -183,6 +183,30 @@ def main(ref_path):
          shifts=np.array(shifts), p=flat_to_grid(p_cr, lens, shifts, N, 2), s=flat_to_grid(sp, lens, shifts, N, 14),
          T=flat_to_grid(T.reshape(n_cr, 4), lens, shifts, N, 4).reshape(len(lens), N // 2, 2, 2), x=x, y=y)
 
+    # Phase screen (is_phase=True, phi_pos 'out' and 'in'; c/dot.cpp:97-143): forward, forward-mode
+    # derivative and dot_vjp of the reference, screen phases nonzero.
+    for pos in ("out", "in"):
+        N = 8
+        n_cr = N * (N - 1) // 2
+        net = ClementsNetwork(N=N, is_phase=True, phi_pos=pos, p_splitter=rng.normal(0, 0.02, (n_cr, 2)))
+        lens, shifts = list(map(int, net.lens)), list(map(int, net.shifts))
+        net.p_phase[:] = rng.uniform(0, 2 * np.pi, net.p_phase.shape).astype(np.float32).astype(np.float64)
+        net.p_splitter = net.p_splitter.astype(np.float32).astype(np.float64)
+        B = 5
+        x = (rng.standard_normal((B, N)) + 1j * rng.standard_normal((B, N)))
+        x /= np.linalg.norm(x, axis=1, keepdims=True)
+        y = net.dot(x.T).T
+        dp_full = rng.standard_normal(net.n_phase)
+        _, dy = net.dot(x.T, dp=dp_full)
+        t = (rng.standard_normal((B, N)) + 1j * rng.standard_normal((B, N)))
+        g = 2 * (y - t)
+        dJdp, dJdv = net.dot_vjp(y.T, g.T)
+        save("clements_mzi_N8_screen_" + pos, N=N, L=len(lens), crossing="mzi", phi_pos=pos, lens=np.array(lens),
+             shifts=np.array(shifts), p=flat_to_grid(net.p_phase[:n_cr * 2], lens, shifts, N, 2),
+             ph=net.p_phase[n_cr * 2:], s=flat_to_grid(net.p_splitter, lens, shifts, N, 2), x=x, y=y,
+             dp_dir=flat_to_grid(dp_full[:n_cr * 2], lens, shifts, N, 2), dph_dir=dp_full[n_cr * 2:], dy=dy.T,
+             g=g, dJdp=flat_to_grid(dJdp[:n_cr * 2], lens, shifts, N, 2), dJdph=dJdp[n_cr * 2:], g_in=dJdv.T)
+
     print("wrote", *written, sep="\n  ")
 
 

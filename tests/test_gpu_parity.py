@@ -41,7 +41,8 @@ def to_np(t):
 
 
 def fixtures():
-    return sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+    """Fixtures of the plain meshes (the phase-screen and lossy fixtures have their own tests)."""
+    return sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz") and "_screen_" not in f and "lossy" not in f)
 
 
 def load_fixture(name):
@@ -286,3 +287,58 @@ def test_shared_tiles_and_fused_l2_target(cr, N, B):
     assert O.rel_err(gx.cpu().numpy(), gin) < TOL
     assert O.rel_err(dp.cpu().numpy().reshape(om.L, N // 2, n_p), O.contract_dp(om, G)) < TOL
     assert lib.mg_read_status(ws.data_ptr(), 0, st) == 0
+
+
+@pytest.mark.parametrize("pos", ["out", "in"])
+def test_golden_phase_screen(pos):
+    """is_phase=True (forbidden by the reference GPU API, defined by its CPU path) against the reference's
+    own dot / fwd-diff / dot_vjp with a nonzero phase screen."""
+    from meshes_gb300 import MeshNetworkGPU
+    z = np.load(os.path.join(GOLDEN, "clements_mzi_N8_screen_%s.npz" % pos))
+    N, L = int(z["N"]), int(z["L"])
+    ncp = L * (N // 2) * 2
+    p_full = np.concatenate([z["p"].reshape(-1), z["ph"]]).astype(np.float32)
+    m = MeshNetworkGPU(N, L, z["lens"], z["shifts"], p_full, z["s"].astype(np.float32), "mzi", phi_pos=pos,
+                       is_phase=True)
+    assert O.rel_err(to_np(m.dot(to_dev(z["x"]))), z["y"]) < TOL
+    y, dy = m.dot(to_dev(z["x"]), dp=np.concatenate([z["dp_dir"].reshape(-1), z["dph_dir"]]).astype(np.float32))
+    assert O.rel_err(to_np(y), z["y"]) < TOL and O.rel_err(to_np(dy), z["dy"]) < TOL
+    dp, gin = m.grad_phi(to_dev(z["y"]), to_dev(z["g"]), vpos="out")
+    dp = dp.cpu().numpy()
+    assert O.rel_err(dp[:ncp].reshape(L, N // 2, 2), z["dJdp"]) < TOL
+    assert O.rel_err(dp[ncp:], z["dJdph"]) < TOL
+    assert O.rel_err(to_np(gin), z["g_in"]) < TOL
+
+
+@pytest.mark.parametrize("pos", ["out", "in"])
+@pytest.mark.parametrize("geo,N,B", [("clements", 64, 33), ("fft", 128, 20), ("reck", 30, 7)])
+def test_random_phase_screen(pos, geo, N, B):
+    from meshes_gb300 import MeshNetworkGPU
+    rng = np.random.default_rng(zlib.crc32(("%s%s%d" % (pos, geo, N)).encode()))
+    om = O.random_mesh(rng, N, geo, "mzi", 0.02)
+    ph = rng.uniform(0, 2 * np.pi, N).astype(np.float32)
+    p_full = np.concatenate([np.asarray(om.p, np.float32).reshape(-1), ph])
+    kw = dict(strides=om.strides) if om.fft else {}
+    m = MeshNetworkGPU(N, om.L, None if om.fft else om.lens, None if om.fft else om.shifts, p_full,
+                       np.asarray(om.s, np.float32), "mzi", phi_pos=pos, is_phase=True, **kw)
+    x = O.unit_columns(rng, N, B).astype(np.complex64)
+    t = O.unit_columns(rng, N, B).astype(np.complex64)
+    y_ref = O.propagate_screened(om, x, ph, pos)
+    assert O.rel_err(to_np(m.dot(to_dev(x))), y_ref) < TOL
+    # forward-mode derivative along a random direction of all phases, screen included
+    dpd = rng.standard_normal(p_full.size).astype(np.float32)
+    dpd[: om.p.size][~np.broadcast_to(om.active_mask()[..., None], om.p.shape).reshape(-1)] = 0
+    _, dy = m.dot(to_dev(x), dp=dpd)
+    _, dy_ref = O.fwddiff_screened(om, x, ph, pos, dpd[: om.p.size], dpd[om.p.size:])
+    assert O.rel_err(to_np(dy), dy_ref) < TOL
+    # gradient from the input (vpos "in") with a callable objective, then accumulated into out_dp
+    tt = to_dev(t)
+    dp, gin = m.grad_phi(to_dev(x), lambda yy: 2 * (yy - tt))
+    dp_ref, dph_ref, gin_ref = O.grad_screened(om, y_ref, 2 * (y_ref - t), ph, pos)
+    dp = dp.cpu().numpy()
+    assert O.rel_err(dp[: om.p.size].reshape(om.p.shape), dp_ref) < TOL
+    assert O.rel_err(dp[om.p.size:], dph_ref) < TOL
+    assert O.rel_err(to_np(gin), gin_ref) < TOL
+    acc = torch.ones(p_full.size, dtype=torch.float32, device="cuda")
+    m.grad_phi(to_dev(x), lambda yy: 2 * (yy - tt), out_dp=acc)
+    assert O.rel_err(acc.cpu().numpy() - 1.0, dp) < 1e-6

@@ -14,7 +14,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def fixtures():
-    return sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+    """Fixtures of the plain meshes (the phase-screen and lossy fixtures have their own tests)."""
+    return sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz") and "_screen_" not in f and "lossy" not in f)
 
 
 def load(name):
@@ -176,6 +177,23 @@ def test_lossy_generic_gradient_central_differences():
     assert np.allclose(dp.reshape(-1)[idx], fd, rtol=1e-6, atol=1e-9)
     Gu, _, _ = O.vjp_unitary(om, y, 2 * (y - t))
     assert O.rel_err(O.contract_dp(om, Gu).reshape(-1)[idx], fd) > 1e-2
+
+
+@pytest.mark.parametrize("pos", ["out", "in"])
+def test_phase_screen_matches_reference_fixtures(pos):
+    """Forward, forward-mode derivative and VJP of a Clements mesh with a phase screen (is_phase=True)."""
+    f = np.load(os.path.join(GOLDEN, "clements_mzi_N8_screen_%s.npz" % pos))
+    assert str(f["phi_pos"]) == pos
+    om = O.OracleMesh(N=int(f["N"]), L=int(f["L"]), crossing="mzi", lens=list(f["lens"]), shifts=list(f["shifts"]),
+                      p=f["p"], s=f["s"])
+    y = O.propagate_screened(om, f["x"], f["ph"], pos)
+    assert O.rel_err(y, f["y"]) < 1e-13
+    y2, dy = O.fwddiff_screened(om, f["x"], f["ph"], pos, f["dp_dir"], f["dph_dir"])
+    assert O.rel_err(y2, f["y"]) < 1e-13 and O.rel_err(dy, f["dy"]) < 1e-12
+    dp, dph, gin = O.grad_screened(om, f["y"], f["g"], f["ph"], pos)
+    assert O.rel_err(dp, f["dJdp"]) < 1e-12
+    assert O.rel_err(dph, f["dJdph"]) < 1e-12
+    assert O.rel_err(gin, f["g_in"]) < 1e-12
 
 
 def test_geometry_helpers_agree():
