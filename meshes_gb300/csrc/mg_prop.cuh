@@ -721,10 +721,11 @@ __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem
     const int lo = chunk_lo(c), hi = chunk_hi(c);
     const bool ok = mbar_wait_bounded(smem_u32(bars + (c % a.S)), (uint32_t)((c / a.S) & 1));
     if (__syncthreads_or(!ok)) {
-      // give up: record, wait (bounded) for the copies still in flight, leave
+      // give up: record, wait (bounded) for the copies still in flight, release the barriers, leave
       if (tid == 0) {
         set_status(a.status, ST_TIMEOUT);
         for (int cc = c + 1; cc < issued; ++cc) mbar_wait_bounded(smem_u32(bars + (cc % a.S)), (uint32_t)((cc / a.S) & 1));
+        for (int s = 0; s <= a.S; ++s) mbar_inval(smem_u32(bars + s));
       }
       return;
     }
@@ -742,6 +743,7 @@ __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem
         if (tid == 0) {
           set_status(a.status, ST_TIMEOUT);
           for (int cc = c + 1; cc < issued; ++cc) mbar_wait_bounded(smem_u32(bars + (cc % a.S)), (uint32_t)((cc / a.S) & 1));
+          for (int s = 0; s <= a.S; ++s) mbar_inval(smem_u32(bars + s));
         }
         return;
       }
@@ -749,6 +751,10 @@ __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem
     }
     if (tid == 0 && issued < nch) issue(issued++);
   }
+  // every copy has been waited for and every thread is past its last wait (the barrier after the last
+  // chunk): release the mbarriers so that a persistent caller can initialise them again
+  if (tid == 0)
+    for (int s = 0; s <= a.S; ++s) mbar_inval(smem_u32(bars + s));
   (void)R;
   store_fields<M, V, REAL>(u, a.out0, vb0, a.vend, a.N, a.ldu, j);
   if constexpr (OP != OP_FWD) store_fields<M, V, REAL>(w, a.out1, vb0, a.vend, a.N, a.ldu, j);

@@ -81,3 +81,30 @@ def test_batched_equals_plain_path_bitwise():
     from meshes_gb300.autograd import mesh_apply
     y_plain = mesh_apply(m, torch.tensor(x, dtype=torch.complex64, device="cuda"))
     assert torch.equal(y_plain, bm.states[0].y)
+
+
+def test_many_items_per_cta():
+    """A small persistent grid makes every CTA run many work items in turn (its pipeline barriers are
+    released and initialised again per item); forward and back-propagation against the oracle."""
+    from meshes_gb300.batched import BatchedMeshes
+    rng = np.random.default_rng(33)
+    specs = [("clements", "mzi", 64, 700), ("clements", "orth", 256, 90), ("reck", "mzi", 32, 300),
+             ("clements", "mzi", 256, 100), ("fft", "mzi", 128, 64)]
+    oms = [O.random_mesh(rng, N, geo, cr, 0.01 if cr == "mzi" else 0.0) for geo, cr, N, _ in specs]
+    xs = [O.unit_columns(rng, om.N, B, real=om.crossing == "orth") for om, (*_, B) in zip(oms, specs)]
+    gs = [O.unit_columns(rng, om.N, B, real=om.crossing == "orth") for om, (*_, B) in zip(oms, specs)]
+    bm = BatchedMeshes([gpu_mesh(om) for om in oms], [x.shape[0] for x in xs], grid=3)
+    assert bm.n_items > 3 * 4
+    for st, x, g in zip(bm.states, xs, gs):
+        st.x.copy_(torch.tensor(x, dtype=st.x.dtype))
+    bm.forward()
+    for st, g in zip(bm.states, gs):
+        st.gy.copy_(torch.tensor(g, dtype=st.gy.dtype))
+    bm.backward()
+    assert bm.check_status() == 0
+    for om, st, x, g in zip(oms, bm.states, xs, gs):
+        y_ref = O.propagate(om, x)
+        G, _, gin = O.vjp_unitary(om, y_ref, g)
+        assert O.rel_err(st.y.cpu().numpy(), y_ref) < TOL, (om.N, om.crossing)
+        assert O.rel_err(st.gx.cpu().numpy(), gin) < TOL, (om.N, om.crossing)
+        assert O.rel_err(st.dp.cpu().numpy(), O.contract_dp(om, G)) < TOL, (om.N, om.crossing)
