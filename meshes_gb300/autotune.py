@@ -1,8 +1,9 @@
 """Autotuner of the propagation kernels' tile configuration.
 
-For a shape (op, crossing, geometry, N, L, B) it times every valid candidate (modes per lane M,
-vectors per lane V, warps per CTA W, layers per pipeline stage CL, stages S) on the GPU - tiles built
-once, CUDA events on the launch stream, L2 flushed between repetitions - and keeps the fastest.
+For a shape (op, crossing, geometry, N, L, B) it times the valid candidates on the GPU - tiles built
+once, CUDA events on the launch stream, L2 flushed between repetitions - in two stages: the register
+blocking and CTA width (modes per lane M, vectors per lane V, warps per CTA W), then, around the
+winner, layers per pipeline stage CL and stages S - and keeps the fastest.
 Results live in ``tuned_configs.json`` next to this file (keyed by op/crossing/geometry/N and a batch
 range) and are loaded into the library's tuning table by ``load_table()`` (called on import of the
 package), so every call that passes no explicit configuration - the reference-shaped entry points
@@ -50,14 +51,18 @@ def load_table(path: str = TABLE) -> int:
     return n
 
 
-def candidates(op: int, N: int, real: bool) -> List[Tuple[int, int, int, int, int]]:
+def candidates(op: int, N: int, real: bool) -> List[Tuple[int, ...]]:
+    """Stage 1: the register blocking and CTA width (M, V, W), pipeline and schedule left to the heuristic."""
     Np = 1 << max(1, (N - 1).bit_length())
     Ms = [m for m in (2, 4, 8, 16) if m <= Np and Np // m <= 32]
     Vs = {OP_FWD: (2, 4, 8), OP_FWDDIFF: (1, 2, 4), OP_BWD: (1, 2, 4)}[op]
-    out = []
-    for M, V, W, CL, S in itertools.product(Ms, Vs, (2, 4, 8), (0, 4, 8, 16), (2, 3)):
-        out.append((M, V, W, CL, S))
-    return out
+    return [(M, V, W, 0, 0) for M, V, W in itertools.product(Ms, Vs, (2, 4, 8))]
+
+
+def refinements(c: Tuple[int, ...]) -> List[Tuple[int, ...]]:
+    """Stage 2 around a stage-1 winner: layers per pipeline stage CL and stages S."""
+    M, V, W = c[:3]
+    return [(M, V, W, CL, S) for CL, S in itertools.product((0, 4, 8, 16), (2, 3))]
 
 
 def tune(op: int, N: int, L: int, B: int, crossing: int = 0, geometry: int = 0, reps: int = 5,
@@ -90,17 +95,18 @@ def tune(op: int, N: int, L: int, B: int, crossing: int = 0, geometry: int = 0, 
     gi = torch.empty_like(x)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     results = {}
-    for c in (cands or candidates(op, N, real)):
+
+    def measure(c):
         cfg = _lib.config(*c)
         nb = lib.mg_workspace_bytes(op, N, L, B, crossing, geometry, _lib.cfg_ptr(cfg))
         if nb == 0:
-            continue
+            return
         ws = torch.empty(nb, dtype=torch.uint8, device=dev)
         lib.mg_workspace_init(ws.data_ptr(), nb, st)
         if lib.mg_build_tiles(op, N, L, geometry, *geo_args, crossing, p.data_ptr(), N // 2 * n_p,
                               None if s is None else s.data_ptr(), N // 2 * n_s, p.data_ptr() if op == OP_FWDDIFF
                               else None, None, None, B, _lib.cfg_ptr(cfg), ws.data_ptr(), nb, st):
-            continue
+            return
         args = {OP_FWD: (x.data_ptr(), None, y.data_ptr(), None), OP_FWDDIFF: (x.data_ptr(), g.data_ptr(),
                 y.data_ptr(), gi.data_ptr()), OP_BWD: (y.data_ptr(), g.data_ptr(), None, gi.data_ptr())}[op]
 
@@ -109,7 +115,7 @@ def tune(op: int, N: int, L: int, B: int, crossing: int = 0, geometry: int = 0, 
                                     ws.data_ptr(), nb, st)
 
         if run():
-            continue
+            return
         ts = []
         for _ in range(reps):
             flush.zero_()
@@ -119,7 +125,15 @@ def tune(op: int, N: int, L: int, B: int, crossing: int = 0, geometry: int = 0, 
             e1.record()
             torch.cuda.synchronize(dev)
             ts.append(e0.elapsed_time(e1))
-        results[c] = statistics.median(ts)
+        if lib.mg_read_status(ws.data_ptr(), 1, st) == 0:
+            results[c] = statistics.median(ts)
+
+    for c in (cands or candidates(op, N, real)):
+        measure(c)
+    if not cands and results:
+        for c in refinements(min(results, key=results.get)):
+            if c not in results:
+                measure(c)
     best = min(results, key=results.get)
     return best, results
 
@@ -154,7 +168,7 @@ def main():
     op = OPS[a.op]
     best, res = tune(op, a.N, L, a.B, CROSS[a.crossing], geo)
     for c, ms in sorted(res.items(), key=lambda kv: kv[1])[:8]:
-        print("M=%d V=%d W=%d CL=%d S=%d  %.4f ms" % (c + (ms,)))
+        print("M=%d V=%d W=%d CL=%d S=%d  %.4f ms" % (tuple(c) + (ms,)))
     if a.write:
         rng = tuple(a.B_range) if a.B_range else (a.B // 2 + 1, a.B * 2)
         record(op, CROSS[a.crossing], geo, a.N, rng, best, res[best])

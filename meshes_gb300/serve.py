@@ -79,8 +79,33 @@ class _Tick:
     event: torch.cuda.Event
     dev_off: int
     dev_bytes: int
-    host: torch.Tensor
-    out_spans: list
+    host: torch.Tensor            # pinned staging buffer (returned to the pool on retirement)
+    outs: tuple                   # result offsets and sizes in `host` (arrays over the tick's requests)
+
+
+_DESC = np.dtype(mg_batch_mesh)
+_ITEM = np.dtype(mg_batch_item)
+
+
+def _alignv(n):
+    return (n + ALIGN - 1) // ALIGN * ALIGN
+
+
+class _PinnedPool:
+    """Reusable pinned host buffers (one per tick in flight), grown on demand."""
+
+    def __init__(self):
+        self.free: List[torch.Tensor] = []
+
+    def get(self, n: int) -> torch.Tensor:
+        for i, t in enumerate(self.free):
+            if t.numel() >= n:
+                return self.free.pop(i)
+        return torch.empty(max(n, 1 << 20), dtype=torch.uint8, pin_memory=True)
+
+    def put(self, t: torch.Tensor):
+        self.free.append(t)
+        self.free.sort(key=lambda x: x.numel())
 
 
 class _Arena:
@@ -144,6 +169,26 @@ class MeshServer:
         self.ticks = 0
         self.error: Optional[BaseException] = None
         self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self.pool = _PinnedPool()
+        self._tables()
+
+    def _tables(self):
+        """Per-mesh constants as arrays indexed by mesh id (the tick packing is vectorised over requests)."""
+        R = self.res
+
+        def col(f):
+            return np.array([f(r) for r in R], dtype=np.int64)
+        self.t_N, self.t_L = col(lambda r: r.mesh.N), col(lambda r: r.mesh.L)
+        self.t_esz = col(lambda r: 4 if r.mesh.X == "orth" else 8)
+        self.t_cap, self.t_np2 = col(lambda r: r.cap), col(lambda r: r.np2)
+        self.t_cls, self.t_G, self.t_np = col(lambda r: r.cls), col(lambda r: r.G), col(lambda r: r.mesh.X_np)
+        self.t_mzi = col(lambda r: r.n_mzi)
+        self.t_op = {}
+        for op in (OP_FWD, OP_BWD):
+            self.t_op[op] = dict(CL=col(lambda r: r.info[op].CL), S=col(lambda r: r.info[op].S),
+                                 lb=col(lambda r: r.info[op].layer_bytes),
+                                 tiles=col(lambda r: r.ws[op].data_ptr() + r.info[op].off_tiles),
+                                 kinds=col(lambda r: r.ws[op].data_ptr() + r.info[op].off_kinds))
 
     # ---- programming (tiles resident on the device)
     def _program(self, m: MeshNetworkGPU) -> _Resident:
@@ -255,17 +300,22 @@ class MeshServer:
         while self.inflight and self.inflight[0].event.query():
             t = self.inflight.popleft()
             now = time.perf_counter()
-            host = t.host
-            for req, spans in zip(t.reqs, t.out_spans):
-                outs = []
-                for (off, nbytes, shape, dtype) in spans:
-                    a = host[off: off + nbytes].numpy().view(dtype).reshape(shape).copy()
-                    outs.append(a)
+            hv = t.host.numpy()
+            o_y, n_y, o_dp, n_dp, o_gx, gidx = (a.tolist() for a in t.outs)
+            res = [hv[o: o + n].view(q.x.dtype).reshape(q.x.shape).copy() for q, o, n in zip(t.reqs, o_y, n_y)]
+            for k, i in enumerate(gidx):                   # gradient requests: (y, dJ/dp, dJ/dx*)
+                q = t.reqs[i]
+                m = self.res[q.mesh_id].mesh
+                dp = hv[o_dp[k]: o_dp[k] + n_dp[k]].view(np.float32).reshape(m.L, m.N // 2, m.X_np).copy()
+                gx = hv[o_gx[k]: o_gx[k] + n_y[i]].view(q.x.dtype).reshape(q.x.shape).copy()
+                res[i] = (res[i], dp, gx)
+            for req, r in zip(t.reqs, res):
                 req.t_done = now
                 req.future.t_done = now                    # completion time, for latency accounting
                 if not req.future.done():
-                    req.future.set_result(outs[0] if req.gy is None else tuple(outs))
+                    req.future.set_result(r)
             self.arena.release(t.dev_off, t.dev_bytes)
+            self.pool.put(t.host)
             self.completed += len(t.reqs)
             done = True
         return done
@@ -291,131 +341,122 @@ class MeshServer:
         return True
 
     def _run(self, reqs: List[Request]):
+        """Pack one tick.  Device layout of its arena span (one H2D copy of the first part, one D2H copy of
+        the outputs): [descriptors fwd | descriptors bwd | items fwd | items bwd | queue heads | inputs x |
+        inputs gy][outputs y | outputs gx | outputs dJ/dp][gradient partials]."""
         lib = self.lib
-        # ---- device layout: [per-request buffers][descriptors fwd][descriptors bwd][items fwd][items bwd][head]
-        items_f, items_b = [], []
-        desc_f = (mg_batch_mesh * len(reqs))()
-        grads = [i for i, q in enumerate(reqs) if q.gy is not None]
-        desc_b = (mg_batch_mesh * max(len(grads), 1))()
-        layout = []                                        # per request: dict of offsets
-        off = 0
-        for q in reqs:
-            r = self.res[q.mesh_id]
-            b, N = q.x.shape
-            fe = _align(b * N * q.x.itemsize)
-            d = {"x": off, "y": off + fe}
-            off += 2 * fe
-            if q.gy is not None:
-                n_items = (b + r.cap - 1) // r.cap
-                d["gy"], d["gx"] = off, off + fe
-                off += 2 * fe
-                d["dp"] = off
-                off += _align(r.mesh.L * (N // 2) * r.mesh.X_np * 4)
-                d["part"] = off
-                off += _align(n_items * r.mesh.L * r.np2 * 8)
-            layout.append(d)
-        data_bytes = off
-        off_df = data_bytes
-        off_db = off_df + _align(ctypes.sizeof(desc_f))
-        n_if = sum((q.x.shape[0] + self.res[q.mesh_id].cap - 1) // self.res[q.mesh_id].cap for q in reqs)
-        n_ib = sum((reqs[i].x.shape[0] + self.res[reqs[i].mesh_id].cap - 1) // self.res[reqs[i].mesh_id].cap
-                   for i in grads)
-        off_if = off_db + _align(ctypes.sizeof(desc_b))
-        off_ib = off_if + _align(max(n_if, 1) * 16)
-        off_head = off_ib + _align(max(n_ib, 1) * 16)
-        total = off_head + ALIGN
+        K = len(reqs)
+        mid = np.fromiter((q.mesh_id for q in reqs), np.int64, K)
+        b = np.fromiter((q.x.shape[0] for q in reqs), np.int64, K)
+        isg = np.fromiter((q.gy is not None for q in reqs), bool, K)
+        gidx = np.flatnonzero(isg)
+        KG = len(gidx)
+        N, L, esz, cap, np2, n_p = (self.t_N[mid], self.t_L[mid], self.t_esz[mid], self.t_cap[mid], self.t_np2[mid],
+                                    self.t_np[mid])
+        fe = _alignv(b * N * esz)
+        nit = (b + cap - 1) // cap
+        dpn = L * (N // 2) * n_p * 4
+        # region sizes and per-request offsets inside each region
+        def region(sizes):
+            o = np.zeros(len(sizes), np.int64)
+            if len(sizes) > 1:
+                np.cumsum(sizes[:-1], out=o[1:])
+            return o, int(sizes.sum())
+        o_x, n_x = region(fe)
+        o_gy, n_gy = region(fe[gidx])
+        o_y, n_y = region(fe)
+        o_gx, n_gx = region(fe[gidx])
+        o_dp, n_dp = region(_alignv(dpn[gidx]))
+        o_pt, n_pt = region(_alignv(nit[gidx] * L[gidx] * np2[gidx] * 8))
+        n_if, n_ib = int(nit.sum()), int(nit[gidx].sum())
+        off_df = 0
+        off_db = off_df + _align(K * _DESC.itemsize)
+        off_if = off_db + _align(max(KG, 1) * _DESC.itemsize)
+        off_ib = off_if + _align(max(n_if, 1) * _ITEM.itemsize)
+        off_head = off_ib + _align(max(n_ib, 1) * _ITEM.itemsize)
+        off_x = off_head + ALIGN
+        off_gy = off_x + n_x
+        in_bytes = off_gy + n_gy                           # host -> device
+        off_y = in_bytes
+        off_gx = off_y + n_y
+        off_dp = off_gx + n_gx
+        out_end = off_dp + n_dp                            # device -> host: [off_y, out_end)
+        off_pt = out_end
+        total = off_pt + n_pt
         base_off = self.arena.alloc(total)
         if base_off is None:                               # raced with fragmentation: put the requests back
             with self.qlock:
                 self.queue.extendleft(reversed(reqs))
             return
         base = self.arena.buf.data_ptr() + base_off
-        # ---- descriptors and items (longest first)
-        fl = []
-        for i, (q, d) in enumerate(zip(reqs, layout)):
-            r = self.res[q.mesh_id]
-            m, info = r.mesh, r.info[OP_FWD]
-            b = q.x.shape[0]
-            ds = desc_f[i]
-            ds.N, ds.L, ds.B, ds.ldu = m.N, m.L, b, m.N
-            ds.cls, ds.G, ds.CL, ds.S = r.cls, info.G, info.CL, info.S
-            ds.layer_bytes, ds.n_items, ds.ldp, ds.n_p = info.layer_bytes, 0, 0, m.X_np
-            ds.tiles = r.ws[OP_FWD].data_ptr() + info.off_tiles
-            ds.kinds = r.ws[OP_FWD].data_ptr() + info.off_kinds
-            ds.in0, ds.out0 = base + d["x"], base + d["y"]
-            for k in range(0, b, r.cap):
-                fl.append((m.L * r.np2 * r.cap, i, k, min(k + r.cap, b), k // r.cap))
-        fl.sort(key=lambda t: -t[0])
-        it_f = (mg_batch_item * max(n_if, 1))()
-        for n, (_, i, v0, v1, part) in enumerate(fl):
-            it_f[n].mesh, it_f[n].v0, it_f[n].vend, it_f[n].part = i, v0, v1, part
-        bl = []
-        for j, i in enumerate(grads):
-            q, d = reqs[i], layout[i]
-            r = self.res[q.mesh_id]
-            m, info = r.mesh, r.info[OP_BWD]
-            b = q.x.shape[0]
-            ds = desc_b[j]
-            ds.N, ds.L, ds.B, ds.ldu = m.N, m.L, b, m.N
-            ds.cls, ds.G, ds.CL, ds.S = r.cls, info.G, info.CL, info.S
-            ds.layer_bytes, ds.n_items = info.layer_bytes, (b + r.cap - 1) // r.cap
-            ds.ldp, ds.n_p = m.N // 2 * m.X_np, m.X_np
-            ds.tiles = r.ws[OP_BWD].data_ptr() + info.off_tiles
-            ds.kinds = r.ws[OP_BWD].data_ptr() + info.off_kinds
-            ds.in0, ds.in1, ds.out0, ds.out1 = base + d["y"], base + d["gy"], None, base + d["gx"]
-            ds.dp, ds.partial = base + d["dp"], base + d["part"]
-            for k in range(0, b, r.cap):
-                bl.append((m.L * r.np2 * r.cap, j, k, min(k + r.cap, b), k // r.cap))
-        bl.sort(key=lambda t: -t[0])
-        it_b = (mg_batch_item * max(n_ib, 1))()
-        for n, (_, j, v0, v1, part) in enumerate(bl):
-            it_b[n].mesh, it_b[n].v0, it_b[n].vend, it_b[n].part = j, v0, v1, part
-        # ---- host staging: inputs + descriptors + items, then room for the outputs
-        host = torch.empty(total, dtype=torch.uint8).pin_memory()
+        host = self.pool.get(total)
         hv = host.numpy()
-        for q, d in zip(reqs, layout):
-            xb = q.x.view(np.uint8).reshape(-1)
-            hv[d["x"]: d["x"] + xb.size] = xb
-            if q.gy is not None:
-                gb = q.gy.view(np.uint8).reshape(-1)
-                hv[d["gy"]: d["gy"] + gb.size] = gb
-        for (o, st) in ((off_df, desc_f), (off_db, desc_b), (off_if, it_f), (off_ib, it_b)):
-            raw = np.frombuffer(bytes(st), dtype=np.uint8)
-            hv[o: o + raw.size] = raw
+        # ---- forward descriptors and items (longest first)
+        tf = self.t_op[OP_FWD]
+        df = np.zeros(K, _DESC)
+        df["N"], df["L"], df["B"], df["ldu"] = N, L, b, N
+        df["cls"], df["G"], df["CL"], df["S"] = self.t_cls[mid], self.t_G[mid], tf["CL"][mid], tf["S"][mid]
+        df["layer_bytes"], df["n_p"] = tf["lb"][mid], n_p
+        df["tiles"], df["kinds"] = tf["tiles"][mid], tf["kinds"][mid]
+        df["in0"], df["out0"] = base + off_x + o_x, base + off_y + o_y
+
+        def items(sel, nitems, cost):
+            ri = np.repeat(np.arange(len(sel)), nitems)
+            k = np.arange(int(nitems.sum())) - np.repeat(np.cumsum(nitems) - nitems, nitems)
+            capr, br = cap[sel][ri], b[sel][ri]
+            it = np.zeros(len(ri), _ITEM)
+            order = np.argsort(-cost[sel][ri], kind="stable")
+            it["mesh"], it["v0"] = ri[order], (k * capr)[order]
+            it["vend"], it["part"] = np.minimum((k + 1) * capr, br)[order], k[order]
+            return it
+        cost = L * np2 * cap
+        it_f = items(np.arange(K), nit, cost)
+        hv[off_df: off_df + df.nbytes] = df.view(np.uint8)
+        hv[off_if: off_if + it_f.nbytes] = it_f.view(np.uint8)
+        if KG:
+            tb = self.t_op[OP_BWD]
+            g = gidx
+            db = np.zeros(KG, _DESC)
+            db["N"], db["L"], db["B"], db["ldu"] = N[g], L[g], b[g], N[g]
+            db["cls"], db["G"], db["CL"], db["S"] = self.t_cls[mid[g]], self.t_G[mid[g]], tb["CL"][mid[g]], tb["S"][mid[g]]
+            db["layer_bytes"], db["n_items"], db["ldp"], db["n_p"] = tb["lb"][mid[g]], nit[g], N[g] // 2 * n_p[g], n_p[g]
+            db["tiles"], db["kinds"] = tb["tiles"][mid[g]], tb["kinds"][mid[g]]
+            db["in0"], db["in1"] = base + off_y + o_y[g], base + off_gy + o_gy
+            db["out1"], db["dp"], db["partial"] = base + off_gx + o_gx, base + off_dp + o_dp, base + off_pt + o_pt
+            it_b = items(g, nit[g], cost)
+            hv[off_db: off_db + db.nbytes] = db.view(np.uint8)
+            hv[off_ib: off_ib + it_b.nbytes] = it_b.view(np.uint8)
         hv[off_head: off_head + 8] = 0
+        # ---- inputs
+        for q, o in zip(reqs, o_x):
+            xb = q.x.view(np.uint8).reshape(-1)
+            hv[off_x + o: off_x + o + xb.size] = xb
+        for i, o in zip(gidx, o_gy):
+            gb = reqs[i].gy.view(np.uint8).reshape(-1)
+            hv[off_gy + o: off_gy + o + gb.size] = gb
+        # ---- result spans (host offsets = device offsets within the tick), read back on retirement
+        outs = (off_y + o_y, b * N * esz, off_dp + o_dp, dpn[gidx], off_gx + o_gx, gidx)
+        # ---- enqueue on the next stream
         stream = self.streams[self.next_stream]
         self.next_stream = (self.next_stream + 1) % len(self.streams)
         dev = self.arena.buf[base_off: base_off + total]
-        out_spans = []
         with torch.cuda.stream(stream):
-            dev.copy_(host, non_blocking=True)
+            dev[:in_bytes].copy_(host[:in_bytes], non_blocking=True)
             st = stream.cuda_stream
             head = base + off_head
-            check(lib.mg_batched_propagate(OP_FWD, base + off_df, len(reqs), base + off_if, n_if, head, self.sms,
+            check(lib.mg_batched_propagate(OP_FWD, base + off_df, K, base + off_if, n_if, head, self.sms,
                                            self.smem[OP_FWD], self.status.data_ptr(), st), "mg_batched_propagate")
-            if grads:
-                check(lib.mg_batched_propagate(OP_BWD, base + off_db, len(grads), base + off_ib, n_ib, head + 4,
+            if KG:
+                check(lib.mg_batched_propagate(OP_BWD, base + off_db, KG, base + off_ib, n_ib, head + 4,
                                                self.sms, self.smem[OP_BWD], self.status.data_ptr(), st),
                       "mg_batched_propagate")
-                check(lib.mg_batched_reduce(base + off_db, len(grads), st), "mg_batched_reduce")
-            # results back: y for every request, (dp, gx) for gradient requests
-            for q, d in zip(reqs, layout):
-                r = self.res[q.mesh_id]
-                b, N = q.x.shape
-                fe = b * N * q.x.itemsize
-                spans = [(d["y"], fe, (b, N), q.x.dtype)]
-                if q.gy is not None:
-                    dpn = r.mesh.L * (N // 2) * r.mesh.X_np * 4
-                    spans += [(d["dp"], dpn, (r.mesh.L, N // 2, r.mesh.X_np), np.float32), (d["gx"], fe, (b, N), q.x.dtype)]
-                for (o, n, _, _) in spans:
-                    host[o: o + n].copy_(dev[o: o + n], non_blocking=True)
-                out_spans.append(spans)
+                check(lib.mg_batched_reduce(base + off_db, KG, st), "mg_batched_reduce")
+            host[off_y:out_end].copy_(dev[off_y:out_end], non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(stream)
-        for q in reqs:
-            self.mzi_apps += self.res[q.mesh_id].n_mzi * q.x.shape[0] * (2 if q.gy is not None else 1)
+        self.mzi_apps += int((self.t_mzi[mid] * b * (1 + isg)).sum())
         self.ticks += 1
-        self.inflight.append(_Tick(reqs, ev, base_off, total, host, out_spans))
+        self.inflight.append(_Tick(reqs, ev, base_off, total, host, outs))
 
     def kernel_status(self) -> int:
         torch.cuda.synchronize(self.device)
