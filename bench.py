@@ -330,12 +330,10 @@ def run_ours(args, rank, world, local_rank):
     t_probe = min(timed(probe, 3))
     peak = props.multi_processor_count * 4 * 256 * iters * 64 * 2 / t_probe
 
-    # ---- reduce over ranks
-    t_max = t_step
-    if world > 1:
-        tt = torch.tensor([t_step, t_e2e], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max, t_e2e = float(tt[0]), float(tt[1])
+    # ---- reduce over ranks (replicas: the job ends with its slowest rank)
+    from meshes_gb300.replicas import max_over_ranks
+    t_max = max_over_ranks(t_step, device=dev)
+    t_e2e = max_over_ranks(t_e2e, device=dev)
     if rank != 0:
         return
     units = n_mzi * B * world
