@@ -59,6 +59,7 @@ extern "C" {
  * heuristic; the autotuner (meshes_gb300/autotune.py) measures and stores better choices. */
 typedef struct mg_config {
   int M, V, W, CL, S;
+  int split;   /* 0: automatic, 1: two CTA kinds per SM (V and V-1 vectors per lane group), 2: uniform CTAs */
 } mg_config;
 
 /* ---- library ---------------------------------------------------------------------------- */
@@ -155,6 +156,7 @@ int mg_propagate(int op, int N, int L, int B, int crossing, int geometry, const 
 /* Plan of one launch (for hosts that manage tiles themselves, e.g. the batched engine). */
 typedef struct mg_plan_info {
   int M, V, W, CL, S, G, grid;
+  int nA;   /* split launch: CTAs holding V vectors per lane group (the other grid - nA hold V-1); 0 if uniform */
   unsigned layer_bytes, dlayer_bytes;
   size_t smem, off_kinds, off_tiles, off_dtiles, off_partial, total;
 } mg_plan_info;

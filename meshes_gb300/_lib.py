@@ -25,15 +25,15 @@ class MeshLibraryError(RuntimeError):
 
 
 class mg_config(Structure):
-    _fields_ = [("M", c_int), ("V", c_int), ("W", c_int), ("CL", c_int), ("S", c_int)]
+    _fields_ = [("M", c_int), ("V", c_int), ("W", c_int), ("CL", c_int), ("S", c_int), ("split", c_int)]
 
     def as_tuple(self):
-        return (self.M, self.V, self.W, self.CL, self.S)
+        return (self.M, self.V, self.W, self.CL, self.S, self.split)
 
 
 class mg_plan_info(Structure):
     _fields_ = [("M", c_int), ("V", c_int), ("W", c_int), ("CL", c_int), ("S", c_int), ("G", c_int),
-                ("grid", c_int), ("layer_bytes", c_uint), ("dlayer_bytes", c_uint), ("smem", c_size_t),
+                ("grid", c_int), ("nA", c_int), ("layer_bytes", c_uint), ("dlayer_bytes", c_uint), ("smem", c_size_t),
                 ("off_kinds", c_size_t), ("off_tiles", c_size_t), ("off_dtiles", c_size_t),
                 ("off_partial", c_size_t), ("total", c_size_t)]
 
@@ -132,8 +132,8 @@ def check(rc: int, what: str):
         raise MeshLibraryError("%s failed (rc=%d): %s" % (what, rc, last_error()))
 
 
-def config(M=0, V=0, W=0, CL=0, S=0):
-    return mg_config(M, V, W, CL, S)
+def config(M=0, V=0, W=0, CL=0, S=0, split=0):
+    return mg_config(M, V, W, CL, S, split)
 
 
 def cfg_ptr(cfg):

@@ -3,7 +3,8 @@
 For a shape (op, crossing, geometry, N, L, B) it times the valid candidates on the GPU - tiles built
 once, CUDA events on the launch stream, L2 flushed between repetitions - in two stages: the register
 blocking and CTA width (modes per lane M, vectors per lane V, warps per CTA W), then, around the
-winner, layers per pipeline stage CL and stages S - and keeps the fastest.
+winner, layers per pipeline stage CL, stages S and (forward) the split launch - and keeps the
+fastest.
 Results live in ``tuned_configs.json`` next to this file (keyed by op/crossing/geometry/N and a batch
 range) and are loaded into the library's tuning table by ``load_table()`` (called on import of the
 package), so every call that passes no explicit configuration - the reference-shaped entry points
@@ -56,13 +57,17 @@ def candidates(op: int, N: int, real: bool) -> List[Tuple[int, ...]]:
     Np = 1 << max(1, (N - 1).bit_length())
     Ms = [m for m in (2, 4, 8, 16) if m <= Np and Np // m <= 32]
     Vs = {OP_FWD: (2, 4, 8), OP_FWDDIFF: (1, 2, 4), OP_BWD: (1, 2, 4)}[op]
-    return [(M, V, W, 0, 0) for M, V, W in itertools.product(Ms, Vs, (2, 4, 8))]
+    return [(M, V, W, 0, 0, 2) for M, V, W in itertools.product(Ms, Vs, (2, 4, 8))]
 
 
-def refinements(c: Tuple[int, ...]) -> List[Tuple[int, ...]]:
-    """Stage 2 around a stage-1 winner: layers per pipeline stage CL and stages S."""
+def refinements(c: Tuple[int, ...], op: int = OP_FWD) -> List[Tuple[int, ...]]:
+    """Stage 2 around a stage-1 winner: layers per pipeline stage CL and stages S; for forward
+    propagation also the split launch (two 4-warp CTAs per SM with V and V-1 vectors per lane group)."""
     M, V, W = c[:3]
-    return [(M, V, W, CL, S) for CL, S in itertools.product((0, 4, 8, 16), (2, 3))]
+    out = [(M, V, W, CL, S, 2) for CL, S in itertools.product((0, 4, 8, 16), (2, 3))]
+    if op == OP_FWD and V >= 2:
+        out += [(M, V, 4, CL, S, 1) for CL, S in itertools.product((0, 4, 6, 8, 12), (2, 3))]
+    return out
 
 
 def tune(op: int, N: int, L: int, B: int, crossing: int = 0, geometry: int = 0, reps: int = 5,
@@ -131,7 +136,7 @@ def tune(op: int, N: int, L: int, B: int, crossing: int = 0, geometry: int = 0, 
     for c in (cands or candidates(op, N, real)):
         measure(c)
     if not cands and results:
-        for c in refinements(min(results, key=results.get)):
+        for c in refinements(min(results, key=results.get), op):
             if c not in results:
                 measure(c)
     best = min(results, key=results.get)
@@ -168,7 +173,7 @@ def main():
     op = OPS[a.op]
     best, res = tune(op, a.N, L, a.B, CROSS[a.crossing], geo)
     for c, ms in sorted(res.items(), key=lambda kv: kv[1])[:8]:
-        print("M=%d V=%d W=%d CL=%d S=%d  %.4f ms" % (tuple(c) + (ms,)))
+        print("M=%d V=%d W=%d CL=%d S=%d split=%d  %.4f ms" % (tuple(c) + (0,) * (6 - len(c)) + (ms,)))
     if a.write:
         rng = tuple(a.B_range) if a.B_range else (a.B // 2 + 1, a.B * 2)
         record(op, CROSS[a.crossing], geo, a.N, rng, best, res[best])

@@ -57,7 +57,7 @@ class _MeshState:
         self.cls = kernel_class(mesh)
         M, V = _CLS_MV[self.cls]
         self.M, self.V = M, V
-        self.cfg = {op: _lib.config(M, V, WARPS, 0, 0) for op in (OP_FWD, OP_BWD)}
+        self.cfg = {op: _lib.config(M, V, WARPS, 0, 0, 2) for op in (OP_FWD, OP_BWD)}
         self.info = {op: plan(op, mesh.N, mesh.L, max(self.B, 1), mesh.crossing, mesh.geometry, self.cfg[op])
                      for op in (OP_FWD, OP_BWD)}
         self.ws = {}

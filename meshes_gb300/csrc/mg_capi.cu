@@ -56,6 +56,7 @@ size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 struct DevInfo {
   int sms = 0;
   int smem_optin = 0;
+  int smem_per_sm = 0;
 };
 DevInfo dev_info() {
   static std::mutex mu;
@@ -67,8 +68,10 @@ DevInfo dev_info() {
   if (d.sms == 0) {
     cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&d.smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&d.smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     if (d.sms <= 0) d.sms = 152;
     if (d.smem_optin <= 0) d.smem_optin = 227 * 1024;
+    if (d.smem_per_sm <= 0) d.smem_per_sm = 228 * 1024;
   }
   return d;
 }
@@ -102,6 +105,8 @@ struct Plan {
   bool real;
   int gr;
   int M, V, W, CL, S, G, logG, R, np2, grid;
+  bool split;   // two CTA kinds per SM (V and V-1 vectors per lane group), CTAs [0, nA) the first kind
+  int nA;
   unsigned lb, dlb;
   size_t smem;
   size_t off_kinds, off_tiles, off_dtiles, off_partial, total;
@@ -155,6 +160,21 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   if (stored ? !instantiated_stored(OP_BWD, M, V) : !instantiated(op, M, V))
     return fail(MG_E_CONFIG, "no kernel instantiated for op=%d M=%d V=%d", stored ? MG_OP_BWD_STORED : op, M, V);
   p.M = M; p.V = V; p.G = G; p.logG = ilog2(G); p.R = 32 / G; p.np2 = G * M / 2;
+  // split launch: when one wave of uniform CTAs cannot cover the SMs evenly (B between SMs x 4 warps x V
+  // and SMs x 4 warps x (2V-1) vectors), run two 4-warp CTAs per SM holding V and V-1 vectors per lane
+  // group.  split: 0 auto, 1 on, 2 off.  Automatic for forward propagation only: measured on GB300 at
+  // N=256, B=4096 it saves 5% there, while back-propagation loses more than it gains (every CTA reduces
+  // the gradient of every slot, so twice the CTAs is twice that work and twice the partials).
+  const int split_mode = cfg ? cfg->split : 0;
+  p.split = false;
+  p.nA = 0;
+  if (split_mode != 2 && (op == OP_FWD || op == OP_BWD) && V >= 2 && !stored &&
+      split_instantiated(op, crossing == CR_ORTH, M, V, G == 32, p.gr)) {
+    const long ws = (cfg && cfg->W) ? cfg->W : 4;
+    const long capA = ws * p.R * V, capB = ws * p.R * (V - 1);
+    p.split = split_mode == 1 ||
+              (op == OP_FWD && (long)di.sms * capA < B && B <= (long)di.sms * (capA + capB));
+  }
   const unsigned tslot = p.real ? 16 : 32;               // bytes per slot of a T tile
   // layer tiles are copied by bulk TMA: every size and offset must be a multiple of 16 bytes
   p.lb = (unsigned)align16((size_t)p.np2 * tslot * (op == OP_FWDDIFF ? 2 : 1) + (p.gr == 1 ? (size_t)p.np2 * 8 : 0));
@@ -162,7 +182,7 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   const int gslot = (op != OP_BWD) ? 0 : ((p.gr == 1 || p.gr == 2) ? 8 : (p.real ? 16 : 32));
   const size_t gstl = (size_t)p.np2 * gslot;
   const int maxw = prop_max_threads(op, M, V) / 32;
-  int W = (cfg && cfg->W) ? cfg->W : 0;
+  int W = (cfg && cfg->W) ? cfg->W : (p.split ? 4 : 0);
   if (!W) {
     // enough warps to cover the batch in one wave, rounded up to a multiple of 4 so the four
     // schedulers of an SM carry equal work (measured: 8 warps on 128 SMs beat 7 warps on 147)
@@ -173,14 +193,16 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
     W = (int)std::min<long>(w, std::min(8, maxw));
   }
   if (W < 1 || W > maxw) return fail(MG_E_CONFIG, "W=%d warps outside [1, %d]", W, maxw);
-  int S = (cfg && cfg->S) ? cfg->S : (op == OP_FWD ? 2 : 3);
+  int S = (cfg && cfg->S) ? cfg->S : ((op == OP_FWD || p.split) ? 2 : 3);
   if (S < 1 || S > 8) return fail(MG_E_CONFIG, "S=%d stages outside [1, 8]", S);
-  const size_t budget = (size_t)di.smem_optin - 1024;
+  // a split launch keeps two CTAs resident per SM (each also pays the 1 KB the SM reserves per CTA)
+  const size_t budget = p.split ? (size_t)di.smem_per_sm / 2 - 1024 : (size_t)di.smem_optin - 1024;
   int CL = (cfg && cfg->CL) ? cfg->CL : 0;
   const size_t per_layer = (size_t)S * p.lb + p.dlb + W * gstl;
   const size_t fixed = 8 * (size_t)(S + 1) + (L <= kMaxSmemKinds ? 4 * (size_t)L : 0);
   if (!CL) {
-    const size_t target = (op == OP_BWD) ? budget : std::min<size_t>(budget, 160 * 1024);
+    // forward: deep enough to hide the copies, shallow enough to start soon (split CTAs: about 68 KB measured best)
+    const size_t target = (op == OP_BWD) ? budget : std::min<size_t>(budget, (p.split ? 68 : 160) * 1024);
     CL = (int)std::max<size_t>(1, std::min<size_t>(16, (target > fixed ? target - fixed : 0) / per_layer));
     if (L > 0) CL = std::min(CL, L);
   }
@@ -195,6 +217,13 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
     return fail(MG_E_CONFIG, "one pipeline stage exceeds the 1 MB bulk-copy limit");
   const long per_cta = (long)W * p.R * V;
   p.grid = (int)((B + per_cta - 1) / per_cta);
+  if (p.split) {
+    const long capB = (long)W * p.R * (V - 1);
+    const long nA = std::min<long>(di.sms, (B + per_cta - 1) / per_cta);
+    const long rem = std::max<long>(0, (long)B - nA * per_cta);
+    p.nA = (int)nA;
+    p.grid = (int)(nA + (rem + capB - 1) / capB);
+  }
   p.off_kinds = 256;
   p.off_tiles = p.off_kinds + align256((size_t)std::max(L, 1) * 12);   // kinds + (shift, len)
   p.off_dtiles = p.off_tiles + align256((size_t)L * p.lb);
@@ -276,7 +305,9 @@ int run_prop(const Plan& P, const void* in0, const void* in1, void* out0, void* 
   lc.smem = P.smem;
   lc.stream = st;
   cudaError_t e;
-  e = launch_prop(P.op, P.real, P.M, P.V, P.G == 32, P.gr, lc, a);
+  a.nA = P.nA;
+  e = P.split ? launch_prop_split(P.op, P.real, P.M, P.V, P.G == 32, P.gr, lc, a)
+              : launch_prop(P.op, P.real, P.M, P.V, P.G == 32, P.gr, lc, a);
   if (e != cudaSuccess) return cuda_fail(e, "prop_kernel launch");
   if (P.op == OP_BWD && dp && P.L > 0) {
     const int n = P.L * P.np2;
@@ -502,12 +533,13 @@ int mg_propagate(int op, int N, int L, int B, int crossing, int geometry, const 
     Plan Pb, Pf;
     TRY(make_plan(OP_BWD, N, L, B, crossing, geometry, cfg, &Pb));
     TRY(check_ws(Pb, ws, wsb));
-    mg_config cf = {Pb.M, 0, 0, 0, 0};
+    mg_config cf = {Pb.M, 0, 0, 0, 0, cfg ? cfg->split : 0};
     TRY(make_plan(OP_FWD, N, L, B, crossing, geometry, &cf, &Pf));
     Pf.lb = Pb.lb;
     Pf.off_kinds = Pb.off_kinds;
     Pf.off_tiles = Pb.off_tiles;
-    const size_t budget = (size_t)dev_info().smem_optin - 1024;
+    const DevInfo di = dev_info();
+    const size_t budget = Pf.split ? (size_t)di.smem_per_sm / 2 - 1024 : (size_t)di.smem_optin - 1024;
     for (;;) {
       Pf.smem = prop_smem_bytes(OP_FWD, 0, Pf.M, Pf.G, Pf.W, Pf.CL, Pf.S, Pf.lb, 0, L);
       if (Pf.smem <= budget && (size_t)Pf.CL * Pf.lb < (1u << 20)) break;
@@ -560,6 +592,7 @@ int mg_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_co
   TRY(make_plan(op, N, L, B, crossing, geometry, cfg, &P));
   if (out) {
     out->M = P.M; out->V = P.V; out->W = P.W; out->CL = P.CL; out->S = P.S; out->G = P.G; out->grid = P.grid;
+    out->nA = P.split ? P.nA : 0;
     out->layer_bytes = P.lb; out->dlayer_bytes = P.dlb; out->smem = P.smem;
     out->off_kinds = P.off_kinds; out->off_tiles = P.off_tiles; out->off_dtiles = P.off_dtiles;
     out->off_partial = P.off_partial; out->total = P.total;
@@ -590,6 +623,10 @@ int mg_propagate_range(int op, int N, int L, int l0, int l1, int B, int crossing
   g_err.clear();
   if (op != OP_FWD && op != MG_OP_BWD_STORED) return fail(MG_E_ARG, "op %d not in {MG_OP_FWD, MG_OP_BWD_STORED}", op);
   if (l0 < 0 || l1 < l0 || l1 > L) return fail(MG_E_ARG, "layer range [%d, %d) outside [0, %d)", l0, l1, L);
+  // layer ranges run uniform CTAs (the stored-activation kernels have no split form)
+  mg_config cu = cfg ? *cfg : mg_config{0, 0, 0, 0, 0, 0};
+  cu.split = 2;
+  cfg = &cu;
   Plan P;
   TRY(make_plan(op, N, L, B, crossing, geometry, cfg, &P));
   TRY(check_ws(P, ws, wsb));
@@ -650,6 +687,7 @@ int mg_propagate_range(int op, int N, int L, int l0, int l1, int B, int crossing
   a.status = reinterpret_cast<int*>(w);
   a.act = act;
   a.act_plane = (size_t)B * ldu;
+  a.nA = 0;
   LaunchCfg lc;
   lc.grid = dim3(P.grid);
   lc.block = dim3(32 * P.W);

@@ -47,6 +47,16 @@ inline cudaError_t launch_one(const LaunchCfg& lc, const PropArgs& a) {
   return cudaGetLastError();
 }
 
+template <int OP, int M, int V, bool REAL, int GT, int GR>
+inline cudaError_t launch_split(const LaunchCfg& lc, const PropArgs& a) {
+  static std::atomic<unsigned long long> done{0};
+  auto k = prop_split_kernel<OP, M, V, REAL, GT, GR>;
+  cudaError_t e = ensure_smem_attr(k, done);
+  if (e != cudaSuccess) return e;
+  k<<<lc.grid, lc.block, lc.smem, lc.stream>>>(a);
+  return cudaGetLastError();
+}
+
 // max threads per CTA the instantiation was compiled for
 inline int prop_max_threads(int op, int M, int V) {
   return ((op == OP_FWD && M * V <= 16) || (op == OP_BWD && M * V <= 8)) ? 512 : 256;
@@ -59,5 +69,10 @@ int set_last_error(int code, const char* fmt, ...);
 // full: a vector fills the warp (G = 32), selecting the compile-time-G instantiation;
 // gr: back-propagation gradient mode (0 dJ/dT + dT/dp tiles, 1 MZI direct, 2 orth direct)
 cudaError_t launch_prop(int op, bool real, int M, int V, bool full, int gr, const LaunchCfg& lc, const PropArgs& a);
+// split launches (two CTA kinds per SM); instantiated only for the full-warp configurations in
+// split_instantiated()
+bool split_instantiated(int op, bool real, int M, int V, bool full, int gr);
+cudaError_t launch_prop_split(int op, bool real, int M, int V, bool full, int gr, const LaunchCfg& lc,
+                              const PropArgs& a);
 
 }  // namespace mg

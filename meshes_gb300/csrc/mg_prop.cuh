@@ -58,6 +58,7 @@ struct PropArgs {
   const void* target;            // BWD: when set, dJ/du_out* = 2 (u_out - target) replaces in1
   void* act;                     // GR 4: per-layer inputs [L][act_plane] (FWD writes them, BWD reads them)
   size_t act_plane;              // elements between the stored inputs of consecutive layers
+  int nA;                        // split launch: CTAs [0, nA) hold V vectors per lane group, the rest V-1
 };
 
 template <bool REAL> struct Fld { using T = float2; using C = C2x2; };
@@ -770,6 +771,29 @@ prop_kernel(const PropArgs a0) {
   a.vend = a.B;
   if (OP == OP_BWD) a.partial = a0.partial + (size_t)blockIdx.x * a.L * ((G * M) >> 1) * (GR == 4 ? 4 : 1);
   prop_body<OP, M, V, REAL, GT, GR>(a, smem);
+}
+
+// Split launch for a batch that one wave of full CTAs cannot spread evenly: two CTAs per SM, the first
+// nA CTAs with V vectors per lane group, the others with V-1, so that each SM scheduler carries one
+// warp of each kind (2V-1 vectors) instead of two full warps on some SMs and none on others.  The two
+// bodies are separate code paths chosen once per CTA.
+template <int OP, int M, int V, bool REAL, int GT, int GR>
+__global__ void __launch_bounds__(PropTraits<OP, M, V, REAL>::kMaxThreads, 1)
+prop_split_kernel(const PropArgs a0) {
+  static_assert(V >= 2, "a split launch needs V >= 2");
+  extern __shared__ __align__(128) unsigned char smem[];
+  PropArgs a = a0;
+  const int G = GT ? GT : a.G;
+  const int groups = a.W * (32 / G);
+  a.vend = a.B;
+  if (OP == OP_BWD) a.partial = a0.partial + (size_t)blockIdx.x * a.L * ((G * M) >> 1) * (GR == 4 ? 4 : 1);
+  if ((int)blockIdx.x < a.nA) {
+    a.v0 = blockIdx.x * groups * V;
+    prop_body<OP, M, V, REAL, GT, GR>(a, smem);
+  } else {
+    a.v0 = a.nA * groups * V + (blockIdx.x - a.nA) * groups * (V - 1);
+    prop_body<OP, M, V - 1, REAL, GT, GR>(a, smem);
+  }
 }
 
 }  // namespace mg

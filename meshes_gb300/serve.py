@@ -194,7 +194,7 @@ class MeshServer:
     def _program(self, m: MeshNetworkGPU) -> _Resident:
         cls = kernel_class(m)
         M, V = _CLS_MV[cls]
-        cfg = {op: _lib.config(M, V, WARPS, 0, 0) for op in (OP_FWD, OP_BWD)}
+        cfg = {op: _lib.config(M, V, WARPS, 0, 0, 2) for op in (OP_FWD, OP_BWD)}
         info = {op: plan(op, m.N, m.L, 1, m.crossing, m.geometry, cfg[op]) for op in (OP_FWD, OP_BWD)}
         ws = {}
         st = torch.cuda.current_stream(m.device).cuda_stream

@@ -342,3 +342,55 @@ def test_random_phase_screen(pos, geo, N, B):
     acc = torch.ones(p_full.size, dtype=torch.float32, device="cuda")
     m.grad_phi(to_dev(x), lambda yy: 2 * (yy - tt), out_dp=acc)
     assert O.rel_err(acc.cpu().numpy() - 1.0, dp) < 1e-6
+
+
+@pytest.mark.parametrize("cr,N,B", [("mzi", 256, 4096), ("mzi", 256, 2500), ("mzi", 512, 3000), ("orth", 256, 3000)])
+def test_split_launch_parity(cr, N, B):
+    """Split launches (two CTA kinds per SM, V and V-1 vectors per lane group) against the oracle, forward
+    and back-propagation, and bit-identical to themselves on a second run."""
+    from meshes_gb300 import _lib
+    import ctypes
+    lib = _lib.load()
+    rng = np.random.default_rng(N * 7 + B)
+    om = O.random_mesh(rng, N, "clements", cr, 0.02 if cr == "mzi" else 0.0)
+    real = cr == "orth"
+    x = O.unit_columns(rng, N, B, real=real)
+    g = O.unit_columns(rng, N, B, real=real)
+    m = gpu_mesh(om)
+    dt = torch.float32 if real else torch.complex64
+    xd, gd = torch.tensor(x, dtype=dt, device="cuda"), torch.tensor(g, dtype=dt, device="cuda")
+    y, gx = torch.empty_like(xd), torch.empty_like(xd)
+    dp = torch.empty(m.p_phase.numel(), device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    s = m.p_splitter
+    ldp, lds = N // 2 * m.X_np, N // 2 * m.X_ns
+    outs = []
+    for op in (0, 2):
+        cfg = _lib.config(split=1)
+        info = _lib.mg_plan_info()
+        assert lib.mg_plan(op, N, om.L, B, m.crossing, 0, _lib.cfg_ptr(cfg), ctypes.byref(info)) == 0
+        assert info.nA > 0 and info.grid > info.nA                # really split
+        nb = info.total
+        ws = torch.zeros(nb, dtype=torch.uint8, device="cuda")
+        assert lib.mg_build_tiles(op, N, om.L, 0, m.lens.data_ptr(), m.shifts.data_ptr(), None, m.crossing,
+                                  m.p_phase.data_ptr(), ldp, s.data_ptr() if s.numel() else None, lds, None, None,
+                                  None, B, _lib.cfg_ptr(cfg), ws.data_ptr(), nb, st) == 0, _lib.last_error()
+        for rep in range(2):
+            if op == 0:
+                assert lib.mg_propagate(0, N, om.L, B, m.crossing, 0, xd.data_ptr(), None, y.data_ptr(), None, N,
+                                        None, 0, 0, _lib.cfg_ptr(cfg), ws.data_ptr(), nb, st) == 0, _lib.last_error()
+                outs.append(y.clone())
+            else:
+                assert lib.mg_propagate(2, N, om.L, B, m.crossing, 0, y.data_ptr(), gd.data_ptr(), None,
+                                        gx.data_ptr(), N, dp.data_ptr(), ldp, 0, _lib.cfg_ptr(cfg), ws.data_ptr(),
+                                        nb, st) == 0, _lib.last_error()
+                outs.append((gx.clone(), dp.clone()))
+        assert lib.mg_read_status(ws.data_ptr(), 0, st) == 0
+    assert torch.equal(outs[0], outs[1])
+    assert torch.equal(outs[2][0], outs[3][0]) and torch.equal(outs[2][1], outs[3][1])
+    y_ref = O.propagate(om, x)
+    G, _, gin = O.vjp_unitary(om, y_ref, g)
+    n_p = O.CROSSINGS[cr][0]
+    assert O.rel_err(outs[0].cpu().numpy(), y_ref) < TOL
+    assert O.rel_err(outs[2][0].cpu().numpy(), gin) < TOL
+    assert O.rel_err(outs[2][1].cpu().numpy().reshape(om.L, N // 2, n_p), O.contract_dp(om, G)) < TOL
