@@ -404,7 +404,7 @@ def run_batched(args):
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     st = torch.cuda.current_stream().cuda_stream
-    prob = make_batched_problem()
+    prob = make_batched_problem(n_meshes=args.meshes)
     meshes, bufs = [], []
     for d in prob:
         m = MeshNetworkGPU(d["N"], d["L"], d["lens"], d["shifts"], d["p"].reshape(-1), d["s"], d["cr"],
@@ -440,6 +440,12 @@ def run_batched(args):
     for stt, b in zip(bm.states, bufs):
         stt.x.copy_(b["x"])
         stt.gy.copy_(b["g"])
+    if args.profile:
+        # two untimed steps (forward + back-propagation launches) for ncu captures of batched_kernel
+        bm.step(True)
+        bm.step(True)
+        print(json.dumps({"profile_steps": 2, "meshes": len(prob), "items": bm.n_items, "status": bm.check_status()}))
+        return
     g_f = BatchedMeshes.capture(bm, backward=False)
     bm2 = bm
     g_fb = torch.cuda.CUDAGraph()
@@ -469,7 +475,7 @@ def run_batched(args):
     line = {"metric": "MZI-apps/s (batched uneven meshes, fwd+bwd)", "value": units / t_bat_fb, "unit": "MZI-apps/s",
             "n_gpus": 1, "steps": k, "warmup": args.warmup, "ms_per_step": t_bat_fb * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64/f32", "data": "synthetic (seeded)",
-            "config": {"workload": "batched_512_meshes_clements_reck_orth_N8-256_B1-2048", "meshes": len(prob),
+            "config": {"workload": "batched_%d_meshes_clements_reck_orth_N8-256_B1-2048" % len(prob), "meshes": len(prob),
                        "mzi_apps_per_pass": units, "items": bm.n_items, "graph": True},
             "batched": {"fwd_mzi_per_s": units / t_bat_f, "fwdbwd_mzi_per_s": units / t_bat_fb,
                         "fwd_ms": t_bat_f * 1e3, "fwdbwd_ms": t_bat_fb * 1e3},
@@ -527,6 +533,7 @@ def run_serve(args):
     for i in range(64):
         srv.submit(i, pools[i][:4]).result(60)
     futs = []
+    t_submit = 0.0
     t0 = time.perf_counter()
     k = 0
     while k < n_req:
@@ -534,7 +541,9 @@ def run_serve(args):
         while k < n_req and arrivals[k] <= now:
             i, b = int(mesh_ids[k]), int(bsz[k])
             x = pools[i][:b]
+            ts0 = time.perf_counter()
             f = srv.submit(i, x, gy=x if grad[k] else None)
+            t_submit += time.perf_counter() - ts0
             futs.append((k, f))
             k += 1
         time.sleep(20e-6)
@@ -553,6 +562,8 @@ def run_serve(args):
                        "duration_s": duration, "requests": len(futs), "grad_fraction": float(grad.mean())},
             "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
             "throughput_mzi_apps_per_s": apps / span, "served_req_per_s": len(futs) / span, "ticks": srv.ticks,
+            "host_us_per_request": {k: 1e6 * v / max(srv.completed, 1) for k, v in srv.host_s.items()},
+            "client_us_per_submit": 1e6 * t_submit / max(len(futs), 1),
             "status": srv.kernel_status()}
     print(json.dumps(line))
 
@@ -568,6 +579,7 @@ def main():
                     help="clements256: the headline fwd+bwd step; batched: 512 uneven meshes, plain vs "
                          "persistent; serve: Poisson request stream on 64 resident meshes")
     ap.add_argument("--duration", type=float, default=10.0, help="serve workload: seconds of traffic")
+    ap.add_argument("--meshes", type=int, default=512, help="batched workload: number of meshes")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

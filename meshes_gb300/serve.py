@@ -59,6 +59,8 @@ class _Resident:
     info: dict
     ws: dict
     n_mzi: int
+    dp_bytes: int = 0        # aligned bytes of dJ/dp
+    part_bytes: int = 0      # gradient-partial bytes of one work item
 
 
 @dataclass
@@ -167,6 +169,7 @@ class MeshServer:
         self.completed = 0
         self.mzi_apps = 0
         self.ticks = 0
+        self.host_s = {"pack": 0.0, "retire": 0.0}       # scheduler-thread time spent packing and retiring
         self.error: Optional[BaseException] = None
         self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.pool = _PinnedPool()
@@ -209,7 +212,9 @@ class MeshServer:
                                           ws[op].numel(), st), "mg_build_tiles")
         G = info[OP_FWD].G
         n_mzi = sum(m.lens_h) if m.strides is None else m.L * (m.N // 2)
-        return _Resident(m, cls, M, V, G, WARPS * (32 // G) * V, G * M // 2, info, ws, n_mzi)
+        np2 = G * M // 2
+        return _Resident(m, cls, M, V, G, WARPS * (32 // G) * V, np2, info, ws, n_mzi,
+                         _align(m.L * (m.N // 2) * m.X_np * 4), m.L * np2 * 8)
 
     # ---- client side
     def submit(self, mesh_id: int, x, gy=None) -> Future:
@@ -237,15 +242,12 @@ class MeshServer:
 
     def _request_bytes(self, req: Request) -> int:
         r = self.res[req.mesh_id]
-        b, N = req.x.shape
-        e = req.x.itemsize
-        n = 2 * _align(b * N * e)                           # x, y
-        if req.gy is not None:
-            n_items = (b + r.cap - 1) // r.cap
-            n += 2 * _align(b * N * e)                      # gy, gx
-            n += _align(r.mesh.L * (N // 2) * r.mesh.X_np * 4)               # dp
-            n += _align(n_items * r.mesh.L * r.np2 * 8)     # partials
-        return n
+        b = req.x.shape[0]
+        fe = _align(req.x.nbytes)
+        if req.gy is None:
+            return 2 * fe                                   # x, y
+        # x, y, gy, gx, dJ/dp and the gradient partials of its work items
+        return 4 * fe + r.dp_bytes + _align((b + r.cap - 1) // r.cap * r.part_bytes)
 
     # ---- scheduler
     def start(self):
@@ -277,7 +279,10 @@ class MeshServer:
         try:
             torch.cuda.set_device(self.device)
             while self.running:
+                t0 = time.perf_counter()
                 progressed = self._retire()
+                if progressed:
+                    self.host_s["retire"] += time.perf_counter() - t0
                 progressed |= self._launch_tick()
                 if not progressed:
                     time.sleep(self.idle_sleep)
@@ -325,19 +330,22 @@ class MeshServer:
             if not self.queue:
                 return False
             batch, need = [], 0
+            room = self.arena.largest() - 65536            # the tick's descriptors and items get 64 KB + 2 KB/request
             while self.queue and len(batch) < self.max_per_tick:
                 req = self.queue[0]
                 if req.future.cancelled():
                     self.queue.popleft()
                     continue
                 n = need + req.nbytes
-                if n + 65536 + 64 * (len(batch) + 1) * 32 > self.arena.largest():
+                if n + 2048 * (len(batch) + 1) > room:
                     break                                   # no memory now: wait for ticks to retire
                 batch.append(self.queue.popleft())
                 need = n
         if not batch:
             return False
+        t0 = time.perf_counter()
         self._run(batch)
+        self.host_s["pack"] += time.perf_counter() - t0
         return True
 
     def _run(self, reqs: List[Request]):
