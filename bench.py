@@ -152,8 +152,20 @@ def cpu_baseline(problem, seconds=10.0):
         if time.perf_counter() - t0 > seconds and reps >= 2:
             break
     rate = n_mzi * bs * reps / work
+    # the same in complex128 (the reference's own precision for dot / dot_vjp), a shorter sample
+    a = time.perf_counter()
+    reps128 = 0
+    while True:
+        y = P.forward(fns, om, xs, threads=threads, dtype=np.complex128)
+        P.vjp(fns, om, y, 2 * (y - ts), threads=threads, dtype=np.complex128)
+        reps128 += 1
+        if time.perf_counter() - a > seconds / 4 and reps128 >= 2:
+            break
+    rate128 = n_mzi * bs * reps128 / (time.perf_counter() - a)
     return {"value": rate, "unit": "MZI-apps/s", "cores": threads, "kind": "port",
-            "sample": "%d of the %d vectors, fwd (mode 0) + bwd (mode 2), %d repeats, %.1f s" % (bs, B, reps, work)}
+            "sample": "%d of the %d vectors, fwd (mode 0) + bwd (mode 2), complex64, %d repeats, %.1f s"
+                      % (bs, B, reps, work),
+            "value_complex128": rate128}
 
 
 def traffic_from_profiles(name: str):
@@ -394,6 +406,104 @@ def make_batched_problem(seed=1003, n_meshes=512):
     return out
 
 
+def run_c1(args):
+    """Plain forward propagation, Clements mzi N=64 L=64 (2016 MZIs), ideal splitters, B=1024 unit-norm
+    complex64 columns, through the reference-shaped entry point mg_fwdprop; with the unitarity error
+    ||U U^H - I||_F of the programmed mesh."""
+    import torch
+    from meshes_gb300 import MeshNetworkGPU
+    from meshes_gb300 import geometry as gm
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(1000)
+    Nc, Bc = 64, 1024
+    lens, shifts = gm.clements(Nc)
+    mask = gm.active_mask_nn(Nc, lens, shifts)
+    p = rng.uniform(0, 2 * np.pi, (len(lens), Nc // 2, 2)).astype(np.float32)
+    p[~mask] = 0
+    m = MeshNetworkGPU(Nc, len(lens), lens, shifts, p.reshape(-1), None, "mzi", is_phase=False, device=dev)
+    x = rng.standard_normal((Bc, Nc)) + 1j * rng.standard_normal((Bc, Nc))
+    x = torch.from_numpy((x / np.linalg.norm(x, axis=1, keepdims=True)).astype(np.complex64)).to(dev).t()
+    out = torch.empty_like(x)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(max(3, args.warmup)):
+        m.dot(x, out=out)
+    ts = []
+    for _ in range(max(5, min(args.steps, 200))):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        m.dot(x, out=out)
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e-3)
+    t = statistics.median(ts)
+    U = m.matrix().t().to(torch.complex128)
+    unit_err = float(torch.linalg.norm(U @ U.conj().t() - torch.eye(Nc, dtype=torch.complex128, device=dev)))
+    n_mzi = int(mask.sum())
+    print(json.dumps({"metric": "MZI-apps/s (fwd)", "value": n_mzi * Bc / t, "unit": "MZI-apps/s", "n_gpus": 1,
+                      "steps": len(ts), "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+                      "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded)",
+                      "config": {"workload": "clements_mzi_N64_L64_B1024_fwd", "n_mzi": n_mzi,
+                                 "l2": "flushed between timed calls"},
+                      "unitarity_error": unit_err, "status": m.status()}))
+
+
+def run_c4(args):
+    """Unitary fitting: Clements mzi N=128 L=128 with splitting errors N(0, 0.02), target a Haar-random
+    unitary (QR of a complex Gaussian with the R-diagonal phase fix), x = I, J = ||U - U_t||_F^2,
+    2000 Adam steps (lr 1e-2) on theta, phi through the autograd function; steps/s and the fidelity
+    |tr(U^H U_t)|^2 / N^2 reached."""
+    import torch
+    from meshes_gb300 import MeshNetworkGPU
+    from meshes_gb300 import geometry as gm
+    from meshes_gb300.autograd import mesh_apply
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(1004)
+    Nc = 128
+    lens, shifts = gm.clements(Nc)
+    mask = gm.active_mask_nn(Nc, lens, shifts)
+    p0 = rng.uniform(0, 2 * np.pi, (len(lens), Nc // 2, 2)).astype(np.float32)
+    s0 = rng.normal(0, 0.02, (len(lens), Nc // 2, 2)).astype(np.float32)
+    p0[~mask] = 0
+    s0[~mask] = 0
+    m = MeshNetworkGPU(Nc, len(lens), lens, shifts, p0.reshape(-1), s0, "mzi", is_phase=False, device=dev)
+    Z = (rng.standard_normal((Nc, Nc)) + 1j * rng.standard_normal((Nc, Nc))) / np.sqrt(2)
+    Q, R = np.linalg.qr(Z)
+    Ut = (Q * (np.diag(R) / np.abs(np.diag(R)))[None, :]).astype(np.complex64)
+    x = torch.eye(Nc, dtype=torch.complex64, device=dev)
+    target = torch.tensor(Ut.T, device=dev)
+    p = torch.tensor(p0, device=dev, requires_grad=True)
+    opt = torch.optim.Adam([p], lr=1e-2)
+    n_steps = 2000
+
+    def step():
+        opt.zero_grad(set_to_none=True)
+        loss = ((mesh_apply(m, x, p) - target).abs() ** 2).sum()
+        loss.backward()
+        opt.step()
+        return loss
+
+    first = float(step())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(n_steps - 1):
+        loss = step()
+    torch.cuda.synchronize()
+    t = (time.perf_counter() - t0) / (n_steps - 1)
+    with torch.no_grad():
+        U = mesh_apply(m, x, p).t().to(torch.complex128)
+        fid = float(torch.abs(torch.trace(U.conj().t() @ torch.tensor(Ut, dtype=torch.complex128, device=dev))) ** 2
+                    / Nc ** 2)
+    print(json.dumps({"metric": "Adam steps/s (unitary fitting)", "value": 1.0 / t, "unit": "steps/s", "n_gpus": 1,
+                      "steps": n_steps, "warmup": 1, "ms_per_step": t * 1e3, "higher_is_better": True,
+                      "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded)",
+                      "config": {"workload": "clements_mzi_N128_L128_haar_fit_2000_adam", "lr": 1e-2},
+                      "loss_first": first, "loss_last": float(loss), "fidelity": fid,
+                      "timing": "host wall clock per optimisation step (fwd + bwd + Adam), device synchronised"}))
+
+
 def run_batched(args):
     """Batched uneven meshes: the one-mesh-per-call drop-in (mg_fwdprop / mg_backdiff per mesh) against
     the persistent multi-mesh launch replayed from a CUDA graph; forward and forward + backward."""
@@ -575,9 +685,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--profile", action="store_true", help="two untimed steps only (for ncu captures)")
-    ap.add_argument("--workload", default="clements256", choices=["clements256", "batched", "serve"],
+    ap.add_argument("--workload", default="clements256", choices=["clements256", "batched", "serve", "c1", "c4"],
                     help="clements256: the headline fwd+bwd step; batched: 512 uneven meshes, plain vs "
-                         "persistent; serve: Poisson request stream on 64 resident meshes")
+                         "persistent; serve: Poisson request stream on 64 resident meshes; c1: N=64 forward; "
+                         "c4: N=128 unitary fitting with Adam")
     ap.add_argument("--duration", type=float, default=10.0, help="serve workload: seconds of traffic")
     ap.add_argument("--meshes", type=int, default=512, help="batched workload: number of meshes")
     args = ap.parse_args()
@@ -587,9 +698,9 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank)
         return
-    if args.workload in ("batched", "serve"):
+    if args.workload != "clements256":
         if rank == 0:
-            (run_batched if args.workload == "batched" else run_serve)(args)
+            {"batched": run_batched, "serve": run_serve, "c1": run_c1, "c4": run_c4}[args.workload](args)
         return
     if world > 1:
         import torch

@@ -86,6 +86,7 @@ _SIGS = {
                                 c_void_p]),
     "mg_phase_screen_grad": (c_int, [c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p]),
     "mg_fma_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
+    "mg_fma2_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
     "mg_plan": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, POINTER(mg_config), POINTER(mg_plan_info)]),
     # mesh and item arrays live in device memory: passed as raw addresses
     "mg_batched_propagate": (c_int, [c_int, c_void_p, c_int, c_void_p, c_int, c_void_p, c_int, c_size_t, c_void_p,
@@ -112,7 +113,11 @@ def load(path: str = LIB_PATH):
             except OSError as e:   # pragma: no cover - exercised only on broken installs
                 raise MeshLibraryError("cannot load %s: %s" % (path, e)) from e
             for name, (res, args) in _SIGS.items():
-                f = getattr(lib, name)
+                try:
+                    f = getattr(lib, name)
+                except AttributeError as e:
+                    raise MeshLibraryError("%s lacks %s (built from older sources); rebuild with "
+                                           "`python -m meshes_gb300.build`" % (path, name)) from e
                 f.restype = res
                 f.argtypes = args
             _lib = lib

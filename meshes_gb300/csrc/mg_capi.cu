@@ -414,6 +414,25 @@ __global__ void fma_probe_kernel(float* sink, int iters, float m) {
   sink[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// The same chains with packed FP32 pairs (one fma.rn.f32x2 = two FMAs per lane): whether the FMA pipe
+// retires more FLOPs per clock through the packed form than through scalar FMAs.
+__global__ void fma2_probe_kernel(float* sink, int iters, float m) {
+  float2 a[32];
+#pragma unroll
+  for (int k = 0; k < 32; ++k) a[k] = make_float2(threadIdx.x * 1e-3f + k, threadIdx.x * 2e-3f - k);
+  const float2 mm = make_float2(m, m), p = make_float2(0.25f, 0.25f), q = make_float2(-0.25f, -0.25f);
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int k = 0; k < 32; ++k) a[k] = __ffma2_rn(a[k], mm, p);
+#pragma unroll
+    for (int k = 0; k < 32; ++k) a[k] = __ffma2_rn(a[k], mm, q);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < 32; ++k) s += a[k].x + a[k].y;
+  sink[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace
 
 namespace mg {
@@ -712,6 +731,14 @@ int mg_fma_probe(float* sink, int blocks, int threads, int iters, void* stream) 
   fma_probe_kernel<<<blocks, threads, 0, static_cast<cudaStream_t>(stream)>>>(sink, iters, 0.999f);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MG_OK : cuda_fail(e, "fma_probe launch");
+}
+
+int mg_fma2_probe(float* sink, int blocks, int threads, int iters, void* stream) {
+  g_err.clear();
+  if (!sink || blocks < 1 || threads < 32 || threads > 1024 || iters < 1) return fail(MG_E_ARG, "bad probe arguments");
+  fma2_probe_kernel<<<blocks, threads, 0, static_cast<cudaStream_t>(stream)>>>(sink, iters, 0.999f);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MG_OK : cuda_fail(e, "fma2_probe launch");
 }
 
 }  // extern "C"

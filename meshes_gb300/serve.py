@@ -305,14 +305,17 @@ class MeshServer:
         while self.inflight and self.inflight[0].event.query():
             t = self.inflight.popleft()
             now = time.perf_counter()
-            hv = t.host.numpy()
-            o_y, n_y, o_dp, n_dp, o_gx, gidx = (a.tolist() for a in t.outs)
-            res = [hv[o: o + n].view(q.x.dtype).reshape(q.x.shape).copy() for q, o, n in zip(t.reqs, o_y, n_y)]
+            # one copy of the tick's results out of the pinned staging buffer; every result is a view of it
+            o_y, n_y, o_dp, n_dp, o_gx, gidx, lo, hi = t.outs
+            buf = t.host.numpy()[lo:hi].copy()
+            o_y, n_y, o_dp, n_dp, o_gx, gidx = ((a - lo if k in (0, 2, 4) else a).tolist()
+                                                for k, a in enumerate((o_y, n_y, o_dp, n_dp, o_gx, gidx)))
+            res = [buf[o: o + n].view(q.x.dtype).reshape(q.x.shape) for q, o, n in zip(t.reqs, o_y, n_y)]
             for k, i in enumerate(gidx):                   # gradient requests: (y, dJ/dp, dJ/dx*)
                 q = t.reqs[i]
                 m = self.res[q.mesh_id].mesh
-                dp = hv[o_dp[k]: o_dp[k] + n_dp[k]].view(np.float32).reshape(m.L, m.N // 2, m.X_np).copy()
-                gx = hv[o_gx[k]: o_gx[k] + n_y[i]].view(q.x.dtype).reshape(q.x.shape).copy()
+                dp = buf[o_dp[k]: o_dp[k] + n_dp[k]].view(np.float32).reshape(m.L, m.N // 2, m.X_np)
+                gx = buf[o_gx[k]: o_gx[k] + n_y[i]].view(q.x.dtype).reshape(q.x.shape)
                 res[i] = (res[i], dp, gx)
             for req, r in zip(t.reqs, res):
                 req.t_done = now
@@ -443,7 +446,7 @@ class MeshServer:
             gb = reqs[i].gy.view(np.uint8).reshape(-1)
             hv[off_gy + o: off_gy + o + gb.size] = gb
         # ---- result spans (host offsets = device offsets within the tick), read back on retirement
-        outs = (off_y + o_y, b * N * esz, off_dp + o_dp, dpn[gidx], off_gx + o_gx, gidx)
+        outs = (off_y + o_y, b * N * esz, off_dp + o_dp, dpn[gidx], off_gx + o_gx, gidx, off_y, out_end)
         # ---- enqueue on the next stream
         stream = self.streams[self.next_stream]
         self.next_stream = (self.next_stream + 1) % len(self.streams)
