@@ -130,7 +130,7 @@ def gpu_id(torch, dev) -> str:
         return str(dev.index or 0)
 
 
-def cpu_baseline(problem, seconds=10.0):
+def cpu_baseline(problem, seconds=10.0, with_c128=True):
     """Reference algorithm on the host cores: the oracle's C++ port of c/dot.cpp (complex64, OpenMP),
     forward (mode 0) + back-propagation (mode 2) on a bounded sample of the batch."""
     from oracle import meshes_oracle as O
@@ -152,6 +152,11 @@ def cpu_baseline(problem, seconds=10.0):
         if time.perf_counter() - t0 > seconds and reps >= 2:
             break
     rate = n_mzi * bs * reps / work
+    out = {"value": rate, "unit": "MZI-apps/s", "cores": threads, "kind": "port",
+           "sample": "%d of the %d vectors, fwd (mode 0) + bwd (mode 2), complex64, %d repeats, %.1f s"
+                     % (bs, B, reps, work)}
+    if not with_c128:
+        return out
     # the same in complex128 (the reference's own precision for dot / dot_vjp), a shorter sample
     a = time.perf_counter()
     reps128 = 0
@@ -161,11 +166,8 @@ def cpu_baseline(problem, seconds=10.0):
         reps128 += 1
         if time.perf_counter() - a > seconds / 4 and reps128 >= 2:
             break
-    rate128 = n_mzi * bs * reps128 / (time.perf_counter() - a)
-    return {"value": rate, "unit": "MZI-apps/s", "cores": threads, "kind": "port",
-            "sample": "%d of the %d vectors, fwd (mode 0) + bwd (mode 2), complex64, %d repeats, %.1f s"
-                      % (bs, B, reps, work),
-            "value_complex128": rate128}
+    out["value_complex128"] = n_mzi * bs * reps128 / (time.perf_counter() - a)
+    return out
 
 
 def traffic_from_profiles(name: str):
@@ -185,12 +187,13 @@ def run_reference(args, rank):
         return
     problem = make_problem()
     n_mzi = problem[6]
-    per_step = max(2.0, 60.0 / max(args.steps + args.warmup, 1))
+    # about a minute of CPU work in total, whatever K and W are (each step is a bounded sample)
+    per_step = max(0.05, 60.0 / max(args.steps + args.warmup, 1))
     for _ in range(args.warmup):
-        cpu_baseline(problem, seconds=0.5)
+        cpu_baseline(problem, seconds=min(per_step, 0.5), with_c128=False)
     vals = []
     for _ in range(args.steps):
-        vals.append(cpu_baseline(problem, seconds=per_step))
+        vals.append(cpu_baseline(problem, seconds=per_step, with_c128=False))
     value = statistics.median(v["value"] for v in vals)
     cb = dict(vals[0])
     cb["value"] = value
