@@ -488,7 +488,7 @@ def run_c4(args):
         opt.step()
         return loss
 
-    first = float(step())
+    first = float(step().detach())
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(n_steps - 1):
@@ -503,7 +503,7 @@ def run_c4(args):
                       "steps": n_steps, "warmup": 1, "ms_per_step": t * 1e3, "higher_is_better": True,
                       "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded)",
                       "config": {"workload": "clements_mzi_N128_L128_haar_fit_2000_adam", "lr": 1e-2},
-                      "loss_first": first, "loss_last": float(loss), "fidelity": fid,
+                      "loss_first": first, "loss_last": float(loss.detach()), "fidelity": fid,
                       "timing": "host wall clock per optimisation step (fwd + bwd + Adam), device synchronised"}))
 
 

@@ -244,6 +244,9 @@ int mg_phase_screen_grad(int N, int B, const void* u, const void* g, int ldu, fl
  * independent FMAs; writes one float per thread to `sink`.  Used by bench.py to measure the FP32
  * CUDA-core peak of the device it runs on. */
 int mg_fma_probe(float* sink, int blocks, int threads, int iters, void* stream);
+/* Self-check of the coefficient precompute's double-precision sin/cos: out[2i], out[2i+1] = the
+ * differences (sin, cos)(x[i]) own - library, for n device doubles x (used by the tests). */
+int mg_trig_check(const double* x, double* out, int n, void* stream);
 /* The same probe with packed FP32 pairs (fma.rn.f32x2, sm_100+): 128 FMAs per thread-iteration. */
 int mg_fma2_probe(float* sink, int blocks, int threads, int iters, void* stream);
 

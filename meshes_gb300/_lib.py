@@ -87,6 +87,7 @@ _SIGS = {
     "mg_phase_screen_grad": (c_int, [c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p]),
     "mg_fma_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
     "mg_fma2_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
+    "mg_trig_check": (c_int, [c_void_p, c_void_p, c_int, c_void_p]),
     "mg_plan": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, POINTER(mg_config), POINTER(mg_plan_info)]),
     # mesh and item arrays live in device memory: passed as raw addresses
     "mg_batched_propagate": (c_int, [c_int, c_void_p, c_int, c_void_p, c_int, c_void_p, c_int, c_size_t, c_void_p,

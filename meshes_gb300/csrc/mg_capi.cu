@@ -414,6 +414,17 @@ __global__ void fma_probe_kernel(float* sink, int iters, float m) {
   sink[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// sincos_d (the coefficient precompute's own double sin/cos) against the library sincos
+__global__ void trig_check_kernel(const double* x, double* out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s, c, s2, c2;
+  sincos_d(x[i], &s, &c);
+  sincos(x[i], &s2, &c2);
+  out[2 * i] = s - s2;
+  out[2 * i + 1] = c - c2;
+}
+
 // The same chains with packed FP32 pairs (one fma.rn.f32x2 = two FMAs per lane): whether the FMA pipe
 // retires more FLOPs per clock through the packed form than through scalar FMAs.
 __global__ void fma2_probe_kernel(float* sink, int iters, float m) {
@@ -731,6 +742,15 @@ int mg_fma_probe(float* sink, int blocks, int threads, int iters, void* stream) 
   fma_probe_kernel<<<blocks, threads, 0, static_cast<cudaStream_t>(stream)>>>(sink, iters, 0.999f);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MG_OK : cuda_fail(e, "fma_probe launch");
+}
+
+int mg_trig_check(const double* x, double* out, int n, void* stream) {
+  g_err.clear();
+  if (!x || !out || n < 0) return fail(MG_E_ARG, "bad trig check arguments");
+  if (n == 0) return MG_OK;
+  trig_check_kernel<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(x, out, n);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MG_OK : cuda_fail(e, "trig_check launch");
 }
 
 int mg_fma2_probe(float* sink, int blocks, int threads, int iters, void* stream) {

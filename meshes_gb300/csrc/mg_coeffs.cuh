@@ -136,7 +136,7 @@ __global__ void coef_kernel(const CoefArgs a) {
       if (active) {
         const float be = a.s ? a.s[(size_t)l * a.lds + (size_t)q * 2 + 1] : 0.f;
         double sb, cb;
-        sincos(0.78539816339744830962 + (double)be, &sb, &cb);
+        sincos_d(0.78539816339744830962 + (double)be, &sb, &cb);
         csv = make_float2((float)cb, (float)sb);
       }
       float2* cs = reinterpret_cast<float2*>(tl + M * G);

@@ -164,6 +164,60 @@ __device__ __forceinline__ Z zscale(double s, Z a) { return {s * a.x, s * a.y}; 
 __device__ __forceinline__ Z zi(Z a) { return {-a.y, a.x}; }
 __device__ __forceinline__ float2 zf(Z a) { return make_float2((float)a.x, (float)a.y); }
 
+// sin and cos in double precision for the coefficient precompute (GB300's FP64 pipe is narrow, and
+// this runs for every slot of every training step).  Cody-Waite reduction by pi/2 with a two-term
+// constant (PIO2_HI has its low 27 bits clear, so k * PIO2_HI is exact for |k| < 2^26; the split's
+// residual is 6e-25), then the Taylor series of sin and cos on [-pi/4, pi/4] evaluated by Horner's rule
+// to r^17 / r^18 (truncation below 1e-19; a shorter series below |r| < 1/8, truncation below 1e-20).
+// Arguments beyond 2^20 go to the library sincos.  Tested against the library sincos in the GPU tests.
+__device__ __forceinline__ void sincos_series(double r, double* s, double* c) {
+  const double r2 = r * r;
+  if (fabs(r) < 0.125) {
+    *s = r * fma(r2, fma(r2, fma(r2, fma(r2, fma(r2, -2.505210838544172e-08, 2.7557319223985893e-06),
+                                                -1.984126984126984e-04), 8.333333333333333e-03),
+                         -0.16666666666666666), 1.0);
+    *c = fma(r2, fma(r2, fma(r2, fma(r2, fma(r2, fma(r2, 2.08767569878681e-09, -2.755731922398589e-07),
+                                                 2.48015873015873e-05), -1.388888888888889e-03),
+                                 0.041666666666666664), -0.5), 1.0);
+    return;
+  }
+  double ps = 2.8114572543455206e-15;                                     // 1/17!
+  ps = fma(ps, r2, -7.647163731819816e-13);                               // 1/15!
+  ps = fma(ps, r2, 1.6059043836821613e-10);                               // 1/13!
+  ps = fma(ps, r2, -2.505210838544172e-08);                               // 1/11!
+  ps = fma(ps, r2, 2.7557319223985893e-06);                               // 1/9!
+  ps = fma(ps, r2, -1.984126984126984e-04);                               // 1/7!
+  ps = fma(ps, r2, 8.333333333333333e-03);                                // 1/5!
+  ps = fma(ps, r2, -0.16666666666666666);                                 // 1/3!
+  *s = fma(r * r2, ps, r);
+  double pc = -1.5619206968586225e-16;                                    // 1/18!
+  pc = fma(pc, r2, 4.779477332387385e-14);                                // 1/16!
+  pc = fma(pc, r2, -1.1470745597729725e-11);                              // 1/14!
+  pc = fma(pc, r2, 2.08767569878681e-09);                                 // 1/12!
+  pc = fma(pc, r2, -2.755731922398589e-07);                               // 1/10!
+  pc = fma(pc, r2, 2.48015873015873e-05);                                 // 1/8!
+  pc = fma(pc, r2, -1.388888888888889e-03);                               // 1/6!
+  pc = fma(pc, r2, 0.041666666666666664);                                 // 1/4!
+  pc = fma(pc, r2, -0.5);                                                 // 1/2!
+  *c = fma(r2, pc, 1.0);
+}
+__device__ __forceinline__ void sincos_d(double x, double* s, double* c) {
+  if (!(fabs(x) < 1048576.0)) {
+    sincos(x, s, c);
+    return;
+  }
+  const double k = rint(x * 0.63661977236758134308);                     // nearest multiple of pi/2
+  const double r = fma(-k, 1.5893254773528196e-08, fma(-k, 1.5707963109016418, x));
+  double sr, cr;
+  sincos_series(r, &sr, &cr);
+  switch (static_cast<int>(k) & 3) {
+    case 0: *s = sr; *c = cr; break;
+    case 1: *s = cr; *c = -sr; break;
+    case 2: *s = -sr; *c = -cr; break;
+    default: *s = -cr; *c = sr; break;
+  }
+}
+
 // Standard MZI T = S(beta) P(theta) S(alpha) P(phi) (reference crossing.py:216-221):
 //   T = e^{i th/2} [[e^{i ph}(i S Cm - C Sp),  i C Cp - S Sm],
 //                   [e^{i ph}(i C Cp + S Sm), -i S Cm - C Sp]]
@@ -171,11 +225,11 @@ __device__ __forceinline__ float2 zf(Z a) { return make_float2((float)a.x, (floa
 // (crossing.py:223-231): dE/dth = (i/2)E for both exponentials, dT/dph = T diag(i, 0).
 __device__ __forceinline__ void mzi_T(float th, float ph, float al, float be, C2x2* T, C2x2* D0, C2x2* D1) {
   double S, C, Sph, Cph, Sp = 0.0, Cp = 1.0, Sm = 0.0, Cm = 1.0;
-  sincos(0.5 * (double)th, &S, &C);
-  sincos((double)ph, &Sph, &Cph);
+  sincos_d(0.5 * (double)th, &S, &C);
+  sincos_d((double)ph, &Sph, &Cph);
   if (al != 0.f || be != 0.f) {
-    sincos((double)al + (double)be, &Sp, &Cp);
-    sincos((double)al - (double)be, &Sm, &Cm);
+    sincos_d((double)al + (double)be, &Sp, &Cp);
+    sincos_d((double)al - (double)be, &Sm, &Cm);
   }
   const Z E0 = {C, S};                                      // e^{i th/2}
   const Z E1 = zmul(E0, Z{Cph, Sph});                       // e^{i(th/2+ph)}
@@ -202,9 +256,9 @@ __device__ __forceinline__ void mzi_T(float th, float ph, float al, float be, C2
 //   T = [[e^{i ph}(S + i C sin2a), i C cos2a], [i C cos2a, e^{-i ph}(S - i C sin2a)]]
 __device__ __forceinline__ void sym_T(float th, float ph, float al, C2x2* T, C2x2* D0, C2x2* D1) {
   double S, C, Sph, Cph, S2a = 0.0, C2a = 1.0;
-  sincos(0.5 * (double)th, &S, &C);
-  sincos((double)ph, &Sph, &Cph);
-  if (al != 0.f) sincos(2.0 * (double)al, &S2a, &C2a);
+  sincos_d(0.5 * (double)th, &S, &C);
+  sincos_d((double)ph, &Sph, &Cph);
+  if (al != 0.f) sincos_d(2.0 * (double)al, &S2a, &C2a);
   const Z e = {Cph, Sph}, em = {Cph, -Sph};
   const Z T00 = zmul(e, Z{S, C * S2a}), T11 = zmul(em, Z{S, -C * S2a});
   T->t00 = zf(T00);
@@ -225,7 +279,7 @@ __device__ __forceinline__ void sym_T(float th, float ph, float al, C2x2* T, C2x
 // Real orthogonal crossing (reference gpu/crossing.cu:132-148): T = [[S, -C], [C, S]], S,C of th/2.
 __device__ __forceinline__ void orth_T(float th, R2x2* T, R2x2* D0) {
   double S, C;
-  sincos(0.5 * (double)th, &S, &C);
+  sincos_d(0.5 * (double)th, &S, &C);
   T->t00 = (float)S; T->t01 = (float)-C; T->t10 = (float)C; T->t11 = (float)S;
   if (D0) {
     D0->t00 = (float)(0.5 * C); D0->t01 = (float)(0.5 * S); D0->t10 = (float)(-0.5 * S); D0->t11 = (float)(0.5 * C);

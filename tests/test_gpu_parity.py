@@ -394,3 +394,18 @@ def test_split_launch_parity(cr, N, B):
     assert O.rel_err(outs[0].cpu().numpy(), y_ref) < TOL
     assert O.rel_err(outs[2][0].cpu().numpy(), gin) < TOL
     assert O.rel_err(outs[2][1].cpu().numpy().reshape(om.L, N // 2, n_p), O.contract_dp(om, G)) < TOL
+
+
+def test_coefficient_trigonometry_matches_library():
+    """The coefficient precompute's own double sin/cos (Cody-Waite reduction + Taylor series) agrees with
+    the CUDA library's to a few units in the last place, over phase-like, small and large arguments."""
+    from meshes_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(77)
+    x = np.concatenate([rng.uniform(0, 2 * np.pi, 20000), rng.uniform(-20, 20, 20000),
+                        rng.normal(0, 0.02, 20000), rng.uniform(-1e5, 1e5, 5000),
+                        np.arange(-64, 65) * np.pi / 4, [0.0, 1e-30, -1e-30, 0.125, -0.125, 2.0 ** 20, 3e7]])
+    xd = torch.tensor(x, dtype=torch.float64, device="cuda")
+    out = torch.empty(2 * x.size, dtype=torch.float64, device="cuda")
+    assert lib.mg_trig_check(xd.data_ptr(), out.data_ptr(), x.size, torch.cuda.current_stream().cuda_stream) == 0
+    assert out.abs().max().item() < 1e-15
