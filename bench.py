@@ -635,7 +635,7 @@ def run_serve(args):
     # 0.2 ms instead of every 5 ms, so neither side waits a whole default interval for the other
     sys.setswitchinterval(2e-4)
     n_mzi = [(sum(m.lens_h) if m.strides is None else m.L * (m.N // 2)) for m in meshes]
-    rate, duration = 20000.0, float(args.duration)
+    rate, duration = float(args.rate), float(args.duration)
     n_req = int(rate * duration)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
     mesh_ids = rng.integers(0, 64, n_req)
@@ -671,12 +671,11 @@ def run_serve(args):
     line = {"metric": "serve p50/p99 latency (ms) and MZI-apps/s", "value": float(np.percentile(lat, 50) * 1e3),
             "unit": "ms (p50 latency)", "n_gpus": 1, "steps": len(futs), "warmup": 64, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded Poisson stream)",
-            "config": {"workload": "serve_64_meshes_clements_butterfly_N16-512_20k_req_s", "rate_req_s": rate,
+            "config": {"workload": "serve_64_meshes_clements_butterfly_N16-512_%dk_req_s" % round(rate / 1000), "rate_req_s": rate,
                        "duration_s": duration, "requests": len(futs), "grad_fraction": float(grad.mean())},
             "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
             "throughput_mzi_apps_per_s": apps / span, "served_req_per_s": len(futs) / span, "ticks": srv.ticks,
-            "host_us_per_request": {k: 1e6 * v / max(srv.completed, 1) for k, v in srv.host_s.items()},
-            "client_us_per_submit": 1e6 * t_submit / max(len(futs), 1),
+            "client_us_per_submit": 1e6 * t_submit / max(len(futs), 1), "scheduler": "native (mg_server)",
             "status": srv.kernel_status()}
     print(json.dumps(line))
 
@@ -694,6 +693,7 @@ def main():
                          "c4: N=128 unitary fitting with Adam")
     ap.add_argument("--duration", type=float, default=10.0, help="serve workload: seconds of traffic")
     ap.add_argument("--meshes", type=int, default=512, help="batched workload: number of meshes")
+    ap.add_argument("--rate", type=float, default=20000.0, help="serve workload: offered requests per second")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

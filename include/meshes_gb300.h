@@ -208,6 +208,43 @@ int mg_propagate_l2(int N, int L, int B, int crossing, int geometry, const void*
                     void* g_out, int ldu, float* dp, int ldp, int accumulate, const mg_config* cfg, void* workspace,
                     size_t workspace_bytes, void* stream);
 
+/* ---- serving: native continuous-batching scheduler over resident meshes ------------------------
+ * The meshes' tiles are built beforehand (mg_build_tiles, W = 8 persistent configuration of their kernel
+ * class, both ops) and stay resident.  A scheduler thread owned by the server packs queued requests
+ * into ticks (admission by free space in a fixed device arena), runs one persistent forward launch
+ * per tick and, for gradient requests, one persistent back-propagation launch and reduction, and
+ * copies results into the caller's buffers; tags of finished requests come back from mg_server_wait.
+ * Inputs and outputs are host memory owned by the caller until the request's tag is returned. */
+typedef struct mg_server_mesh {
+  int N, L, cls, G, n_p, cap;          /* cls MG_BCLS_*; cap = vectors per work item (8 x 32/G x V) */
+  int fwd_CL, fwd_S, bwd_CL, bwd_S;
+  unsigned fwd_layer_bytes, bwd_layer_bytes;
+  const void* fwd_tiles;
+  const int* fwd_kinds;
+  const void* bwd_tiles;
+  const int* bwd_kinds;
+} mg_server_mesh;
+typedef struct mg_server mg_server;
+/* NULL on error (mg_last_error).  grid: persistent CTAs (the SM count); smem_*: the largest mg_plan_info.smem
+ * of the meshes' W = 8 plans per op. */
+mg_server* mg_server_create(const mg_server_mesh* meshes, int n_meshes, size_t arena_bytes, int n_streams,
+                            int max_per_tick, int grid, size_t smem_fwd, size_t smem_bwd, int device);
+/* Device bytes a request needs (admission accounting). */
+int mg_server_request_bytes(const mg_server* s, int mesh, int b, int grad, size_t* out);
+/* Queue a request: x (b, N) complex64 (float32 for orth), y (b, N) receives U x; with gy (b, N) = 2 dJ/dy*,
+ * dp (L, N/2, n_p) float32 receives dJ/dp and gx (b, N) receives 2 dJ/dx*.  MG_E_WORKSPACE if it can
+ * never fit the arena. */
+int mg_server_submit(mg_server* s, int mesh, int b, const void* x, const void* gy, void* y, float* dp, void* gx,
+                     unsigned long long tag);
+/* Up to max completed tags (waits up to timeout_us for the first); < 0 once the server has failed. */
+int mg_server_wait(mg_server* s, unsigned long long* tags, int max, int timeout_us);
+/* out[0] completed requests, out[1] ticks, out[2] queued requests. */
+int mg_server_stats(mg_server* s, long long* out);
+/* Kernel status word of the server's launches (synchronous read; 0 = ok). */
+int mg_server_status(mg_server* s);
+/* Stop: with drain, finish queued and in-flight requests first; then free everything. */
+void mg_server_destroy(mg_server* s, int drain);
+
 /* ---- lossy meshes: layer ranges and stored activations ----------------------------------------
  * The reference back-propagates by inverting each layer with T^H (c/dot.cpp:75-80, gpu/backprop.cu),
  * which is exact only for unitary crossings; for lossy ones (crossing.py:444-508, gains g_ij) that

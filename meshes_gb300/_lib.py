@@ -45,6 +45,13 @@ class mg_batch_mesh(Structure):
                 ("out0", c_void_p), ("out1", c_void_p), ("dp", c_void_p), ("partial", c_void_p)]
 
 
+class mg_server_mesh(Structure):
+    _fields_ = [("N", c_int), ("L", c_int), ("cls", c_int), ("G", c_int), ("n_p", c_int), ("cap", c_int),
+                ("fwd_CL", c_int), ("fwd_S", c_int), ("bwd_CL", c_int), ("bwd_S", c_int),
+                ("fwd_layer_bytes", c_uint), ("bwd_layer_bytes", c_uint), ("fwd_tiles", c_void_p),
+                ("fwd_kinds", c_void_p), ("bwd_tiles", c_void_p), ("bwd_kinds", c_void_p)]
+
+
 class mg_batch_item(Structure):
     _fields_ = [("mesh", c_int), ("v0", c_int), ("vend", c_int), ("part", c_int)]
 
@@ -85,6 +92,14 @@ _SIGS = {
     "mg_phase_screen": (c_int, [c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
                                 c_void_p]),
     "mg_phase_screen_grad": (c_int, [c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p]),
+    "mg_server_create": (c_void_p, [c_void_p, c_int, c_size_t, c_int, c_int, c_int, c_size_t, c_size_t, c_int]),
+    "mg_server_request_bytes": (c_int, [c_void_p, c_int, c_int, c_int, POINTER(c_size_t)]),
+    "mg_server_submit": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                 ctypes.c_ulonglong]),
+    "mg_server_wait": (c_int, [c_void_p, c_void_p, c_int, c_int]),
+    "mg_server_stats": (c_int, [c_void_p, c_void_p]),
+    "mg_server_status": (c_int, [c_void_p]),
+    "mg_server_destroy": (None, [c_void_p, c_int]),
     "mg_fma_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
     "mg_fma2_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
     "mg_trig_check": (c_int, [c_void_p, c_void_p, c_int, c_void_p]),
