@@ -507,6 +507,58 @@ def run_c4(args):
                       "timing": "host wall clock per optimisation step (fwd + bwd + Adam), device synchronised"}))
 
 
+def run_lossy(args):
+    """Lossy generic MZIs (phase errors and gains g_ij; reference crossing.py:444-488) on the Clements
+    N=256 L=256 mesh, B=4096: forward + adjoint through LossyMesh (inputs checkpointed every 16 layers,
+    each segment recomputed and back-propagated from stored layer inputs), J = sum |y - y_t|^2."""
+    import torch
+    from meshes_gb300 import geometry as gm
+    from meshes_gb300.lossy import LossyMesh
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    lens, shifts, p, s, x_h, yt_h, n_mzi = make_problem()
+    rng = np.random.default_rng(1006)
+    L = len(lens)
+    mask = gm.active_mask_nn(N, lens, shifts)
+    s14 = np.zeros((L, N // 2, 14))
+    s14[..., :2] = s
+    s14[..., 2:10] = rng.normal(0, 0.02, (L, N // 2, 8))
+    s14[..., 10:] = -np.abs(rng.normal(0.004, 0.002, (L, N // 2, 4)))
+    s14[~mask] = 0
+    mesh = LossyMesh(N, lens, shifts, device=dev)
+    pt = torch.tensor(p, dtype=torch.float64, device=dev, requires_grad=True)
+    st = torch.tensor(s14, dtype=torch.float64, device=dev)
+    x = torch.from_numpy(x_h).to(dev)
+    yt = torch.from_numpy(yt_h).to(dev)
+
+    def step():
+        pt.grad = None
+        y = mesh(x, mesh.T(pt, st))
+        loss = torch.sum(torch.abs(y - yt) ** 2)
+        loss.backward()
+        return loss
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    k = max(5, min(args.steps, 50))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(k):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) * 1e-3 / k
+    print(json.dumps({"metric": "MZI-apps/s (fwd+bwd, lossy, checkpointed)", "value": n_mzi * B / t,
+                      "unit": "MZI-apps/s", "n_gpus": 1, "steps": k, "warmup": args.warmup, "ms_per_step": t * 1e3,
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+                      "data": "synthetic (seeded)",
+                      "config": {"workload": "clements_lossy_mzi_N256_L256_B4096_fwd+bwd", "segment": mesh.segment,
+                                 "includes": "T(p) in float64 torch ops and its autograd, 16 forward-range "
+                                             "launches, 16 x (recompute + stored back-propagation + reduce)"},
+                      "status": mesh.status()}))
+
+
 def run_batched(args):
     """Batched uneven meshes: the one-mesh-per-call drop-in (mg_fwdprop / mg_backdiff per mesh) against
     the persistent multi-mesh launch replayed from a CUDA graph; forward and forward + backward."""
@@ -647,6 +699,10 @@ def run_serve(args):
         srv.submit(i, pools[i][:4]).result(60)
     futs = []
     t_submit = 0.0
+    # the harness keeps every future and result alive; without this the interpreter's full collections
+    # walk hundreds of thousands of them and stall the client and completion threads for ~0.1-0.2 s
+    import gc
+    gc.disable()
     t0 = time.perf_counter()
     k = 0
     while k < n_req:
@@ -663,6 +719,7 @@ def run_serve(args):
     for _, f in futs:
         f.result(120)
     t_end = max(f.t_done for _, f in futs)
+    gc.enable()
     srv.stop()
     # latency of each request: result available on the host minus its scheduled arrival time
     lat = np.array([f.t_done - (t0 + arrivals[kk]) for kk, f in futs])
@@ -687,10 +744,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--profile", action="store_true", help="two untimed steps only (for ncu captures)")
-    ap.add_argument("--workload", default="clements256", choices=["clements256", "batched", "serve", "c1", "c4"],
+    ap.add_argument("--workload", default="clements256", choices=["clements256", "batched", "serve", "c1", "c4", "lossy"],
                     help="clements256: the headline fwd+bwd step; batched: 512 uneven meshes, plain vs "
                          "persistent; serve: Poisson request stream on 64 resident meshes; c1: N=64 forward; "
-                         "c4: N=128 unitary fitting with Adam")
+                         "c4: N=128 unitary fitting with Adam; lossy: checkpointed adjoint of lossy MZIs")
     ap.add_argument("--duration", type=float, default=10.0, help="serve workload: seconds of traffic")
     ap.add_argument("--meshes", type=int, default=512, help="batched workload: number of meshes")
     ap.add_argument("--rate", type=float, default=20000.0, help="serve workload: offered requests per second")
@@ -703,7 +760,8 @@ def main():
         return
     if args.workload != "clements256":
         if rank == 0:
-            {"batched": run_batched, "serve": run_serve, "c1": run_c1, "c4": run_c4}[args.workload](args)
+            {"batched": run_batched, "serve": run_serve, "c1": run_c1, "c4": run_c4,
+             "lossy": run_lossy}[args.workload](args)
         return
     if world > 1:
         import torch
