@@ -163,8 +163,9 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   // split launch: when one wave of uniform CTAs cannot cover the SMs evenly (B between SMs x 4 warps x V
   // and SMs x 4 warps x (2V-1) vectors), run two 4-warp CTAs per SM holding V and V-1 vectors per lane
   // group.  split: 0 auto, 1 on, 2 off.  Automatic for forward propagation only: measured on GB300 at
-  // N=256, B=4096 it saves 5% there, while back-propagation loses more than it gains (every CTA reduces
-  // the gradient of every slot, so twice the CTAs is twice that work and twice the partials).
+  // N=256, B=4096 it saves 5% there, while back-propagation gets 28% slower: its two bodies (V and
+  // V-1, ~25 KB of code each) overflow the instruction cache together (ncu: instruction-fetch stalls
+  // 17x those of the uniform launch).
   const int split_mode = cfg ? cfg->split : 0;
   p.split = false;
   p.nA = 0;

@@ -137,7 +137,8 @@ class MeshServer:
                 time.sleep(1e-3)
         self._final_stats = self.stats()
         self._final_status = self.lib.mg_server_status(h)
-        self.handle = None
+        with self.plock:
+            self.handle = None                             # no submit reaches h after this
         if self.waiter is not None:
             self.waiter.join(timeout)                      # sees handle None within one wait period
         self.lib.mg_server_destroy(h, 1 if drain else 0)  # joins the scheduler thread, frees its memory
@@ -170,18 +171,19 @@ class MeshServer:
             dp = np.empty((m.L, m.N // 2, m.X_np), dtype=np.float32)
             gx = np.empty_like(x)
         fut: Future = Future()
-        with self.plock:
+        with self.plock:                                   # stop() clears the handle under the same lock
+            if self.handle is None:
+                raise ServerError("server stopped")
             self.tag += 1
             tag = self.tag
+            rc = self.lib.mg_server_submit(self.handle, mesh_id, x.shape[0], x.ctypes.data,
+                                           None if gy is None else gy.ctypes.data, y.ctypes.data,
+                                           None if dp is None else dp.ctypes.data,
+                                           None if gx is None else gx.ctypes.data, tag)
+            if rc != 0:
+                raise ServerError(_lib.last_error())
             self.pending[tag] = (fut, (x, gy), (y, dp, gx))
-        rc = self.lib.mg_server_submit(h, mesh_id, x.shape[0], x.ctypes.data, None if gy is None else gy.ctypes.data,
-                                       y.ctypes.data, None if dp is None else dp.ctypes.data,
-                                       None if gx is None else gx.ctypes.data, tag)
-        if rc != 0:
-            with self.plock:
-                self.pending.pop(tag, None)
-            raise ServerError(_lib.last_error())
-        self.mzi_apps += self.res[mesh_id].n_mzi * x.shape[0] * (2 if gy is not None else 1)
+            self.mzi_apps += self.res[mesh_id].n_mzi * x.shape[0] * (2 if gy is not None else 1)
         return fut
 
     def _wait_loop(self, h):
