@@ -275,6 +275,19 @@ int mg_phase_screen(int N, int B, const float* ph, const float* dph, int sgn, co
 int mg_phase_screen_grad(int N, int B, const void* u, const void* g, int ldu, float* dph, int accumulate,
                          void* stream);
 
+/* The whole checkpointed adjoint of a generic (lossy) mesh in two calls (tiles of MG_OP_FWD in ws /
+ * ws_fwd, of MG_OP_BWD_STORED in ws_bwd; complex64 fields with leading dimension ldu).
+ * mg_lossy_forward: y = U x by segments of `seg` layers, keeping the input of every segment after the
+ * first in ckpt ([ceil(L/seg) - 1][B][ldu]).
+ * mg_lossy_backward: from x, ckpt and gy = 2 dJ/dy*: gx = 2 dJ/dx*, and dT (complex64 [L][N/2][2][2]) =
+ * sum_b g_i conj(x_j) per slot; segments in reverse, each recomputed into act ([seg][B][ldu]) and
+ * back-propagated from it; gtmp is a (B, ldu) scratch field. */
+int mg_lossy_forward(int N, int L, int B, int geometry, int seg, const void* x, void* y, void* ckpt, int ldu, void* ws,
+                     size_t ws_bytes, void* stream);
+int mg_lossy_backward(int N, int L, int B, int geometry, int seg, const void* x, const void* ckpt, const void* gy,
+                      void* gx, void* gtmp, void* act, void* dT, int ldu, void* ws_fwd, size_t ws_fwd_bytes,
+                      void* ws_bwd, size_t ws_bwd_bytes, void* stream);
+
 /* ---- measurement helpers -------------------------------------------------------------------- */
 
 /* FP32 FMA throughput probe: `blocks` x `threads` threads each run `iters` iterations of 64

@@ -100,6 +100,10 @@ _SIGS = {
     "mg_server_stats": (c_int, [c_void_p, c_void_p]),
     "mg_server_status": (c_int, [c_void_p]),
     "mg_server_destroy": (None, [c_void_p, c_int]),
+    "mg_lossy_forward": (c_int, [c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p,
+                                 c_size_t, c_void_p]),
+    "mg_lossy_backward": (c_int, [c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                  c_void_p, c_void_p, c_int, c_void_p, c_size_t, c_void_p, c_size_t, c_void_p]),
     "mg_fma_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
     "mg_fma2_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
     "mg_trig_check": (c_int, [c_void_p, c_void_p, c_int, c_void_p]),

@@ -737,6 +737,64 @@ int mg_propagate_range(int op, int N, int L, int l0, int l1, int B, int crossing
   return MG_OK;
 }
 
+int mg_lossy_forward(int N, int L, int B, int geometry, int seg, const void* x, void* y, void* ckpt, int ldu, void* ws,
+                     size_t wsb, void* stream) {
+  g_err.clear();
+  if (seg < 1) return fail(MG_E_ARG, "segment length %d < 1", seg);
+  if (L == 0) {
+    if (B > 0 && y != x) {
+      cudaError_t e = cudaMemcpy2DAsync(y, (size_t)ldu * 8, x, (size_t)ldu * 8, (size_t)N * 8, B,
+                                        cudaMemcpyDeviceToDevice, static_cast<cudaStream_t>(stream));
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy2DAsync");
+    }
+    return MG_OK;
+  }
+  if (L > seg && !ckpt && B > 0) return fail(MG_E_ARG, "ckpt is NULL");
+  const size_t plane = (size_t)B * ldu;
+  const void* cur = x;
+  for (int l0 = 0, k = 0; l0 < L; l0 += seg, ++k) {
+    const int l1 = std::min(L, l0 + seg);
+    void* out = (l1 < L) ? static_cast<void*>(static_cast<float2*>(ckpt) + (size_t)k * plane) : y;
+    TRY(mg_propagate_range(OP_FWD, N, L, l0, l1, B, CR_GENERIC, geometry, cur, nullptr, out, nullptr, ldu, nullptr,
+                           nullptr, 0, nullptr, ws, wsb, stream));
+    cur = out;
+  }
+  return MG_OK;
+}
+
+int mg_lossy_backward(int N, int L, int B, int geometry, int seg, const void* x, const void* ckpt, const void* gy,
+                      void* gx, void* gtmp, void* act, void* dT, int ldu, void* ws_fwd, size_t wsb_fwd, void* ws_bwd,
+                      size_t wsb_bwd, void* stream) {
+  g_err.clear();
+  if (seg < 1) return fail(MG_E_ARG, "segment length %d < 1", seg);
+  if (B > 0 && (!gy || !gx || !gtmp || !act || !x)) return fail(MG_E_ARG, "NULL buffer");
+  if (L == 0) {
+    if (B > 0 && gx != gy) {
+      cudaError_t e = cudaMemcpy2DAsync(gx, (size_t)ldu * 8, gy, (size_t)ldu * 8, (size_t)N * 8, B,
+                                        cudaMemcpyDeviceToDevice, static_cast<cudaStream_t>(stream));
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy2DAsync");
+    }
+    return MG_OK;
+  }
+  if (L > seg && !ckpt && B > 0) return fail(MG_E_ARG, "ckpt is NULL");
+  const size_t plane = (size_t)B * ldu;
+  const int K = (L + seg - 1) / seg;
+  const void* g = gy;
+  for (int k = K - 1; k >= 0; --k) {
+    const int l0 = k * seg, l1 = std::min(L, l0 + seg);
+    const void* in = (k == 0) ? x : static_cast<const void*>(static_cast<const float2*>(ckpt) + (size_t)(k - 1) * plane);
+    // the layer inputs of the segment, recomputed from its checkpoint
+    TRY(mg_propagate_range(OP_FWD, N, L, l0, l1, B, CR_GENERIC, geometry, in, nullptr, nullptr, nullptr, ldu, act,
+                           nullptr, 0, nullptr, ws_fwd, wsb_fwd, stream));
+    // back-propagation through them; gradients alternate between gx and gtmp and end in gx
+    void* out = (k % 2 == 0) ? gx : gtmp;
+    TRY(mg_propagate_range(MG_OP_BWD_STORED, N, L, l0, l1, B, CR_GENERIC, geometry, nullptr, g, nullptr, out, ldu,
+                           act, dT, 0, nullptr, ws_bwd, wsb_bwd, stream));
+    g = out;
+  }
+  return MG_OK;
+}
+
 int mg_fma_probe(float* sink, int blocks, int threads, int iters, void* stream) {
   g_err.clear();
   if (!sink || blocks < 1 || threads < 32 || threads > 1024 || iters < 1) return fail(MG_E_ARG, "bad probe arguments");

@@ -6,7 +6,8 @@ A lossy crossing - the generic MZI of crossing.py:444-488, with phase errors and
 Here the adjoint keeps the mesh input of every segment of ``segment`` = ceil(sqrt(L)) layers during the
 forward pass; back-propagation then walks the segments in reverse, recomputes each segment's layer inputs
 from its checkpoint (one forward launch that writes them to a (segment, B, N) buffer) and back-propagates
-through the segment from those stored inputs (one launch plus a deterministic reduction).  Memory is
+through the segment from those stored inputs (one launch plus a deterministic reduction).  Each
+direction is one library call (mg_lossy_forward / mg_lossy_backward) that runs all its segments.  Memory is
 about 2 sqrt(L) fields instead of L; work is one extra forward pass.
 
 The crossing is given as its transfer matrices ``T`` (L, N/2, 2, 2), complex, in the reference's slot
@@ -153,41 +154,36 @@ class LossyMeshFunction(torch.autograd.Function):
         x = x.detach().to(device=mesh.device, dtype=torch.complex64).contiguous()
         Tc = T.detach().to(device=mesh.device, dtype=torch.complex64).contiguous()
         B, L, seg = x.shape[0], mesh.L, mesh.segment
-        ckpts = [x]
-        cur = x
-        if B > 0 and L > 0:
-            ws, nb = mesh._build(OP_FWD, Tc, B)
-            for l0 in range(0, L, seg):
-                out = torch.empty_like(x)
-                mesh._range(OP_FWD, l0, min(L, l0 + seg), B, cur, None, out, None, None, None, ws, nb)
-                if l0 + seg < L:
-                    ckpts.append(out)
-                cur = out
-        y = cur.clone() if cur is x else cur
+        K = -(-L // seg)
+        ckpt = torch.empty((max(K - 1, 0), B, mesh.N), dtype=torch.complex64, device=mesh.device)
+        y = torch.empty_like(x)
+        if B > 0:
+            ws, nb = mesh._build(OP_FWD, Tc, B) if L > 0 else (None, 0)
+            check(load().mg_lossy_forward(mesh.N, L, B, mesh.geometry, seg, x.data_ptr(), y.data_ptr(),
+                                          ckpt.data_ptr() if ckpt.numel() else None, mesh.N, ws, nb,
+                                          _stream(mesh.device)), "mg_lossy_forward")
         ctx.mesh = mesh
         ctx.T_dtype = T.dtype
-        ctx.save_for_backward(Tc, *ckpts)
+        ctx.save_for_backward(Tc, x, ckpt)
         return y
 
     @staticmethod
     def backward(ctx, gy: torch.Tensor):
         mesh = ctx.mesh
-        Tc, *ckpts = ctx.saved_tensors
-        B, N, L, seg = ckpts[0].shape[0], mesh.N, mesh.L, mesh.segment
-        g = gy.detach().to(torch.complex64).contiguous()
+        Tc, x, ckpt = ctx.saved_tensors
+        B, N, L, seg = x.shape[0], mesh.N, mesh.L, mesh.segment
+        gy = gy.detach().to(torch.complex64).contiguous()
         dT = torch.zeros((L, N // 2, 2, 2), dtype=torch.complex64, device=mesh.device)
-        if B > 0 and L > 0:
-            wsf, nbf = mesh._build(OP_FWD, Tc, B)
-            wsb, nbb = mesh._build(OP_BWD_STORED, Tc, B)
-            act = torch.empty((seg, B, N), dtype=torch.complex64, device=mesh.device)
-            starts = list(range(0, L, seg))
-            for k in range(len(starts) - 1, -1, -1):
-                l0, l1 = starts[k], min(L, starts[k] + seg)
-                # the inputs of layers l0..l1-1, recomputed from the segment's checkpoint
-                mesh._range(OP_FWD, l0, l1, B, ckpts[k], None, None, None, act, None, wsf, nbf)
-                gn = torch.empty_like(g)
-                mesh._range(OP_BWD_STORED, l0, l1, B, None, g, None, gn, act, dT, wsb, nbb)
-                g = gn
+        g = torch.empty_like(gy)
+        if B > 0:
+            wsf, nbf = mesh._build(OP_FWD, Tc, B) if L > 0 else (None, 0)
+            wsb, nbb = mesh._build(OP_BWD_STORED, Tc, B) if L > 0 else (None, 0)
+            act = torch.empty((min(seg, max(L, 1)), B, N), dtype=torch.complex64, device=mesh.device)
+            gtmp = torch.empty_like(gy)
+            check(load().mg_lossy_backward(N, L, B, mesh.geometry, seg, x.data_ptr(),
+                                           ckpt.data_ptr() if ckpt.numel() else None, gy.data_ptr(), g.data_ptr(),
+                                           gtmp.data_ptr(), act.data_ptr(), dT.data_ptr(), N, wsf, nbf, wsb, nbb,
+                                           _stream(mesh.device)), "mg_lossy_backward")
         gx = g if ctx.needs_input_grad[0] else None
         gT = dT.to(ctx.T_dtype) if ctx.needs_input_grad[1] else None
         return gx, gT, None
