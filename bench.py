@@ -588,9 +588,9 @@ def run_lossy(args):
                       "unit": "MZI-apps/s", "n_gpus": 1, "steps": k, "warmup": args.warmup, "ms_per_step": t * 1e3,
                       "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
                       "data": "synthetic (seeded)",
-                      "config": {"workload": "clements_lossy_mzi_N256_L256_B4096_fwd+bwd", "segment": mesh.segment,
-                                 "includes": "T(p) in float64 torch ops and its autograd, 16 forward-range "
-                                             "launches, 16 x (recompute + stored back-propagation + reduce)"},
+                      "config": {"workload": "clements_lossy_mzi_N256_L256_B4096_fwd+bwd", "segment": mesh.segment_for(B),
+                                 "includes": "T(p) in float64 torch ops and its autograd; per segment a forward "
+                                             "launch, then a recompute, a stored back-propagation and a reduce"},
                       "status": mesh.status()}))
 
 

@@ -728,7 +728,8 @@ int mg_propagate_range(int op, int N, int L, int l0, int l1, int B, int crossing
   if (e != cudaSuccess) return cuda_fail(e, "prop_kernel launch");
   if (bwd) {
     const int n = nl * P.np2;
-    raw_reduce_kernel<<<(n + 255) / 256, 256, 0, lc.stream>>>(a.partial, P.grid, nl, P.np2, P.M, P.G, N,
+    raw_reduce_kernel<<<(4 * n + kReduceCols - 1) / kReduceCols, kReduceCols * kReduceRows, 0, lc.stream>>>(
+        a.partial, P.grid, nl, P.np2, P.M, P.G, N,
                                                              static_cast<float2*>(dT) + (size_t)l0 * (N / 2) * 4,
                                                              accumulate, kinds_full + L + 2 * l0);
     e = cudaGetLastError();

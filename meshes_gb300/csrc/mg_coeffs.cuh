@@ -279,31 +279,42 @@ dp_reduce_kernel(const float2* __restrict__ partial, int nC, int L, int np2, int
 // Stored-activation back-propagation (lossy crossings): dT[l][q][k] (= or +=) the conjugate of the sum
 // over the nC per-CTA raw partials [c][l][k][pos], k = (00, 01, 10, 11).  The conjugate turns the kernel's
 // sum of conj(g_i) x_j into g_i conj(x_j) = 2 dJ/dT_ij*, the gradient convention of complex tensors in
-// PyTorch.  Inactive slots give 0.  One thread per (layer, slot position), CTAs summed in order.
-__global__ void __launch_bounds__(256)
+// PyTorch.  Inactive slots give 0.  A CTA's partials are one contiguous block of nl*4*np2 float2, so a
+// block of 32 columns x 8 rows owns 32 consecutive entries: its rows sum the CTAs c = row, row + 8, ...
+// (several loads in flight), then the 8 row sums are combined in a fixed order (bit-stable).
+__global__ void __launch_bounds__(kReduceCols * kReduceRows)
 raw_reduce_kernel(const float2* __restrict__ partial, int nC, int L, int np2, int M, int G, int N, float2* dT,
                   int accumulate, const int* geo) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= L * np2) return;
-  const int l = idx / np2, pos = idx - l * np2;
-  const size_t stride = (size_t)L * 4 * np2;
-  const float2* p = partial + (size_t)l * 4 * np2 + pos;
-  float2 s0 = make_float2(0.f, 0.f), s1 = s0, s2 = s0, s3 = s0;
-  for (int c = 0; c < nC; ++c) {
-    const float2* pc = p + (size_t)c * stride;
-    const float2 a0 = __ldg(pc), a1 = __ldg(pc + np2), a2 = __ldg(pc + 2 * np2), a3 = __ldg(pc + 3 * np2);
-    s0 = cadd(s0, a0); s1 = cadd(s1, a1); s2 = cadd(s2, a2); s3 = cadd(s3, a3);
+  __shared__ float2 acc[kReduceRows][kReduceCols];
+  const int col = threadIdx.x % kReduceCols, row = threadIdx.x / kReduceCols;
+  const size_t n = (size_t)L * 4 * np2;
+  const size_t idx = (size_t)blockIdx.x * kReduceCols + col;
+  const bool valid = idx < n;
+  float2 s = make_float2(0.f, 0.f);
+  if (valid) {
+    const float2* p = partial + idx;
+    int c = row;
+    for (; c + 3 * kReduceRows < nC; c += 4 * kReduceRows) {
+      const float2 a0 = __ldg(p + (size_t)c * n), a1 = __ldg(p + (size_t)(c + kReduceRows) * n);
+      const float2 a2 = __ldg(p + (size_t)(c + 2 * kReduceRows) * n), a3 = __ldg(p + (size_t)(c + 3 * kReduceRows) * n);
+      s = cadd(s, a0); s = cadd(s, a1); s = cadd(s, a2); s = cadd(s, a3);
+    }
+    for (; c < nC; c += kReduceRows) s = cadd(s, __ldg(p + (size_t)c * n));
   }
+  acc[row][col] = s;
+  __syncthreads();
+  if (row != 0 || !valid) return;
+  for (int r = 1; r < kReduceRows; ++r) s = cadd(s, acc[r][col]);
+  const int l = (int)(idx / (4 * (size_t)np2));
+  const int rem = (int)(idx - (size_t)l * 4 * np2);
+  const int k = rem / np2, pos = rem - k * np2;
   const int q = pos_slot(pos, M, G);
   if (q >= N / 2) return;
   const int sh = geo[2 * l], ln = geo[2 * l + 1];
   const bool active = q >= sh / 2 && q < sh / 2 + ln;
-  float2* o = dT + ((size_t)l * (N / 2) + q) * 4;
-  const float2 v[4] = {s0, s1, s2, s3};
-  for (int k = 0; k < 4; ++k) {
-    const float2 c = active ? make_float2(v[k].x, -v[k].y) : make_float2(0.f, 0.f);
-    o[k] = accumulate ? cadd(o[k], c) : c;
-  }
+  float2* o = dT + ((size_t)l * (N / 2) + q) * 4 + k;
+  const float2 c = active ? make_float2(s.x, -s.y) : make_float2(0.f, 0.f);
+  *o = accumulate ? cadd(*o, c) : c;
 }
 
 }  // namespace mg

@@ -3,9 +3,10 @@
 The lossless path back-propagates by inverting each layer with T^H (the reference's c/dot.cpp:75-80 and
 gpu/backprop.cu do the same), which needs no stored activations but is exact only for unitary crossings.
 A lossy crossing - the generic MZI of crossing.py:444-488, with phase errors and gains g_ij - breaks it.
-Here the adjoint keeps the mesh input of every segment of ``segment`` = ceil(sqrt(L)) layers during the
-forward pass; back-propagation then walks the segments in reverse, recomputes each segment's layer inputs
-from its checkpoint (one forward launch that writes them to a (segment, B, N) buffer) and back-propagates
+Here the adjoint keeps the mesh input of every segment of ceil(sqrt(L)) layers (fewer when a segment's
+stored layer inputs would not stay in L2) during the forward pass; back-propagation then walks the
+segments in reverse, recomputes each segment's layer inputs from its checkpoint (one forward launch
+that writes them to a (segment, B, N) buffer) and back-propagates
 through the segment from those stored inputs (one launch plus a deterministic reduction).  Each
 direction is one library call (mg_lossy_forward / mg_lossy_backward) that runs all its segments.  Memory is
 about 2 sqrt(L) fields instead of L; work is one extra forward pass.
@@ -62,7 +63,7 @@ class LossyMesh:
     """Geometry of a mesh of generic (possibly lossy) crossings; ``mesh(x, T)`` is y = U(T) x.
 
     Nearest-neighbour geometry (``lens``, ``shifts``, as gpu/mesh.py:50-60) or butterfly/FFT strides.
-    ``segment`` is the checkpoint spacing of the adjoint (default ceil(sqrt(L))).
+    ``segment`` fixes the checkpoint spacing of the adjoint (default: ``segment_for(B)``).
     """
 
     def __init__(self, N: int, lens=None, shifts=None, strides=None, device=None, segment: Optional[int] = None):
@@ -91,8 +92,23 @@ class LossyMesh:
             for l, (ln, sh) in enumerate(zip(self.lens_h, self.shifts_h)):
                 active[l, sh // 2: sh // 2 + ln] = True
         self.active = torch.as_tensor(active, device=self.device)
-        self.segment = int(segment) if segment else max(1, math.ceil(math.sqrt(max(self.L, 1))))
+        self._segment = int(segment) if segment else None
         self._ws = {}
+
+    # stored activations of one segment should stay in the 129 MB L2 between the recompute and the
+    # back-propagation that reads them: at most ~64 MB of them, else ceil(sqrt(L)) layers
+    L2_STAGE_BYTES = 64 << 20
+
+    def segment_for(self, B: int) -> int:
+        """Checkpoint spacing used for a batch of B vectors."""
+        if self._segment:
+            return self._segment
+        seg = max(1, math.ceil(math.sqrt(max(self.L, 1))))
+        return max(1, min(seg, self.L2_STAGE_BYTES // max(1, B * self.N * 8)))
+
+    @property
+    def segment(self) -> int:
+        return self._segment or max(1, math.ceil(math.sqrt(max(self.L, 1))))
 
     # ---- plumbing
     def _geo(self):
@@ -153,7 +169,8 @@ class LossyMeshFunction(torch.autograd.Function):
         assert tuple(T.shape) == (mesh.L, mesh.N // 2, 2, 2), "T must be (L, N/2, 2, 2)"
         x = x.detach().to(device=mesh.device, dtype=torch.complex64).contiguous()
         Tc = T.detach().to(device=mesh.device, dtype=torch.complex64).contiguous()
-        B, L, seg = x.shape[0], mesh.L, mesh.segment
+        B, L = x.shape[0], mesh.L
+        seg = mesh.segment_for(B)
         K = -(-L // seg)
         ckpt = torch.empty((max(K - 1, 0), B, mesh.N), dtype=torch.complex64, device=mesh.device)
         y = torch.empty_like(x)
@@ -163,6 +180,7 @@ class LossyMeshFunction(torch.autograd.Function):
                                           ckpt.data_ptr() if ckpt.numel() else None, mesh.N, ws, nb,
                                           _stream(mesh.device)), "mg_lossy_forward")
         ctx.mesh = mesh
+        ctx.seg = seg
         ctx.T_dtype = T.dtype
         ctx.save_for_backward(Tc, x, ckpt)
         return y
@@ -171,7 +189,7 @@ class LossyMeshFunction(torch.autograd.Function):
     def backward(ctx, gy: torch.Tensor):
         mesh = ctx.mesh
         Tc, x, ckpt = ctx.saved_tensors
-        B, N, L, seg = x.shape[0], mesh.N, mesh.L, mesh.segment
+        B, N, L, seg = x.shape[0], mesh.N, mesh.L, ctx.seg
         gy = gy.detach().to(torch.complex64).contiguous()
         dT = torch.zeros((L, N // 2, 2, 2), dtype=torch.complex64, device=mesh.device)
         g = torch.empty_like(gy)
