@@ -389,6 +389,12 @@ def run_ours(args, rank, world, local_rank):
     bwd_flops = n_mzi * B * FLOP_BWD
     achieved = bwd_flops / t_bwd
     traffic = traffic_from_profiles("prop_bwd_clements_N256_L256_B4096.md")
+    bwd_bytes = B * N * 3 * 8 + n_mzi * 4 * (2 + 2) + n_mzi * 4 * 2
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            hbm_peak, hbm_src = float(json.load(f)["hbm_gbs"]), "measured (copy bandwidth)"
+    except (OSError, KeyError, ValueError):
+        hbm_peak, hbm_src = 6800.0, "fallback"
     line = {
         "metric": METRIC, "value": value, "unit": "MZI-apps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -406,6 +412,12 @@ def run_ours(args, rank, world, local_rank):
                      "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / peak,
                      "peak_source": "measured: FP32 FMA probe on this GPU (no FP32 entry in the measured-peaks file)",
                      "traffic": traffic, "algorithmic_flops_per_launch": bwd_flops},
+        # the same kernel against the HBM roofline (algorithmic bytes: read y and g, write g_in, the
+        # parameters and dJ/dp), showing how far it is from being memory-bound
+        "roofline_hbm": {"kernel": "prop_kernel<BWD> (back-propagation)", "bound": "hbm",
+                         "achieved": bwd_bytes / t_bwd / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": bwd_bytes / t_bwd / 1e9 / hbm_peak, "traffic": traffic,
+                         "peak_source": hbm_src, "algorithmic_bytes_per_launch": bwd_bytes},
         "e2e": {"value": units / t_e2e, "unit": "MZI-apps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "pipelined": "next step's H2D on a second stream during the current step",
                 "serialized_value": units / t_e2e_serial},
