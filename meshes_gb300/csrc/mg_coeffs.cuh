@@ -62,10 +62,17 @@ __device__ __forceinline__ void slot_T(const CoefArgs& a, int l, int q, bool act
   const int n_p = crossing_np(a.crossing), n_s = crossing_ns(a.crossing);
   const float* pp = a.p + (size_t)l * a.ldp + (size_t)q * n_p;
   const float* ss = a.s ? a.s + (size_t)l * a.lds + (size_t)q * n_s : nullptr;
+  // dT/dp only where a tile needs it: forward-mode tiles and the dT/dp tiles of back-propagation
+  // without a direct-gradient mode
+  const bool need_d = a.op == OP_FWDDIFF || (a.op == OP_BWD && a.gr == 0);
+  if (!need_d) {
+    D0 = c2x2_zero();
+    D1 = c2x2_zero();
+  }
   if (a.crossing == CR_MZI) {
-    mzi_T(pp[0], pp[1], ss ? ss[0] : 0.f, ss ? ss[1] : 0.f, &T, &D0, &D1);
+    mzi_T(pp[0], pp[1], ss ? ss[0] : 0.f, ss ? ss[1] : 0.f, &T, need_d ? &D0 : nullptr, need_d ? &D1 : nullptr);
   } else {   // CR_SYM
-    sym_T(pp[0], pp[1], ss ? ss[0] : 0.f, &T, &D0, &D1);
+    sym_T(pp[0], pp[1], ss ? ss[0] : 0.f, &T, need_d ? &D0 : nullptr, need_d ? &D1 : nullptr);
   }
 }
 
@@ -75,7 +82,9 @@ __device__ __forceinline__ void slot_R(const CoefArgs& a, int l, int q, bool act
     D0.t00 = D0.t01 = D0.t10 = D0.t11 = 0.f;
     return;
   }
-  orth_T(a.p[(size_t)l * a.ldp + q], &T, &D0);
+  const bool need_d = a.op == OP_FWDDIFF || (a.op == OP_BWD && a.gr == 0);
+  if (!need_d) D0.t00 = D0.t01 = D0.t10 = D0.t11 = 0.f;
+  orth_T(a.p[(size_t)l * a.ldp + q], &T, need_d ? &D0 : nullptr);
 }
 
 // kind of layer l and whether slot q is active; flags malformed geometry
