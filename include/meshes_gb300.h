@@ -288,6 +288,13 @@ int mg_lossy_backward(int N, int L, int B, int geometry, int seg, const void* x,
                       void* gx, void* gtmp, void* act, void* dT, int ldu, void* ws_fwd, size_t ws_fwd_bytes,
                       void* ws_bwd, size_t ws_bwd_bytes, void* stream);
 
+/* Lossy generic MZI (crossing.py:444-488) on the device, double precision, one thread per slot:
+ * mg_generic_mzi_T: T (complex64, n x [t00, t01, t10, t11]) from p (n x (theta, phi)) and s (n x 14:
+ * alpha, beta, 4 fabrication and 4 crosstalk phase errors, 4 log-gains; NULL = 0).
+ * mg_generic_mzi_T_vjp: dp (n x 2) = Re sum_ij conj(G_ij) dT_ij/dp for G = 2 dJ/dT* (complex64 n x 4). */
+int mg_generic_mzi_T(int n, const double* p, const double* s, void* T, void* stream);
+int mg_generic_mzi_T_vjp(int n, const double* p, const double* s, const void* gT, double* dp, void* stream);
+
 /* ---- measurement helpers -------------------------------------------------------------------- */
 
 /* FP32 FMA throughput probe: `blocks` x `threads` threads each run `iters` iterations of 64

@@ -104,6 +104,8 @@ _SIGS = {
                                  c_size_t, c_void_p]),
     "mg_lossy_backward": (c_int, [c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                   c_void_p, c_void_p, c_int, c_void_p, c_size_t, c_void_p, c_size_t, c_void_p]),
+    "mg_generic_mzi_T": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "mg_generic_mzi_T_vjp": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "mg_fma_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
     "mg_fma2_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
     "mg_trig_check": (c_int, [c_void_p, c_void_p, c_int, c_void_p]),

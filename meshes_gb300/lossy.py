@@ -59,6 +59,32 @@ def mzi_generic_T(p: torch.Tensor, s: Optional[torch.Tensor] = None) -> torch.Te
     return torch.stack([torch.stack([t00, t01], -1), torch.stack([t10, t11], -1)], -2)
 
 
+class GenericMZIT(torch.autograd.Function):
+    """T of the lossy generic MZI from the library's double-precision kernel (complex64 result), with its
+    vector-Jacobian product for the phases p; the splitter/error parameters s are held constant."""
+
+    @staticmethod
+    def forward(ctx, p: torch.Tensor, s: Optional[torch.Tensor]):
+        p64 = p.detach().to(torch.float64).contiguous()
+        s64 = None if s is None else s.detach().to(device=p.device, dtype=torch.float64).contiguous()
+        n = p64.numel() // 2
+        T = torch.empty(p64.shape[:-1] + (2, 2), dtype=torch.complex64, device=p.device)
+        check(load().mg_generic_mzi_T(n, p64.data_ptr(), None if s64 is None else s64.data_ptr(), T.data_ptr(),
+                                      _stream(p.device)), "mg_generic_mzi_T")
+        ctx.save_for_backward(p64, s64 if s64 is not None else p64.new_empty(0))
+        ctx.p_dtype = p.dtype
+        return T
+
+    @staticmethod
+    def backward(ctx, gT: torch.Tensor):
+        p64, s64 = ctx.saved_tensors
+        g = gT.detach().to(torch.complex64).contiguous()
+        dp = torch.empty_like(p64)
+        check(load().mg_generic_mzi_T_vjp(p64.numel() // 2, p64.data_ptr(), s64.data_ptr() if s64.numel() else None,
+                                          g.data_ptr(), dp.data_ptr(), _stream(p64.device)), "mg_generic_mzi_T_vjp")
+        return dp.to(ctx.p_dtype), None
+
+
 class LossyMesh:
     """Geometry of a mesh of generic (possibly lossy) crossings; ``mesh(x, T)`` is y = U(T) x.
 
@@ -153,7 +179,11 @@ class LossyMesh:
 
     # ---- user API
     def T(self, p: torch.Tensor, s: Optional[torch.Tensor] = None) -> torch.Tensor:
-        """Lossy generic-MZI transfer matrices (L, N/2, 2, 2) from p (L, N/2, 2) and s (L, N/2, 14)."""
+        """Lossy generic-MZI transfer matrices (L, N/2, 2, 2) from p (L, N/2, 2) and s (L, N/2, 14):
+        the library kernel (complex64, gradient to p) unless s needs a gradient too, in which case
+        the differentiable tensor formula ``mzi_generic_T`` (complex, dtype of p)."""
+        if p.is_cuda and not (s is not None and s.requires_grad):
+            return GenericMZIT.apply(p, s)
         return mzi_generic_T(p, s)
 
     def __call__(self, x: torch.Tensor, T: torch.Tensor) -> torch.Tensor:

@@ -58,7 +58,11 @@ def test_lossy_forward_and_adjoint(geometry, N, B, segment):
     T = mesh.T(p, s)
     T.retain_grad()
     mask = om.active_mask()
-    assert np.abs(T.detach().cpu().numpy()[mask] - om.T_grid()[mask]).max() < 1e-12
+    # the library's double-precision T, rounded once to complex64
+    assert np.abs(T.detach().cpu().numpy()[mask] - om.T_grid()[mask]).max() < 1.5e-7
+    from meshes_gb300.lossy import mzi_generic_T
+    T128 = mzi_generic_T(p.detach(), s)                     # the differentiable tensor formula
+    assert np.abs(T128.cpu().numpy()[mask] - om.T_grid()[mask]).max() < 1e-12
     x_np = O.unit_columns(rng, N, B)
     t_np = O.unit_columns(rng, N, B)
     x = torch.tensor(x_np.astype(np.complex64), device=dev, requires_grad=True)
