@@ -424,14 +424,27 @@ def from_structured(net, device=None) -> MeshNetworkGPU:
     ``net`` is any object exposing N, L, lens, shifts, grid_phase, grid_splitter, X and perm (the
     reference's StructuredMeshNetwork, ClementsNetwork, ReckNetwork).  Permutation-free only, as in
     the reference; a reference ButterflyNetwork (permutations between adjacent-pair layers) is
-    converted to the equivalent stride geometry instead.
+    converted to the equivalent stride geometry instead.  Unlike the reference, a mesh with a phase
+    screen (is_phase) converts too, and a ClippedNetwork (SquareNetwork, QRNetwork) becomes a
+    ClippedMeshGPU around its converted full mesh.
     """
+    if hasattr(net, "full") and hasattr(net, "idx_in"):     # ClippedNetwork, SquareNetwork, QRNetwork
+        from .clipped import ClippedMeshGPU
+        return ClippedMeshGPU(from_structured(net.full, device), net.idx_in, net.idx_out)
     name = type(net.X).__name__
     X = {"MZICrossing": "mzi", "SymCrossing": "sym"}[name]
     n_p, n_s = _NP_NS[X]
     N, L = int(net.N), int(net.L)
     p = np.nan_to_num(np.asarray(net.grid_phase, dtype=np.float32))
     s = np.nan_to_num(np.asarray(net.grid_splitter, dtype=np.float32))
+    if getattr(net, "is_phase", False):
+        # the phase screen rides along (the reference's gpu() refuses it, gpu/mesh.py:65)
+        if any(x is not None for x in net.perm):
+            raise AssertionError("meshes with permutations are not supported (reference mesh.py:573)")
+        ph = np.asarray(net.phi_out, dtype=np.float32).reshape(-1)
+        return MeshNetworkGPU(N, L, np.array(net.lens), np.array(net.shifts),
+                              np.concatenate([p.reshape(-1), ph]), s if s.size else None, X,
+                              phi_pos=net.phi_pos, is_phase=True, device=device)
     perms = [x for x in net.perm if x is not None]
     if perms:
         if type(net).__name__ != "ButterflyNetwork":

@@ -207,6 +207,31 @@ def main(ref_path):
              dp_dir=flat_to_grid(dp_full[:n_cr * 2], lens, shifts, N, 2), dph_dir=dp_full[n_cr * 2:], dy=dy.T,
              g=g, dJdp=flat_to_grid(dJdp[:n_cr * 2], lens, shifts, N, 2), dJdph=dJdp[n_cr * 2:], g_in=dJdv.T)
 
+    # Clipped meshes (mesh.py:718-802): SquareNetwork and QRNetwork (square.py, qr.py), phase screen on,
+    # random crossing phases, screen phases and splitting errors; ClippedNetwork.dot and grad_L2.
+    from meshes.square import SquareNetwork
+    from meshes.qr import QRNetwork
+    for name, cls in (("squarenet", SquareNetwork), ("qrnet", QRNetwork)):
+        n = 4
+        net = cls(N=n)
+        full = net.full
+        n_cr = full.n_cr
+        full.p_phase[:] = rng.uniform(0, 2 * np.pi, full.p_phase.shape).astype(np.float32).astype(np.float64)
+        full.p_splitter = rng.normal(0, 0.02, (n_cr, 2)).astype(np.float32).astype(np.float64)
+        net.p_phase, net.p_splitter = full.p_phase, full.p_splitter
+        lens, shifts = list(map(int, full.lens)), list(map(int, full.shifts))
+        B = 3
+        x = (rng.standard_normal((n, B)) + 1j * rng.standard_normal((n, B)))
+        y = net.dot(x)
+        Z = rng.standard_normal((net.M, n)) + 1j * rng.standard_normal((net.M, n))
+        J, dJdp = net.grad_L2(Z)
+        save("clipped_%s_N%d" % (name, n), N=full.N, L=full.L, lens=np.array(lens), shifts=np.array(shifts),
+             phi_pos=full.phi_pos, p=flat_to_grid(full.p_crossing, lens, shifts, full.N, 2),
+             ph=full.phi_out, s=flat_to_grid(full.p_splitter, lens, shifts, full.N, 2),
+             idx_in=np.arange(full.N)[net.idx_in], idx_out=np.arange(full.N)[net.idx_out], x=x, y=y, U_target=Z,
+             J=J, dJdp=flat_to_grid(dJdp[:n_cr * 2].reshape(n_cr, 2), lens, shifts, full.N, 2),
+             dJdph=dJdp[n_cr * 2:])
+
     print("wrote", *written, sep="\n  ")
 
 

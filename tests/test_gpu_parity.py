@@ -42,7 +42,8 @@ def to_np(t):
 
 def fixtures():
     """Fixtures of the plain meshes (the phase-screen and lossy fixtures have their own tests)."""
-    return sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz") and "_screen_" not in f and "lossy" not in f)
+    return sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz") and "_screen_" not in f and "lossy" not in f
+                  and not f.startswith("clipped_"))
 
 
 def load_fixture(name):
@@ -409,3 +410,24 @@ def test_coefficient_trigonometry_matches_library():
     out = torch.empty(2 * x.size, dtype=torch.float64, device="cuda")
     assert lib.mg_trig_check(xd.data_ptr(), out.data_ptr(), x.size, torch.cuda.current_stream().cuda_stream) == 0
     assert out.abs().max().item() < 1e-15
+
+
+@pytest.mark.parametrize("name", ["clipped_squarenet_N4.npz", "clipped_qrnet_N4.npz"])
+def test_golden_clipped_mesh(name):
+    """SquareNet and QR meshes (ClippedNetwork, reference mesh.py:718-802) against the reference's own dot
+    and grad_L2 with the phase screen on."""
+    from meshes_gb300 import MeshNetworkGPU
+    from meshes_gb300.clipped import ClippedMeshGPU
+    z = np.load(os.path.join(GOLDEN, name))
+    N, L = int(z["N"]), int(z["L"])
+    full = MeshNetworkGPU(N, L, z["lens"], z["shifts"], np.concatenate([z["p"].reshape(-1), z["ph"]]).astype(np.float32),
+                          z["s"].astype(np.float32), "mzi", phi_pos=str(z["phi_pos"]), is_phase=True)
+    m = ClippedMeshGPU(full, z["idx_in"], z["idx_out"])
+    y = m.dot(torch.tensor(z["x"].astype(np.complex64), device="cuda")).cpu().numpy()
+    assert O.rel_err(y, z["y"]) < TOL
+    J, dp = m.grad_L2(z["U_target"])
+    assert abs(J - float(z["J"])) < 1e-5 * float(z["J"])
+    ncp = L * (N // 2) * 2
+    dp = dp.cpu().numpy()
+    assert O.rel_err(dp[:ncp].reshape(L, N // 2, 2), z["dJdp"]) < TOL
+    assert O.rel_err(dp[ncp:], z["dJdph"]) < TOL

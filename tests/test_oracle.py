@@ -15,7 +15,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def fixtures():
     """Fixtures of the plain meshes (the phase-screen and lossy fixtures have their own tests)."""
-    return sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz") and "_screen_" not in f and "lossy" not in f)
+    return sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz") and "_screen_" not in f and "lossy" not in f
+                  and not f.startswith("clipped_"))
 
 
 def load(name):
@@ -194,6 +195,30 @@ def test_phase_screen_matches_reference_fixtures(pos):
     assert O.rel_err(dp, f["dJdp"]) < 1e-12
     assert O.rel_err(dph, f["dJdph"]) < 1e-12
     assert O.rel_err(gin, f["g_in"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["clipped_squarenet_N4.npz", "clipped_qrnet_N4.npz"])
+def test_clipped_mesh_matches_reference_fixtures(name):
+    """ClippedNetwork semantics (mesh.py:718-802): embed the inputs at idx_in, propagate the full mesh
+    (phase screen on), keep idx_out; grad_L2 of ||U[idx_out] - U_t||^2."""
+    f = np.load(os.path.join(GOLDEN, name))
+    pos = str(f["phi_pos"])
+    om = O.OracleMesh(N=int(f["N"]), L=int(f["L"]), crossing="mzi", lens=list(f["lens"]), shifts=list(f["shifts"]),
+                      p=f["p"], s=f["s"])
+    Nf, n_in = int(f["N"]), len(f["idx_in"])
+    X = np.zeros((f["x"].shape[1], Nf), complex)
+    X[:, f["idx_in"]] = f["x"].T
+    y = O.propagate_screened(om, X, f["ph"], pos)[:, f["idx_out"]].T
+    assert O.rel_err(y, f["y"]) < 1e-13
+    E = np.zeros((n_in, Nf), complex)
+    E[np.arange(n_in), f["idx_in"]] = 1
+    U = O.propagate_screened(om, E, f["ph"], pos)                  # rows: U[:, idx_in[k]]
+    dU = U[:, f["idx_out"]].T - f["U_target"]
+    assert abs(np.sum(np.abs(dU) ** 2) - float(f["J"])) < 1e-12 * float(f["J"])
+    G = np.zeros_like(U)
+    G[:, f["idx_out"]] = 2 * dU.T
+    dp, dph, _ = O.grad_screened(om, U, G, f["ph"], pos)
+    assert O.rel_err(dp, f["dJdp"]) < 1e-12 and O.rel_err(dph, f["dJdph"]) < 1e-12
 
 
 def test_geometry_helpers_agree():
