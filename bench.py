@@ -556,7 +556,7 @@ def run_c4(args):
 
 def run_lossy(args):
     """Lossy generic MZIs (phase errors and gains g_ij; reference crossing.py:444-488) on the Clements
-    N=256 L=256 mesh, B=4096: forward + adjoint through LossyMesh (inputs checkpointed every 16 layers,
+    N=256 L=256 mesh, B=4096: forward + adjoint through LossyMesh (inputs checkpointed per segment,
     each segment recomputed and back-propagated from stored layer inputs), J = sum |y - y_t|^2."""
     import torch
     from meshes_gb300 import geometry as gm
@@ -601,7 +601,7 @@ def run_lossy(args):
                       "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
                       "data": "synthetic (seeded)",
                       "config": {"workload": "clements_lossy_mzi_N256_L256_B4096_fwd+bwd", "segment": mesh.segment_for(B),
-                                 "includes": "T(p) in float64 torch ops and its autograd; per segment a forward "
+                                 "includes": "T(p) and its phase VJP (library kernels); per segment a forward "
                                              "launch, then a recompute, a stored back-propagation and a reduce"},
                       "status": mesh.status()}))
 
