@@ -366,6 +366,21 @@ def run_ours(args, rank, world, local_rank):
     bwd_kernel()
     t_bwd = statistics.median(timed(bwd_kernel, max(5, args.steps)))
     t_fwd = statistics.median(timed(fwd_kernel, max(5, args.steps)))
+    # forward-mode derivative (the reference's fwddiff: y and dy along a direction of all phases)
+    wsb_d = lib.mg_workspace_bytes(1, N, L, B, 0, 0, None)
+    ws_d = torch.empty(wsb_d, dtype=torch.uint8, device=dev)
+    _lib.check(lib.mg_workspace_init(ws_d.data_ptr(), wsb_d, st), "mg_workspace_init")
+    dp_dir = torch.randn(L * N // 2 * 2, dtype=torch.float32, device=dev)
+    _lib.check(lib.mg_build_tiles(1, N, L, 0, lens_d.data_ptr(), shifts_d.data_ptr(), None, 0, p_d.data_ptr(), ldp,
+                                  s_d.data_ptr(), lds, dp_dir.data_ptr(), None, None, B, None, ws_d.data_ptr(), wsb_d,
+                                  st), "mg_build_tiles")
+    dy = torch.empty_like(x)
+
+    def fwddiff_kernel():
+        _lib.check(lib.mg_propagate(1, N, L, B, 0, 0, x.data_ptr(), None, y.data_ptr(), dy.data_ptr(), N, None, 0, 0,
+                                    None, ws_d.data_ptr(), wsb_d, st), "mg_propagate")
+
+    t_fwddiff = statistics.median(timed(fwddiff_kernel, max(5, args.steps // 4)))
     # FP32 FMA peak of this device (the measured-peaks file has HBM and bf16 only)
     props = torch.cuda.get_device_properties(dev)
     sink = torch.empty(props.multi_processor_count * 4 * 256, device=dev)
@@ -406,7 +421,8 @@ def run_ours(args, rank, world, local_rank):
         "step": "programmed mesh: mg_build_tiles(bwd) + mg_propagate(fwd from bwd tiles) + mg_propagate_l2",
         "drop_in_step": {"ms": t_dropin * 1e3, "mzi_per_s": units / world / t_dropin,
                          "path": "mg_fwdprop + 2(y - y_t) + mg_backdiff (reference-shaped entry points)"},
-        "kernels": {"fwd_prop_ms": t_fwd * 1e3, "bwd_prop_ms": t_bwd * 1e3,
+        "kernels": {"fwd_prop_ms": t_fwd * 1e3, "bwd_prop_ms": t_bwd * 1e3, "fwddiff_prop_ms": t_fwddiff * 1e3,
+                    "fwddiff_mzi_per_s": n_mzi * B / t_fwddiff,
                     "fwd_mzi_per_s": n_mzi * B / t_fwd, "bwd_mzi_per_s": n_mzi * B / t_bwd},
         "roofline": {"kernel": "prop_kernel<BWD> (back-propagation)", "bound": "fp32", "achieved": achieved / 1e12,
                      "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / peak,
