@@ -18,6 +18,7 @@ and in any mix.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes
 import threading
 import time
@@ -122,6 +123,9 @@ class MeshServer:
         self.waiter = threading.Thread(target=self._wait_loop, args=(h,), name="mesh-server-completions",
                                        daemon=True)
         self.waiter.start()
+        # a server still running at interpreter exit is stopped (its scheduler thread joined) before CUDA
+        # tears the context down
+        atexit.register(self.stop, False, 5.0)
 
     def stop(self, drain: bool = True, timeout: float = 60.0):
         """Stop the server; with drain, finish every queued and in-flight request first."""

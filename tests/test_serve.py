@@ -103,6 +103,7 @@ def test_admission_by_memory_and_bad_requests():
         srv.stop()
 
 
+@pytest.mark.filterwarnings("ignore::pytest.PytestUnhandledThreadExceptionWarning")   # the crash is the point
 def test_client_thread_dying_midway_leaves_the_loop_draining():
     from meshes_gb300.serve import MeshServer
     rng = np.random.default_rng(43)
