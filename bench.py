@@ -276,6 +276,25 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.synchronize(dev)
         return [a.elapsed_time(b) * 1e-3 for a, b in evs]
 
+    if args.profile and args.bwd_config:
+        # three back-propagation launches with an explicit tile configuration (M,V,W,CL,S,split), for ncu
+        # comparisons of configurations (e.g. -k regex:prop -s 1 -c 1)
+        cfg = _lib.config(*[int(v) for v in args.bwd_config.split(",")])
+        nb = lib.mg_workspace_bytes(2, N, L, B, 0, 0, _lib.cfg_ptr(cfg))
+        if nb == 0:
+            raise SystemExit("invalid configuration: " + _lib.last_error())
+        ws_c = torch.empty(nb, dtype=torch.uint8, device=dev)
+        _lib.check(lib.mg_workspace_init(ws_c.data_ptr(), nb, st), "mg_workspace_init")
+        _lib.check(lib.mg_build_tiles(2, N, L, 0, lens_d.data_ptr(), shifts_d.data_ptr(), None, 0, p_d.data_ptr(), ldp,
+                                      s_d.data_ptr(), lds, None, None, None, B, _lib.cfg_ptr(cfg), ws_c.data_ptr(), nb,
+                                      st), "mg_build_tiles")
+        for _ in range(3):
+            _lib.check(lib.mg_propagate(2, N, L, B, 0, 0, x.data_ptr(), yt.data_ptr(), None, gin.data_ptr(), N,
+                                        dp.data_ptr(), ldp, 0, _lib.cfg_ptr(cfg), ws_c.data_ptr(), nb, st),
+                       "mg_propagate")
+        torch.cuda.synchronize(dev)
+        print(json.dumps({"profile_bwd_config": args.bwd_config, "status": lib.mg_read_status(ws_c.data_ptr(), 0, st)}))
+        return
     if args.profile:
         # one warm-up step and one profiled step, no timing (for ncu captures: -s 2 -c 2 on prop_kernel)
         step(x, yt)
@@ -813,6 +832,8 @@ def main():
                          "c4: N=128 unitary fitting with Adam; lossy: checkpointed adjoint of lossy MZIs")
     ap.add_argument("--duration", type=float, default=10.0, help="serve workload: seconds of traffic")
     ap.add_argument("--meshes", type=int, default=512, help="batched workload: number of meshes")
+    ap.add_argument("--bwd-config", default="", help="with --profile: back-propagation launches with tile "
+                                                    "configuration M,V,W,CL,S,split only")
     ap.add_argument("--rate", type=float, default=20000.0, help="serve workload: offered requests per second")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
