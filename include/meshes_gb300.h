@@ -40,6 +40,9 @@ extern "C" {
 #define MG_OP_BWD_STORED 4     /* back-propagation from stored layer inputs (lossy crossings) */
 #define MG_GEO_NN 0
 #define MG_GEO_FFT 1
+/* OR-ed into a geometry: the mesh has permutations between layers (mg_build_perms).  Plans made with
+ * it reserve the permutation tables in the workspace and a gather scratch in shared memory. */
+#define MG_GEO_PERM 4
 
 /* return codes */
 #define MG_OK 0
@@ -152,6 +155,20 @@ int mg_build_tiles(int op, int N, int L, int geometry, const int* lens, const in
 int mg_propagate(int op, int N, int L, int B, int crossing, int geometry, const void* in0, const void* in1, void* out0,
                  void* out1, int ldu, float* dp, int ldp, int accumulate, const mg_config* cfg, void* workspace,
                  size_t workspace_bytes, void* stream);
+
+/* ---- permutations between layers (the reference's StructuredMeshNetwork.perm, mesh.py:238-277, applied
+ * as c/dot.cpp:29-40,150-153,289-292 does; its GPU API forbids them, mesh.py:573) ---------------------
+ * With geometry | MG_GEO_PERM, mg_build_perms writes the gather tables of `perms` into a workspace planned
+ * for the same (op, N, L, B, crossing, geometry, cfg): perms is (L+1) x N int32 on the device, row l
+ * gathered before layer l and row L after the last layer (new[q] = old[perms[l][q]]), or NULL for none.
+ * Call it after mg_build_tiles (which resets the tables to the identity on such a workspace).
+ * Every later mg_propagate on that workspace applies them; back-propagation goes through the inverse
+ * permutations in reverse order (the reference's perms_bk, mesh.py:382).  A row that is not a permutation
+ * of 0..N-1 records MG_ST_BAD_GEOMETRY and acts as the identity.  Permuted meshes run their own kernel
+ * instantiations (runtime lane groups, default V per (op, M), no split launch, at most 4096 layers); layer
+ * ranges, stored activations, the batched engine and the server take no permutations. */
+int mg_build_perms(int op, int N, int L, int B, int crossing, int geometry, const int* perms, const mg_config* cfg,
+                   void* workspace, size_t workspace_bytes, void* stream);
 
 /* Plan of one launch (for hosts that manage tiles themselves, e.g. the batched engine). */
 typedef struct mg_plan_info {

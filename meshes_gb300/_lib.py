@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libmeshes_gb300.so")
 MZI, SYM, ORTH, GENERIC = 0, 1, 2, 3
 OP_FWD, OP_FWDDIFF, OP_BWD, OP_FWD_BWDTILES, OP_BWD_STORED = 0, 1, 2, 3, 4
 GEO_NN, GEO_FFT = 0, 1
+GEO_PERM = 4          # OR-ed into a geometry: permutations between layers (mg_build_perms)
 CROSSING_CODES = {"mzi": MZI, "sym": SYM, "orth": ORTH, "generic": GENERIC}
 STATUS_NAMES = {0: "ok", 1: "timeout", 2: "bad geometry", 3: "bad work item"}
 
@@ -81,6 +82,8 @@ _SIGS = {
                                c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_size_t, c_void_p]),
     "mg_build_tiles": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int,
                                c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_int, POINTER(mg_config), c_void_p,
+                               c_size_t, c_void_p]),
+    "mg_build_perms": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, POINTER(mg_config), c_void_p,
                                c_size_t, c_void_p]),
     "mg_propagate": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
                              c_void_p, c_int, c_int, POINTER(mg_config), c_void_p, c_size_t, c_void_p]),

@@ -33,7 +33,7 @@ class _Plan:
 
     def workspace(self, B: int):
         m = self.mesh
-        nb = load().mg_workspace_bytes(self.op, m.N, m.L, B, m.crossing, m.geometry,
+        nb = load().mg_workspace_bytes(self.op, m.N, m.L, B, m.crossing, m.geo_code,
                                        _lib.cfg_ptr(m.config.get(self.op)))
         if nb == 0:
             check(-1, "mg_workspace_bytes")
@@ -60,10 +60,13 @@ def _build(mesh: MeshNetworkGPU, op: int, p: torch.Tensor, B: int):
     s = mesh.p_splitter
     geo = ((None, None, mesh.strides.data_ptr()) if mesh.strides is not None
            else (mesh.lens.data_ptr(), mesh.shifts.data_ptr(), None))
-    check(lib.mg_build_tiles(op, mesh.N, mesh.L, mesh.geometry, *geo, mesh.crossing, p.data_ptr(),
+    check(lib.mg_build_tiles(op, mesh.N, mesh.L, mesh.geo_code, *geo, mesh.crossing, p.data_ptr(),
                              mesh.N // 2 * mesh.X_np, s.data_ptr() if s.numel() else None, mesh.N // 2 * mesh.X_ns,
                              None, None, None, B, _lib.cfg_ptr(mesh.config.get(op)), ws, nb, _stream(mesh.device)),
           "mg_build_tiles")
+    if mesh.perm_table is not None:
+        check(lib.mg_build_perms(op, mesh.N, mesh.L, B, mesh.crossing, mesh.geo_code, mesh.perm_table.data_ptr(),
+                                 _lib.cfg_ptr(mesh.config.get(op)), ws, nb, _stream(mesh.device)), "mg_build_perms")
     return ws, nb, plan_.version
 
 
@@ -85,7 +88,7 @@ class MeshFunction(torch.autograd.Function):
         else:
             ws, nb, ver = _build(mesh, OP_FWD, p, B)
             op, cfg = OP_FWD, mesh.config.get(OP_FWD)
-        check(lib.mg_propagate(op, N, mesh.L, B, mesh.crossing, mesh.geometry, x.data_ptr(), None, y.data_ptr(),
+        check(lib.mg_propagate(op, N, mesh.L, B, mesh.crossing, mesh.geo_code, x.data_ptr(), None, y.data_ptr(),
                                None, N, None, 0, 0, _lib.cfg_ptr(cfg), ws, nb, _stream(mesh.device)), "mg_propagate")
         ctx.mesh = mesh
         ctx.tiles_version = ver if shared else None
@@ -106,7 +109,7 @@ class MeshFunction(torch.autograd.Function):
             ws, nb, _ = _build(mesh, OP_BWD, p, B)
         gx = torch.empty_like(gy)
         dp = torch.empty(p.numel(), dtype=torch.float32, device=y.device)
-        check(lib.mg_propagate(OP_BWD, N, mesh.L, B, mesh.crossing, mesh.geometry, y.data_ptr(), gy.data_ptr(), None,
+        check(lib.mg_propagate(OP_BWD, N, mesh.L, B, mesh.crossing, mesh.geo_code, y.data_ptr(), gy.data_ptr(), None,
                                gx.data_ptr(), N, dp.data_ptr(), N // 2 * mesh.X_np, 0,
                                _lib.cfg_ptr(mesh.config.get(OP_BWD)), ws, nb, _stream(mesh.device)), "mg_propagate")
         return gx, dp.view_as(p), None

@@ -37,6 +37,8 @@ def plan(op, N, L, B, crossing, geometry, cfg=None) -> mg_plan_info:
 
 
 def kernel_class(mesh: MeshNetworkGPU) -> int:
+    if getattr(mesh, "perm_table", None) is not None:
+        raise ValueError("batched meshes take no permutations between layers")
     if mesh.X == "orth":
         if mesh.N > 256:
             raise ValueError("orth meshes in a batch are limited to N <= 256")

@@ -53,6 +53,7 @@ batched_kernel(const mg_batch_mesh* __restrict__ meshes, int n_meshes, const mg_
     a.status = status;
     a.v0 = it.v0; a.vend = it.vend;
     a.target = nullptr;
+    a.perm = a.pflags = a.perm_last = a.pflag_last = nullptr;   // batched meshes carry no permutations
     switch (md.cls) {
       case MG_BCLS_C8: prop_body<OP, 8, 4, false, 0, (OP == OP_BWD ? 1 : 0)>(a, smem); break;
       case MG_BCLS_C16: prop_body<OP, 16, 2, false, 0, (OP == OP_BWD ? 1 : 0)>(a, smem); break;

@@ -110,7 +110,19 @@ struct Plan {
   unsigned lb, dlb;
   size_t smem;
   size_t off_kinds, off_tiles, off_dtiles, off_partial, total;
+  bool perm;        // MG_GEO_PERM: permutation tables at off_perm, gather scratch after the smem layout
+  size_t off_perm;
 };
+
+// Permutation tables in the workspace: forward rows [L+1][N], back-propagation rows [L+1][N], forward
+// flags [L+1], back-propagation flags [L+1] (int32).
+size_t perm_table_bytes(int N, int L) { return 4 * (2 * (size_t)(L + 1) * N + 2 * (size_t)(L + 1)); }
+
+// Shared memory of a launch of plan P over L layers, with the permutation scratch when P has one.
+size_t launch_smem(const Plan& P, int op, int gslot, int L) {
+  const size_t b = prop_smem_bytes(op, gslot, P.M, P.G, P.W, P.CL, P.S, P.lb, P.dlb, L);
+  return P.perm ? perm_scratch_offset(b) + perm_scratch_bytes(P.W, P.M, P.real) : b;
+}
 
 // (M, V) instantiated for the stored-activation kernels (GR 4), by op (FWD writes, BWD reads)
 bool instantiated_stored(int op, int M, int V) {
@@ -135,15 +147,21 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
     return fail(MG_E_ARG, "op %d not in {0,1,2,4}", op);
   }
   if (crossing < 0 || crossing > 3) return fail(MG_E_ARG, "crossing %d not in {0,1,2,3}", crossing);
-  if (geometry < 0 || geometry > 1) return fail(MG_E_ARG, "geometry %d not in {0,1}", geometry);
+  const bool perm = geometry >= 0 && (geometry & MG_GEO_PERM) != 0;
+  if (perm) geometry &= ~MG_GEO_PERM;
+  if (geometry < 0 || geometry > 1) return fail(MG_E_ARG, "geometry %d not in {0,1} (| MG_GEO_PERM)", geometry);
   if (N < 2 || N % 2) return fail(MG_E_ARG, "N=%d must be even and >= 2 (reference gpu/mesh.py:67)", N);
   if (N > 512) return fail(MG_E_ARG, "N=%d above the supported maximum 512", N);
   if (L < 0 || B < 0) return fail(MG_E_ARG, "L=%d, B=%d must be non-negative", L, B);
+  // the permutation flags travel in the shared-memory copy of the layer kinds
+  if (perm && L > kMaxSmemKinds) return fail(MG_E_ARG, "permuted meshes take at most %d layers", kMaxSmemKinds);
   const DevInfo di = dev_info();
   mg_config tuned;
-  if (!cfg && lookup_tuned(op, crossing, geometry, N, B, &tuned)) cfg = &tuned;
+  // tuned entries were measured without the permutation scratch: permuted meshes take the defaults
+  if (!cfg && !perm && lookup_tuned(op, crossing, geometry, N, B, &tuned)) cfg = &tuned;
   Plan& p = *P;
   p.op = op; p.N = N; p.L = L; p.B = B; p.crossing = crossing; p.geometry = geometry;
+  p.perm = perm;
   p.real = crossing == CR_ORTH;
   p.gr = stored ? 4 : (op != OP_BWD) ? 0 : (crossing == CR_MZI ? 1 : (crossing == CR_ORTH ? 2 : 0));
   const int Np = pow2ceil(N);
@@ -157,8 +175,11 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
     static const int vd[3][5] = {{8, 8, 4, 2, 0}, {4, 4, 2, 1, 0}, {4, 4, 4, 2, 0}};   // by ilog2(M)-1
     V = stored ? stored_default_v(OP_BWD, M) : vd[op][ilog2(M) - 1];
   }
-  if (stored ? !instantiated_stored(OP_BWD, M, V) : !instantiated(op, M, V))
-    return fail(MG_E_CONFIG, "no kernel instantiated for op=%d M=%d V=%d", stored ? MG_OP_BWD_STORED : op, M, V);
+  if (perm && stored) return fail(MG_E_ARG, "stored-activation back-propagation takes no permutations");
+  if (perm ? !perm_instantiated(op, crossing == CR_ORTH, M, V, p.gr)
+           : (stored ? !instantiated_stored(OP_BWD, M, V) : !instantiated(op, M, V)))
+    return fail(MG_E_CONFIG, "no %skernel instantiated for op=%d M=%d V=%d", perm ? "permuted-mesh " : "",
+                stored ? MG_OP_BWD_STORED : op, M, V);
   p.M = M; p.V = V; p.G = G; p.logG = ilog2(G); p.R = 32 / G; p.np2 = G * M / 2;
   // split launch: when one wave of uniform CTAs cannot cover the SMs evenly (B between SMs x 4 warps x V
   // and SMs x 4 warps x (2V-1) vectors), run two 4-warp CTAs per SM holding V and V-1 vectors per lane
@@ -169,7 +190,7 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   const int split_mode = cfg ? cfg->split : 0;
   p.split = false;
   p.nA = 0;
-  if (split_mode != 2 && (op == OP_FWD || op == OP_BWD) && V >= 2 && !stored &&
+  if (split_mode != 2 && (op == OP_FWD || op == OP_BWD) && V >= 2 && !stored && !perm &&
       split_instantiated(op, crossing == CR_ORTH, M, V, G == 32, p.gr)) {
     const long ws = (cfg && cfg->W) ? cfg->W : 4;
     const long capA = ws * p.R * V, capB = ws * p.R * (V - 1);
@@ -200,7 +221,8 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   const size_t budget = p.split ? (size_t)di.smem_per_sm / 2 - 1024 : (size_t)di.smem_optin - 1024;
   int CL = (cfg && cfg->CL) ? cfg->CL : 0;
   const size_t per_layer = (size_t)S * p.lb + p.dlb + W * gstl;
-  const size_t fixed = 8 * (size_t)(S + 1) + (L <= kMaxSmemKinds ? 4 * (size_t)L : 0);
+  const size_t fixed = 8 * (size_t)(S + 1) + (L <= kMaxSmemKinds ? 4 * (size_t)L : 0) +
+                       (perm ? 16 + perm_scratch_bytes(W, M, p.real) : 0);
   if (!CL) {
     // forward: deep enough to hide the copies, shallow enough to start soon (split CTAs: about 68 KB measured best)
     const size_t target = (op == OP_BWD) ? budget : std::min<size_t>(budget, (p.split ? 68 : 160) * 1024);
@@ -209,7 +231,7 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   }
   if (CL < 1) return fail(MG_E_CONFIG, "CL=%d", CL);
   p.W = W; p.S = S; p.CL = CL;
-  p.smem = prop_smem_bytes(op, gslot, M, G, W, CL, S, p.lb, p.dlb, L);
+  p.smem = launch_smem(p, op, gslot, L);
   if (p.smem > budget)
     return fail(MG_E_CONFIG, "shared memory %zu B above the %zu B available (M=%d W=%d CL=%d S=%d)", p.smem, budget, M,
                 W, CL, S);
@@ -228,7 +250,8 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   p.off_kinds = 256;
   p.off_tiles = p.off_kinds + align256((size_t)std::max(L, 1) * 12);   // kinds + (shift, len)
   p.off_dtiles = p.off_tiles + align256((size_t)L * p.lb);
-  p.off_partial = p.off_dtiles + align256((size_t)L * p.dlb);
+  p.off_perm = p.off_dtiles + align256((size_t)L * p.dlb);
+  p.off_partial = p.off_perm + (perm ? align256(perm_table_bytes(N, L)) : 0);
   p.total = p.off_partial + ((op == OP_BWD) ? align256((size_t)p.grid * L * p.np2 * (p.gr == 4 ? 32 : 8)) : 0);
   return MG_OK;
 }
@@ -285,6 +308,24 @@ int build_tiles(const Plan& P, const int* lens, const int* shifts, const int* st
   return e == cudaSuccess ? MG_OK : cuda_fail(e, "coef_kernel launch");
 }
 
+// Permutation arguments of a launch over layers [l0, l1) of plan P (the launch's layer i is layer l0 + i):
+// forward kinds gather forward row l before layer l and row L after layer L-1 (only when the range
+// ends there); back-propagation gathers row l (the inverse of perms[l+1]) before its step through layer
+// l and row L (the inverse of perms[0]) after layer 0 (only when the range starts there).
+void set_perm_args(const Plan& P, unsigned char* ws, int l0, int l1, PropArgs& a) {
+  a.perm = a.pflags = a.perm_last = a.pflag_last = nullptr;
+  if (!P.perm) return;
+  const bool bwd = P.op == OP_BWD;
+  const int* tab = reinterpret_cast<const int*>(ws + P.off_perm) + (bwd ? (size_t)(P.L + 1) * P.N : 0);
+  const int* flags = reinterpret_cast<const int*>(ws + P.off_perm) + 2 * (size_t)(P.L + 1) * P.N + (bwd ? P.L + 1 : 0);
+  a.perm = tab + (size_t)l0 * P.N;
+  a.pflags = flags + l0;
+  if (bwd ? l0 == 0 : l1 == P.L) {
+    a.perm_last = tab + (size_t)P.L * P.N;
+    a.pflag_last = flags + P.L;
+  }
+}
+
 int run_prop(const Plan& P, const void* in0, const void* in1, void* out0, void* out1, int ldu, float* dp, int ldp,
              int accumulate, unsigned char* ws, cudaStream_t st, const void* target = nullptr) {
   if (P.B == 0) return MG_OK;
@@ -300,6 +341,7 @@ int run_prop(const Plan& P, const void* in0, const void* in1, void* out0, void* 
   a.in0 = in0; a.in1 = in1; a.out0 = out0; a.out1 = out1;
   a.partial = reinterpret_cast<float2*>(ws + P.off_partial);
   a.status = reinterpret_cast<int*>(ws);
+  set_perm_args(P, ws, 0, P.L, a);
   LaunchCfg lc;
   lc.grid = dim3(P.grid);
   lc.block = dim3(32 * P.W);
@@ -397,6 +439,55 @@ int backdiff_impl(int geo, int N, int L, int B, const int* lens, const int* shif
   }
   TRY(build_tiles(P, lens, shifts, strides, p, ldp, s, lds, nullptr, nullptr, nullptr, w, st));
   return run_prop(P, u_out, dJdu_out, u_in, dJdu_in, ldu, dp, ldp, accumulate, w, st);
+}
+
+// Gather tables of the reference's perms ((L+1) x N, row k gathered before layer k, row L after the
+// last layer), one block per row k: forward row k = perms[k]; back-propagation row k-1 (row L for k = 0)
+// = the inverse of perms[k], so that the backward step through layer l is preceded by the inverse of
+// perms[l+1] and the last one is the inverse of perms[0] (mesh.py:381-390 with perms_bk = argsort(perms)).
+// Flags mark rows that move something.  A row that is not a permutation of 0..N-1 becomes the identity
+// and records bad geometry.
+__global__ void perm_build_kernel(int N, int L, const int* __restrict__ perms, int* fwd, int* bwd, int* fflags,
+                                  int* bflags, int* status) {
+  __shared__ int hits[512];
+  __shared__ int bad, moved;
+  const int k = blockIdx.x;
+  const int* row = perms + (size_t)k * N;
+  if (threadIdx.x == 0) {
+    bad = 0;
+    moved = 0;
+  }
+  for (int q = threadIdx.x; q < N; q += blockDim.x) hits[q] = 0;
+  __syncthreads();
+  for (int q = threadIdx.x; q < N; q += blockDim.x) {
+    const int t = row[q];
+    if ((unsigned)t < (unsigned)N) atomicAdd(&hits[t], 1);
+    else atomicOr(&bad, 1);
+    if (t != q) atomicOr(&moved, 1);
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < N; q += blockDim.x)
+    if (hits[q] != 1) atomicOr(&bad, 1);
+  __syncthreads();
+  const int kb = (k == 0) ? L : k - 1;
+  int* f = fwd + (size_t)k * N;
+  int* b = bwd + (size_t)kb * N;
+  for (int q = threadIdx.x; q < N; q += blockDim.x) {
+    if (bad) {
+      f[q] = q;
+      b[q] = q;
+    } else {
+      const int t = row[q];
+      f[q] = t;
+      b[t] = q;
+    }
+  }
+  if (threadIdx.x == 0) {
+    const int fl = (!bad && moved) ? 1 : 0;
+    fflags[k] = fl;
+    bflags[kb] = fl;
+    if (bad) set_status(status, ST_BAD_GEOMETRY);
+  }
 }
 
 __global__ void fma_probe_kernel(float* sink, int iters, float m) {
@@ -549,6 +640,11 @@ int mg_build_tiles(int op, int N, int L, int geometry, const int* lens, const in
   TRY(check_params(P, p, ldp, s, lds, Tgen));
   if (crossing == CR_GENERIC && op == OP_BWD && !Dgen && L > 0) return fail(MG_E_ARG, "generic back-prop needs Dgen");
   if (crossing == CR_GENERIC && op == OP_FWDDIFF) return fail(MG_E_ARG, "generic crossings support fwd and bwd only");
+  if (P.perm) {   // no permutation until mg_build_perms writes the tables
+    cudaError_t e = cudaMemsetAsync(static_cast<unsigned char*>(ws) + P.off_perm + 8 * (size_t)(L + 1) * N, 0,
+                                    8 * (size_t)(L + 1), static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(permutation flags)");
+  }
   return build_tiles(P, lens, shifts, strides, p, ldp, s, lds, dp, Tgen, Dgen, static_cast<unsigned char*>(ws),
                      static_cast<cudaStream_t>(stream));
 }
@@ -560,7 +656,8 @@ int mg_propagate(int op, int N, int L, int B, int crossing, int geometry, const 
   if (op == MG_OP_FWD_BWDTILES) {
     // forward propagation reading the tiles mg_build_tiles(MG_OP_BWD) wrote: the layer stride and the
     // workspace layout are the back-propagation plan's, the kernel is the forward one
-    if (geometry != GEO_NN) return fail(MG_E_ARG, "forward from back-propagation tiles needs nearest-neighbour geometry");
+    if ((geometry & ~MG_GEO_PERM) != GEO_NN)
+      return fail(MG_E_ARG, "forward from back-propagation tiles needs nearest-neighbour geometry");
     Plan Pb, Pf;
     TRY(make_plan(OP_BWD, N, L, B, crossing, geometry, cfg, &Pb));
     TRY(check_ws(Pb, ws, wsb));
@@ -569,10 +666,11 @@ int mg_propagate(int op, int N, int L, int B, int crossing, int geometry, const 
     Pf.lb = Pb.lb;
     Pf.off_kinds = Pb.off_kinds;
     Pf.off_tiles = Pb.off_tiles;
+    Pf.off_perm = Pb.off_perm;   // the forward rows of the tables mg_build_perms wrote for this workspace
     const DevInfo di = dev_info();
     const size_t budget = Pf.split ? (size_t)di.smem_per_sm / 2 - 1024 : (size_t)di.smem_optin - 1024;
     for (;;) {
-      Pf.smem = prop_smem_bytes(OP_FWD, 0, Pf.M, Pf.G, Pf.W, Pf.CL, Pf.S, Pf.lb, 0, L);
+      Pf.smem = launch_smem(Pf, OP_FWD, 0, L);
       if (Pf.smem <= budget && (size_t)Pf.CL * Pf.lb < (1u << 20)) break;
       if (Pf.CL == 1) return fail(MG_E_CONFIG, "no pipeline depth fits shared memory");
       Pf.CL = std::max(1, Pf.CL / 2);
@@ -595,6 +693,32 @@ int mg_propagate(int op, int N, int L, int B, int crossing, int geometry, const 
   if (op == OP_BWD && dp && ldp < N / 2 * crossing_np(crossing)) return fail(MG_E_ARG, "ldp too small");
   return run_prop(P, in0, in1, out0, out1, ldu, dp, ldp, accumulate, static_cast<unsigned char*>(ws),
                   static_cast<cudaStream_t>(stream));
+}
+
+int mg_build_perms(int op, int N, int L, int B, int crossing, int geometry, const int* perms, const mg_config* cfg,
+                   void* ws, size_t wsb, void* stream) {
+  g_err.clear();
+  if (op == MG_OP_FWD_BWDTILES) op = OP_BWD;   // the forward kernel on back-propagation tiles shares their workspace
+  Plan P;
+  TRY(make_plan(op, N, L, B, crossing, geometry, cfg, &P));
+  if (!P.perm) return fail(MG_E_ARG, "geometry %d lacks MG_GEO_PERM", geometry);
+  TRY(check_ws(P, ws, wsb));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned char* w = static_cast<unsigned char*>(ws);
+  int* tab = reinterpret_cast<int*>(w + P.off_perm);
+  int* fwd = tab;
+  int* bwd = tab + (size_t)(L + 1) * N;
+  int* fflags = tab + 2 * (size_t)(L + 1) * N;
+  int* bflags = fflags + (L + 1);
+  cudaError_t e;
+  if (!perms) {
+    e = cudaMemsetAsync(fflags, 0, 2 * sizeof(int) * (size_t)(L + 1), st);
+    return e == cudaSuccess ? MG_OK : cuda_fail(e, "cudaMemsetAsync(permutation flags)");
+  }
+  if (reinterpret_cast<uintptr_t>(perms) & 3) return fail(MG_E_ARG, "perms not 4-byte aligned");
+  perm_build_kernel<<<L + 1, 256, 0, st>>>(N, L, perms, fwd, bwd, fflags, bflags, reinterpret_cast<int*>(w));
+  e = cudaGetLastError();
+  return e == cudaSuccess ? MG_OK : cuda_fail(e, "perm_build_kernel launch");
 }
 
 int mg_set_tuned(int op, int crossing, int geometry, int N, int B_lo, int B_hi, const mg_config* cfg) {
@@ -660,6 +784,7 @@ int mg_propagate_range(int op, int N, int L, int l0, int l1, int B, int crossing
   cfg = &cu;
   Plan P;
   TRY(make_plan(op, N, L, B, crossing, geometry, cfg, &P));
+  if (P.perm) return fail(MG_E_ARG, "layer ranges take no permutations");
   TRY(check_ws(P, ws, wsb));
   TRY(check_ldu(P, ldu));
   const bool bwd = op == MG_OP_BWD_STORED;
@@ -701,7 +826,7 @@ int mg_propagate_range(int op, int N, int L, int l0, int l1, int B, int crossing
   // the launch sees layers [l0, l1) as its own layers [0, nl): tiles and kinds start at l0
   unsigned char* w = static_cast<unsigned char*>(ws);
   const int* kinds_full = reinterpret_cast<const int*>(w + P.off_kinds);
-  P.smem = prop_smem_bytes(P.op, bwd ? 32 : 0, P.M, P.G, P.W, P.CL, P.S, P.lb, P.dlb, nl);
+  P.smem = launch_smem(P, P.op, bwd ? 32 : 0, nl);
   PropArgs a;
   a.target = nullptr;
   a.N = N; a.L = nl; a.B = B; a.ldu = ldu;
@@ -719,6 +844,7 @@ int mg_propagate_range(int op, int N, int L, int l0, int l1, int B, int crossing
   a.act = act;
   a.act_plane = (size_t)B * ldu;
   a.nA = 0;
+  a.perm = a.pflags = a.perm_last = a.pflag_last = nullptr;
   LaunchCfg lc;
   lc.grid = dim3(P.grid);
   lc.block = dim3(32 * P.W);

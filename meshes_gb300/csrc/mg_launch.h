@@ -37,10 +37,10 @@ inline cudaError_t ensure_smem_attr(K kernel, std::atomic<unsigned long long>& d
   return cudaSuccess;
 }
 
-template <int OP, int M, int V, bool REAL, int GT, int GR>
+template <int OP, int M, int V, bool REAL, int GT, int GR, bool PERM = false>
 inline cudaError_t launch_one(const LaunchCfg& lc, const PropArgs& a) {
   static std::atomic<unsigned long long> done{0};
-  auto k = prop_kernel<OP, M, V, REAL, GT, GR>;
+  auto k = prop_kernel<OP, M, V, REAL, GT, GR, PERM>;
   cudaError_t e = ensure_smem_attr(k, done);
   if (e != cudaSuccess) return e;
   k<<<lc.grid, lc.block, lc.smem, lc.stream>>>(a);
@@ -69,6 +69,10 @@ int set_last_error(int code, const char* fmt, ...);
 // full: a vector fills the warp (G = 32), selecting the compile-time-G instantiation;
 // gr: back-propagation gradient mode (0 dJ/dT + dT/dp tiles, 1 MZI direct, 2 orth direct)
 cudaError_t launch_prop(int op, bool real, int M, int V, bool full, int gr, const LaunchCfg& lc, const PropArgs& a);
+// permuted meshes (a.perm set): the PERM instantiations, runtime lane-group size, the default V of each
+// (op, M) and the gradient mode of each crossing (mg_prop_perm_*.cu)
+bool perm_instantiated(int op, bool real, int M, int V, int gr);
+cudaError_t launch_prop_perm(int op, bool real, int M, int V, int gr, const LaunchCfg& lc, const PropArgs& a);
 // split launches (two CTA kinds per SM); instantiated only for the full-warp configurations in
 // split_instantiated()
 bool split_instantiated(int op, bool real, int M, int V, bool full, int gr);

@@ -39,6 +39,8 @@ __host__ __device__ constexpr int ilog2_const(int x) { return x <= 1 ? 0 : 1 + i
 //   KIND_XL + e   : butterfly stride 2^e >= M, partner lane j ^ (2^e / M)
 constexpr int KIND_MIS = 8;
 constexpr int KIND_XL = 16;
+// OR-ed into the shared-memory copy of a layer's kind when a permutation precedes the layer
+constexpr int KIND_PERM = 1 << 12;
 
 struct PropArgs {
   int N, L, B, ldu;
@@ -59,6 +61,13 @@ struct PropArgs {
   void* act;                     // GR 4: per-layer inputs [L][act_plane] (FWD writes them, BWD reads them)
   size_t act_plane;              // elements between the stored inputs of consecutive layers
   int nA;                        // split launch: CTAs [0, nA) hold V vectors per lane group, the rest V-1
+  // permutations between layers (reference mesh.py:44-48, 71-72): before layer l, when pflags[l] != 0,
+  // every vector is gathered through row l of `perm` (N ints: new[q] = old[perm[q]]); after the last
+  // layer through perm_last when *pflag_last != 0.  All null: no permutations.
+  const int* perm;
+  const int* pflags;
+  const int* perm_last;
+  const int* pflag_last;
 };
 
 template <bool REAL> struct Fld { using T = float2; using C = C2x2; };
@@ -390,6 +399,41 @@ __device__ __forceinline__ void layer_any(int kind, const float4* tl, int G, int
   }
 }
 
+// ---- permutation of the modes of every vector: new[q] = old[row[q]] for q < N (padding modes stay),
+// through the lane group's shared-memory scratch of G*M fields (mode-major, scr[m*G + j] = mode j*M+m,
+// so that the writes of a warp hit distinct banks).  Entries outside [0, N) leave their mode in place:
+// the table is validated when it is built, and this keeps every access in bounds regardless.
+template <int M, int V, typename F>
+__device__ __forceinline__ void gather_group(F (&u)[V][M], const int (&src)[M], F* scr, int G, int j) {
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+#pragma unroll
+    for (int m = 0; m < M; ++m) scr[m * G + j] = u[v][m];
+    __syncwarp();
+#pragma unroll
+    for (int m = 0; m < M; ++m) u[v][m] = scr[src[m]];
+    __syncwarp();
+  }
+}
+// SKIP_U: back-propagation from stored activations reloads the field, only the gradient moves
+template <int OP, int M, int V, bool SKIP_U, typename F>
+__device__ __forceinline__ void permute_fields(const int* __restrict__ row, int N, F* scr, int G, int j, F (&u)[V][M],
+                                            F (&w)[V][M]) {
+  int src[M];
+#pragma unroll
+  for (int m = 0; m < M; ++m) {
+    const int q = j * M + m;
+    int t = q;
+    if (q < N) {
+      const int r = __ldg(row + q);
+      if ((unsigned)r < (unsigned)N) t = r;
+    }
+    src[m] = (t & (M - 1)) * G + t / M;
+  }
+  if constexpr (!SKIP_U) gather_group<M, V>(u, src, scr, G, j);
+  if constexpr (OP != OP_FWD) gather_group<M, V>(w, src, scr, G, j);
+}
+
 // ---- field I/O: lane j of the vector's group owns modes [j*M, j*M+M); out-of-range modes read 0
 template <int M, int V, bool REAL, typename F>
 __device__ __forceinline__ void load_fields(F (&u)[V][M], const void* src, int vb0, int B, int N, int ldu, int j) {
@@ -442,6 +486,13 @@ __device__ __forceinline__ void store_fields(const F (&u)[V][M], void* dst, int 
 // Layer kinds are staged in shared memory when L is at most this (else read through the L1 cache).
 constexpr int kMaxSmemKinds = 4096;
 
+// Permutation scratch: it starts at the first 16-byte boundary after the rest of the layout and holds
+// 32*M fields per warp.
+__host__ __device__ inline size_t perm_scratch_offset(size_t end) { return (end + 15) & ~size_t(15); }
+__host__ __device__ inline size_t perm_scratch_bytes(int W, int M, bool real) {
+  return (size_t)W * 32 * M * (real ? 4 : 8);
+}
+
 // Shared-memory footprint of one launch (host and device agree on this layout):
 //   [ring: S*CL*layer_bytes][BWD: dT/dp chunk CL*dlayer_bytes][BWD: per-warp dJ/dT W*CL*Np/2*gslot]
 //   [mbarriers: S+1][layer kinds: L ints when L <= kMaxSmemKinds]
@@ -474,7 +525,7 @@ __device__ __forceinline__ void chunk_reduce(const PropArgs& a, const int* kinds
   for (int idx = threadIdx.x; idx < nl * np2; idx += blockDim.x) {
     const int li = idx / np2, pos = idx - li * np2;
     const int l = lo + li;
-    const int kind = kinds[l];
+    const int kind = kinds[l] & ~KIND_PERM;
     const int e = pos / G, j = pos - e * G;
     int la = j, lb = j, ia, ib, mrow_a = 0, mrow_b = 0;
     const bool xl = kind >= KIND_XL;
@@ -536,7 +587,7 @@ __device__ __forceinline__ void chunk_reduce_direct(const PropArgs& a, const int
   for (int idx = threadIdx.x; idx < nl * np2; idx += blockDim.x) {
     const int li = idx / np2, pos = idx - li * np2;
     const int l = lo + li;
-    const int kind = kinds[l];
+    const int kind = kinds[l] & ~KIND_PERM;
     int sp = pos;
     if (kind >= KIND_XL) {
       const int q = pos_slot(pos, M, G);
@@ -563,7 +614,7 @@ __device__ __forceinline__ void chunk_reduce_raw(const PropArgs& a, const int* k
   for (int idx = threadIdx.x; idx < nl * np2; idx += blockDim.x) {
     const int li = idx / np2, pos = idx - li * np2;
     const int l = lo + li;
-    const int kind = kinds[l];
+    const int kind = kinds[l] & ~KIND_PERM;
     const int e = pos / G, j = pos - e * G;
     int la = j, lb = j, ia = 2 * e, ib = 2 * e + 1;
     const bool xl = kind >= KIND_XL;
@@ -598,10 +649,14 @@ struct PropTraits {
 // straight-line block (the compiler interleaves the two layers' crossings); other kinds one by one.
 // GR 4 (stored activations, for lossy crossings) goes layer by layer: the forward pass writes each
 // layer's input to a.act before applying it, back-propagation reloads it in place of T^H reconstruction.
-template <int OP, int M, int V, bool REAL, int GR, typename F>
+// PERM (the permuted-mesh instantiations): a layer whose kind carries KIND_PERM is preceded by the gather of
+// its row of pa.perm (the shared-memory copy of the kinds carries the flags).
+template <int OP, int M, int V, bool REAL, int GR, bool PERM, typename F>
 __device__ __forceinline__ void run_chunk(const PropArgs& pa, int vb0, const int* kinds, const unsigned char* st,
                                           unsigned layer_bytes, int lo, int hi, unsigned char* gst_warp,
-                                          size_t gst_layer, int G, int j, int r, F (&u)[V][M], F (&w)[V][M]) {
+                                          size_t gst_layer, int G, int j, int r, F (&u)[V][M], F (&w)[V][M],
+                                          F* pscr) {
+  static_assert(!(PERM && GR == 4), "stored-activation kernels take no permutations");
   const int nl = hi - lo;
   if constexpr (GR == 4) {
     for (int i = 0; i < nl; ++i) {
@@ -617,9 +672,15 @@ __device__ __forceinline__ void run_chunk(const PropArgs& pa, int vb0, const int
   int i = 0;
   while (i < nl) {
     const int l0 = (OP == OP_BWD) ? (hi - 1 - i) : (lo + i);
-    const int k0 = kinds[l0];
+    int k0 = kinds[l0];
     const float4* t0 = reinterpret_cast<const float4*>(st + (size_t)(l0 - lo) * layer_bytes);
     float4* g0 = reinterpret_cast<float4*>(gst_warp + (size_t)(l0 - lo) * gst_layer);
+    if constexpr (PERM) {
+      if (k0 & KIND_PERM) {   // (a permuted second layer fails the pair test below by its kind)
+        permute_fields<OP, M, V, false>(pa.perm + (size_t)l0 * pa.N, pa.N, pscr, G, j, u, w);
+        k0 &= ~KIND_PERM;
+      }
+    }
     if (i + 1 < nl && (k0 == 0 || k0 == KIND_MIS)) {
       const int l1 = (OP == OP_BWD) ? (l0 - 1) : (l0 + 1);
       const int k1 = kinds[l1];
@@ -645,7 +706,7 @@ __device__ __forceinline__ void run_chunk(const PropArgs& pa, int vb0, const int
 
 // One batch tile of one mesh: vectors [a.v0, a.vend), all L layers, by the W warps of the CTA.
 // Shared by the one-mesh kernel (prop_kernel) and the persistent multi-mesh kernel (mg_batched.cu).
-template <int OP, int M, int V, bool REAL, int GT, int GR>
+template <int OP, int M, int V, bool REAL, int GT, int GR, bool PERM = false>
 __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem) {
   using F = typename Fld<REAL>::T;
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -667,8 +728,19 @@ __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem
   int* skinds = reinterpret_cast<int*>(bars + a.S + 1);
   const int* kinds = a.kinds;
   if (a.L <= kMaxSmemKinds) {
-    for (int l = tid; l < a.L; l += blockDim.x) skinds[l] = __ldg(a.kinds + l);
+    for (int l = tid; l < a.L; l += blockDim.x) {
+      int k = __ldg(a.kinds + l);
+      if constexpr (PERM) k |= (__ldg(a.pflags + l) != 0) ? KIND_PERM : 0;
+      skinds[l] = k;
+    }
     kinds = skinds;
+  }
+  // permutation scratch: 32*M fields per warp after the kinds, 16-byte aligned (perm_scratch_offset); the
+  // host admits permuted launches only with the kinds in shared memory (L <= kMaxSmemKinds)
+  F* pscr = nullptr;
+  if constexpr (PERM) {
+    const size_t off = perm_scratch_offset(static_cast<size_t>(reinterpret_cast<unsigned char*>(skinds + a.L) - smem));
+    pscr = reinterpret_cast<F*>(smem + off) + (size_t)(warp * 32 + r * G) * M;
   }
 
   F u[V][M];
@@ -734,7 +806,8 @@ __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem
       if (tid == 0) issue_d(c);
     }
     const unsigned char* st = ring + (size_t)(c % a.S) * a.CL * a.layer_bytes;
-    run_chunk<OP, M, V, REAL, GR>(a, vb0, kinds, st, a.layer_bytes, lo, hi, gst_warp, gst_layer, G, j, r, u, w);
+    run_chunk<OP, M, V, REAL, GR, PERM>(a, vb0, kinds, st, a.layer_bytes, lo, hi, gst_warp, gst_layer, G, j, r, u, w,
+                                        pscr);
     __syncthreads();
     if constexpr (OP == OP_BWD && kDirect) chunk_reduce_direct<M, GR>(a, kinds, lo, hi - lo, gst, np2, G);
     if constexpr (OP == OP_BWD && GR == 4) chunk_reduce_raw<M>(a, kinds, lo, hi - lo, gst, np2, G);
@@ -757,11 +830,14 @@ __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem
   if (tid == 0)
     for (int s = 0; s <= a.S; ++s) mbar_inval(smem_u32(bars + s));
   (void)R;
+  if constexpr (PERM) {
+    if (a.perm_last != nullptr && __ldg(a.pflag_last) != 0) permute_fields<OP, M, V, false>(a.perm_last, a.N, pscr, G, j, u, w);
+  }
   store_fields<M, V, REAL>(u, a.out0, vb0, a.vend, a.N, a.ldu, j);
   if constexpr (OP != OP_FWD) store_fields<M, V, REAL>(w, a.out1, vb0, a.vend, a.N, a.ldu, j);
 }
 
-template <int OP, int M, int V, bool REAL, int GT, int GR>
+template <int OP, int M, int V, bool REAL, int GT, int GR, bool PERM = false>
 __global__ void __launch_bounds__(PropTraits<OP, M, V, REAL>::kMaxThreads)
 prop_kernel(const PropArgs a0) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -770,7 +846,7 @@ prop_kernel(const PropArgs a0) {
   a.v0 = blockIdx.x * (a.W * (32 / G) * V);
   a.vend = a.B;
   if (OP == OP_BWD) a.partial = a0.partial + (size_t)blockIdx.x * a.L * ((G * M) >> 1) * (GR == 4 ? 4 : 1);
-  prop_body<OP, M, V, REAL, GT, GR>(a, smem);
+  prop_body<OP, M, V, REAL, GT, GR, PERM>(a, smem);
 }
 
 // Split launch for a batch that one wave of full CTAs cannot spread evenly: two CTAs per SM, the first

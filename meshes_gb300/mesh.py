@@ -7,6 +7,10 @@ the same field layout: ``dot`` takes and returns (N, B) arrays whose columns are
 reference's Fortran-order CuPy arrays), here as torch tensors with strides (1, ldu).  Inputs may be
 torch tensors or numpy arrays.  Butterfly meshes take ``strides`` (stride exponents per layer)
 instead of ``lens``/``shifts``, like the reference's *_ft kernels (gpu/consts.cuh:31-35).
+
+Beyond the reference's GPU API (which refuses both, gpu/mesh.py:65 and mesh.py:573), a mesh may carry
+an input or output phase screen (``is_phase``) and permutations between layers (``perm``: L+1 index
+arrays or None, the reference's ``StructuredMeshNetwork.perm``, mesh.py:238-277).
 """
 from __future__ import annotations
 
@@ -16,7 +20,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._lib import GEO_FFT, GEO_NN, OP_BWD, OP_FWD, OP_FWDDIFF, check, load
+from ._lib import GEO_FFT, GEO_NN, GEO_PERM, OP_BWD, OP_FWD, OP_FWDDIFF, check, load
 from . import geometry as geom
 
 _NP_NS = {"mzi": (2, 2), "sym": (2, 1), "orth": (1, 0)}   # gpu/mesh.py:72-73
@@ -53,7 +57,7 @@ class MeshNetworkGPU:
     """Mesh network on the GPU (reference gpu/mesh.py:21-297)."""
 
     def __init__(self, N: int, L: int, lens=None, shifts=None, p_phase=None, p_splitter=None, X: str = "mzi",
-                 phi_pos: str = "out", is_phase: bool = True, strides=None, device=None):
+                 phi_pos: str = "out", is_phase: bool = True, strides=None, device=None, perm=None):
         assert X in ["mzi", "sym", "orth"]
         assert phi_pos in ["in", "out"]
         # the reference GPU API forbids the phase screen (gpu/mesh.py:65); here it is supported for complex
@@ -90,6 +94,11 @@ class MeshNetworkGPU:
         assert n_spl in [self.n_splitter, 0]
         self.p_splitter = (self._param(p_splitter).reshape(L, N // 2, self.X_ns) if n_spl
                            else torch.empty((L, N // 2, 0), dtype=torch.float32, device=self.device))
+        self.perm_h, self.perm_table = _perm_rows(perm, self.N, self.L)
+        if self.perm_table is not None:
+            self.perm_table = torch.as_tensor(self.perm_h, device=self.device)
+        # geometry code of the library calls: the layout, with MG_GEO_PERM when permutations ride along
+        self.geo_code = self.geometry | (GEO_PERM if self.perm_table is not None else 0)
         self._ws = {op: Workspace(self.device) for op in (OP_FWD, OP_FWDDIFF, OP_BWD)}
         self.config = {OP_FWD: None, OP_FWDDIFF: None, OP_BWD: None}   # mg_config per op (autotuner)
 
@@ -169,6 +178,24 @@ class MeshNetworkGPU:
         sp = s.data_ptr() if s.numel() else None
         return p.data_ptr(), ldp, sp, lds
 
+    def _programmed(self, op, p, s, B, dp=None) -> Tuple[int, int]:
+        """Tiles of op for phases p (and direction dp) plus the permutation tables, in op's workspace."""
+        lib = load()
+        wsb = lib.mg_workspace_bytes(op, self.N, self.L, B, self.crossing, self.geo_code, None)
+        if wsb == 0:
+            check(-1, "mg_workspace_bytes")
+        ws, wsn = self._ws[op].get(wsb)
+        stream = _stream(self.device)
+        pptr, ldp, sptr, lds = self._ps_args(p, s)
+        geo = ((None, None, self.strides.data_ptr()) if self.geometry == GEO_FFT
+               else (self.lens.data_ptr(), self.shifts.data_ptr(), None))
+        check(lib.mg_build_tiles(op, self.N, self.L, self.geo_code, *geo, self.crossing, pptr, ldp, sptr, lds,
+                                 None if dp is None else dp.data_ptr(), None, None, B, None, ws, wsn, stream),
+              "mg_build_tiles")
+        check(lib.mg_build_perms(op, self.N, self.L, B, self.crossing, self.geo_code, self.perm_table.data_ptr(), None,
+                                 ws, wsn, stream), "mg_build_perms")
+        return ws, wsn
+
     # ---- forward / forward-mode derivative (gpu/mesh.py:147-174)
     def dot(self, v, p_phase=None, p_splitter=None, dp=None, dv=None, out=None, dout=None):
         """y = U v (v (N, B)); with dp and/or dv also the forward-mode derivative dy (gpu/mesh.py:147-174).
@@ -191,6 +218,13 @@ class MeshNetworkGPU:
                 tmp, ldu = self._out(None, B)
                 tmp.copy_(v)
                 v, ldu_in = tmp, ldu
+            if self.perm_table is not None:
+                if B:
+                    ws, wsn = self._programmed(OP_FWD, p, s, B)
+                    check(lib.mg_propagate(OP_FWD, self.N, self.L, B, self.crossing, self.geo_code, v.data_ptr(), None,
+                                           out.data_ptr(), None, ldu_out, None, 0, 0, None, ws, wsn, stream),
+                          "mg_propagate")
+                return out
             wsb = lib.mg_workspace_bytes(OP_FWD, self.N, self.L, B, self.crossing, self.geometry, None)
             ws, wsn = self._ws[OP_FWD].get(wsb)
             fn = lib.mg_fwdprop_ft if self.geometry == GEO_FFT else lib.mg_fwdprop
@@ -215,6 +249,13 @@ class MeshNetworkGPU:
             self._dot_mesh(v, p, s, dp=dpp, dv=dv, out=o2, dout=d2)
             out.copy_(o2)
             dout.copy_(d2)
+            return out, dout
+        if self.perm_table is not None:
+            if B:
+                ws, wsn = self._programmed(OP_FWDDIFF, p, s, B, dp=dpp)
+                check(lib.mg_propagate(OP_FWDDIFF, self.N, self.L, B, self.crossing, self.geo_code, v.data_ptr(),
+                                       None if dv is None else dv.data_ptr(), out.data_ptr(), dout.data_ptr(), ldu_out,
+                                       None, 0, 0, None, ws, wsn, stream), "mg_propagate")
             return out, dout
         wsb = lib.mg_workspace_bytes(OP_FWDDIFF, self.N, self.L, B, self.crossing, self.geometry, None)
         ws, wsn = self._ws[OP_FWDDIFF].get(wsb)
@@ -289,11 +330,22 @@ class MeshNetworkGPU:
         else:
             assert isinstance(out_dp, torch.Tensor) and out_dp.numel() == p.numel() and out_dp.is_contiguous()
         pptr, ldp, sptr, lds = self._ps_args(p, s)
+        if out_vin is not None:
+            assert out_vin.shape == (self.N, B) and out_vin.stride(0) == 1 and (B == 1 or out_vin.stride(1) == ldu)
+        if self.perm_table is not None:
+            if B == 0:
+                if not accumulate:
+                    out_dp.zero_()
+                return out_dp, out_dJdv
+            ws, wsn = self._programmed(OP_BWD, p, s, B)
+            check(lib.mg_propagate(OP_BWD, self.N, self.L, B, self.crossing, self.geo_code, v2.data_ptr(), g.data_ptr(),
+                                   None if out_vin is None else out_vin.data_ptr(), out_dJdv.data_ptr(), ldu,
+                                   out_dp.data_ptr(), ldp, accumulate, None, ws, wsn, _stream(self.device)),
+                  "mg_propagate")
+            return out_dp, out_dJdv
         wsb = lib.mg_workspace_bytes(OP_BWD, self.N, self.L, B, self.crossing, self.geometry, None)
         ws, wsn = self._ws[OP_BWD].get(wsb)
         fn = lib.mg_backdiff_ft if self.geometry == GEO_FFT else lib.mg_backdiff
-        if out_vin is not None:
-            assert out_vin.shape == (self.N, B) and out_vin.stride(0) == 1 and (B == 1 or out_vin.stride(1) == ldu)
         check(fn(self.N, self.L, B, *self._geo_args(), pptr, out_dp.data_ptr(), ldp, sptr, lds, v2.data_ptr(),
                  g.data_ptr(), None if out_vin is None else out_vin.data_ptr(), out_dJdv.data_ptr(), ldu,
                  self.crossing, accumulate, ws, wsn, _stream(self.device)), fn.__name__)
@@ -408,6 +460,24 @@ class MeshNetworkGPU:
         return max(ws.status(clear) for ws in self._ws.values())
 
 
+def _perm_rows(perm, N: int, L: int):
+    """(L+1, N) int32 gather rows of the reference's ``perm`` list (None rows are the identity), or
+    (None, None) when no row moves anything."""
+    if perm is None:
+        return None, None
+    rows = list(perm)
+    assert len(rows) == L + 1, "perm needs L+1 = %d entries (mesh.py:277)" % (L + 1)
+    if all(r is None for r in rows):
+        return None, None
+    out = np.empty((L + 1, N), dtype=np.int32)
+    for k, r in enumerate(rows):
+        out[k] = np.arange(N) if r is None else np.asarray(r).reshape(-1)
+        assert np.array_equal(np.sort(out[k]), np.arange(N)), "perm[%d] is not a permutation of 0..N-1" % k
+    if all(np.array_equal(r, np.arange(N)) for r in out):
+        return None, None
+    return out, out
+
+
 def _numel(x) -> int:
     return int(x.numel()) if isinstance(x, torch.Tensor) else int(np.asarray(x).size)
 
@@ -422,11 +492,11 @@ def from_structured(net, device=None) -> MeshNetworkGPU:
     """Counterpart of the reference ``StructuredMeshNetwork.gpu()`` (mesh.py:568-579).
 
     ``net`` is any object exposing N, L, lens, shifts, grid_phase, grid_splitter, X and perm (the
-    reference's StructuredMeshNetwork, ClementsNetwork, ReckNetwork).  Permutation-free only, as in
-    the reference; a reference ButterflyNetwork (permutations between adjacent-pair layers) is
-    converted to the equivalent stride geometry instead.  Unlike the reference, a mesh with a phase
-    screen (is_phase) converts too, and a ClippedNetwork (SquareNetwork, QRNetwork) becomes a
-    ClippedMeshGPU around its converted full mesh.
+    reference's StructuredMeshNetwork, ClementsNetwork, ReckNetwork, ButterflyNetwork, ...).  Unlike
+    the reference, which refuses them (mesh.py:573), permutations between layers and a phase screen
+    (is_phase) convert too; a reference ButterflyNetwork (permutations around adjacent-pair layers)
+    becomes the equivalent stride geometry, which needs no permutations.  A ClippedNetwork
+    (SquareNetwork, QRNetwork, PilossNetwork) becomes a ClippedMeshGPU around its converted full mesh.
     """
     if hasattr(net, "full") and hasattr(net, "idx_in"):     # ClippedNetwork, SquareNetwork, QRNetwork
         from .clipped import ClippedMeshGPU
@@ -437,20 +507,17 @@ def from_structured(net, device=None) -> MeshNetworkGPU:
     N, L = int(net.N), int(net.L)
     p = np.nan_to_num(np.asarray(net.grid_phase, dtype=np.float32))
     s = np.nan_to_num(np.asarray(net.grid_splitter, dtype=np.float32))
-    if getattr(net, "is_phase", False):
-        # the phase screen rides along (the reference's gpu() refuses it, gpu/mesh.py:65)
-        if any(x is not None for x in net.perm):
-            raise AssertionError("meshes with permutations are not supported (reference mesh.py:573)")
-        ph = np.asarray(net.phi_out, dtype=np.float32).reshape(-1)
-        return MeshNetworkGPU(N, L, np.array(net.lens), np.array(net.shifts),
-                              np.concatenate([p.reshape(-1), ph]), s if s.size else None, X,
-                              phi_pos=net.phi_pos, is_phase=True, device=device)
-    perms = [x for x in net.perm if x is not None]
-    if perms:
-        if type(net).__name__ != "ButterflyNetwork":
-            raise AssertionError("meshes with permutations are not supported (reference mesh.py:573)")
+    perm = list(net.perm)
+    is_phase = bool(getattr(net, "is_phase", False))
+    if type(net).__name__ == "ButterflyNetwork" and not is_phase and any(x is not None for x in perm):
         strides = geom.butterfly(N)
         return MeshNetworkGPU(N, L, None, None, p, s if s.size else None, X, is_phase=False, strides=strides,
                               device=device)
+    if is_phase:
+        # the phase screen rides along (the reference's gpu() refuses it, gpu/mesh.py:65)
+        ph = np.asarray(net.phi_out, dtype=np.float32).reshape(-1)
+        return MeshNetworkGPU(N, L, np.array(net.lens), np.array(net.shifts),
+                              np.concatenate([p.reshape(-1), ph]), s if s.size else None, X,
+                              phi_pos=net.phi_pos, is_phase=True, device=device, perm=perm)
     return MeshNetworkGPU(N, L, np.array(net.lens), np.array(net.shifts), p, s if s.size else None, X,
-                          phi_pos="out", is_phase=False, device=device)
+                          phi_pos="out", is_phase=False, device=device, perm=perm)

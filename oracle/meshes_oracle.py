@@ -229,6 +229,7 @@ class OracleMesh:
     p: np.ndarray = field(default=None)        # (L, N//2, n_p)
     s: Optional[np.ndarray] = None             # (L, N//2, n_s) or None
     T_override: Optional[np.ndarray] = None    # (L, N//2, 2, 2) complex: generic crossing
+    perm: Optional[np.ndarray] = None          # (L+1, N) gather rows between layers (mesh.py:238-277)
 
     @property
     def fft(self) -> bool:
@@ -294,6 +295,18 @@ def _layer_index(mesh: OracleMesh, n: int):
     return cache[n]
 
 
+def _gather(mesh: OracleMesh, k: int, *fields, inverse=False):
+    """Fields (N, B) <- rows permuted by perm[k] (c/dot.cpp:29-40: new[q] = old[perm[q]]), or by its
+    inverse argsort(perm[k]) (the reference's perms_bk, mesh.py:382)."""
+    if mesh.perm is None:
+        return
+    row = np.asarray(mesh.perm[k])
+    if inverse:
+        row = np.argsort(row)
+    for f in fields:
+        f[:] = f[row]
+
+
 def _apply_layer(mesh: OracleMesh, n: int, T: np.ndarray, u: np.ndarray, conj_transpose=False):
     """u <- T_n u for every active slot of layer n (vectorised over the slots of the layer)."""
     q, a, b = _layer_index(mesh, n)
@@ -316,21 +329,26 @@ def propagate(mesh: OracleMesh, x: np.ndarray, p=None) -> np.ndarray:
         T = T.real
     u = np.ascontiguousarray(u.T)
     for n in range(mesh.L):
+        _gather(mesh, n, u)                 # c/dot.cpp:150-153
         _apply_layer(mesh, n, T, u)
+    _gather(mesh, mesh.L, u)                # c/dot.cpp:289-292
     return np.ascontiguousarray(u.T)
 
 
 def propagate_activations(mesh: OracleMesh, x: np.ndarray, p=None):
-    """Field before every layer: list of L+1 arrays (x, after layer 0, ..., y)."""
+    """Input of every layer (after the permutation before it) and the output: list of L+1 arrays."""
     T = mesh.T_grid(p)
     u = np.array(x, dtype=np.float64 if np.isrealobj(x) else np.complex128)
     if u.dtype == np.float64:
         T = T.real
     u = np.ascontiguousarray(u.T)
-    acts = [u.T.copy()]
+    acts = []
     for n in range(mesh.L):
-        _apply_layer(mesh, n, T, u)
+        _gather(mesh, n, u)
         acts.append(u.T.copy())
+        _apply_layer(mesh, n, T, u)
+    _gather(mesh, mesh.L, u)
+    acts.append(u.T.copy())
     return acts
 
 
@@ -348,6 +366,7 @@ def fwddiff(mesh: OracleMesh, x: np.ndarray, dp: np.ndarray, dx: Optional[np.nda
         T, dT = T.real, dT.real
     u, du = np.ascontiguousarray(u.T), np.ascontiguousarray(du.T)
     for n in range(mesh.L):
+        _gather(mesh, n, u, du)
         q, a, b = _layer_index(mesh, n)
         if q.size == 0:
             continue
@@ -357,6 +376,7 @@ def fwddiff(mesh: OracleMesh, x: np.ndarray, dp: np.ndarray, dx: Optional[np.nda
         du[b] = t[:, 1, 0] * dua + t[:, 1, 1] * dub + d[:, 1, 0] * ua + d[:, 1, 1] * ub
         u[a] = t[:, 0, 0] * ua + t[:, 0, 1] * ub
         u[b] = t[:, 1, 0] * ua + t[:, 1, 1] * ub
+    _gather(mesh, mesh.L, u, du)
     return np.ascontiguousarray(u.T), np.ascontiguousarray(du.T)
 
 
@@ -377,6 +397,7 @@ def vjp_unitary(mesh: OracleMesh, y: np.ndarray, g: np.ndarray, p=None):
     G = np.zeros((mesh.L, mesh.N // 2, 2, 2), dtype=dt)
     u, gg = np.ascontiguousarray(u.T), np.ascontiguousarray(gg.T)
     for n in range(mesh.L - 1, -1, -1):
+        _gather(mesh, n + 1, u, gg, inverse=True)          # c/dot.cpp:150-153 with perms_bk
         q, a, b = _layer_index(mesh, n)
         if q.size == 0:
             continue
@@ -392,6 +413,7 @@ def vjp_unitary(mesh: OracleMesh, y: np.ndarray, g: np.ndarray, p=None):
         G[n, q, 1, 1] = np.sum(gb.conj() * xb, axis=1)
         gg[a] = th[:, 0, 0] * ga + th[:, 0, 1] * gb
         gg[b] = th[:, 1, 0] * ga + th[:, 1, 1] * gb
+    _gather(mesh, 0, u, gg, inverse=True)
     return G, np.ascontiguousarray(u.T), np.ascontiguousarray(gg.T)
 
 
@@ -409,6 +431,7 @@ def vjp_stored(mesh: OracleMesh, x: np.ndarray, g: np.ndarray, p=None):
     G = np.zeros((mesh.L, mesh.N // 2, 2, 2), dtype=gg.dtype)
     gg = np.ascontiguousarray(gg.T)
     for n in range(mesh.L - 1, -1, -1):
+        _gather(mesh, n + 1, gg, inverse=True)
         q, a, b = _layer_index(mesh, n)
         if q.size == 0:
             continue
@@ -422,6 +445,7 @@ def vjp_stored(mesh: OracleMesh, x: np.ndarray, g: np.ndarray, p=None):
         G[n, q, 1, 1] = np.sum(gb.conj() * xb, axis=1)
         gg[a] = th[:, 0, 0] * ga + th[:, 0, 1] * gb
         gg[b] = th[:, 1, 0] * ga + th[:, 1, 1] * gb
+    _gather(mesh, 0, gg, inverse=True)
     return G, np.ascontiguousarray(gg.T)
 
 

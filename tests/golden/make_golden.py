@@ -232,6 +232,61 @@ def main(ref_path):
              J=J, dJdp=flat_to_grid(dJdp[:n_cr * 2].reshape(n_cr, 2), lens, shifts, full.N, 2),
              dJdph=dJdp[n_cr * 2:])
 
+    # Permutations between layers (mesh.py:238-277; c/dot.cpp:29-40,150-153,289-292): a Clements layout
+    # with random permutations before some layers and after the last, without a screen (dot, forward-mode
+    # derivative, dot_vjp) and with an input screen (dot, dot_vjp).
+    from meshes.mesh import StructuredMeshNetwork
+    for name, is_phase, pos in (("perm_mzi_N8_split", False, "out"), ("perm_mzi_N8_screen_in", True, "in")):
+        N = 8
+        lens, shifts = [int(x) for x in ClementsNetwork(N=N).lens], [int(x) for x in ClementsNetwork(N=N).shifts]
+        L = len(lens)
+        n_cr = sum(lens)
+        perm = [None] * (L + 1)
+        for k in (0, 3, 5, L):
+            perm[k] = rng.permutation(N)
+        net = StructuredMeshNetwork(N, lens, shifts, p_splitter=rng.normal(0, 0.02, (n_cr, 2)), perm=perm,
+                                    phi_pos=pos, is_phase=is_phase)
+        net.p_phase[:] = rng.uniform(0, 2 * np.pi, net.p_phase.shape).astype(np.float32).astype(np.float64)
+        net.p_splitter = net.p_splitter.astype(np.float32).astype(np.float64)
+        B = 5
+        x = (rng.standard_normal((B, N)) + 1j * rng.standard_normal((B, N)))
+        x /= np.linalg.norm(x, axis=1, keepdims=True)
+        y = net.dot(x.T).T
+        dp_full = rng.standard_normal(net.n_phase)
+        _, dy = net.dot(x.T, dp=dp_full)
+        t = (rng.standard_normal((B, N)) + 1j * rng.standard_normal((B, N)))
+        g = 2 * (y - t)
+        dJdp, dJdv = net.dot_vjp(y.T, g.T)
+        perm_rows = np.array([np.arange(N) if r is None else r for r in perm])
+        save(name, N=N, L=L, crossing="mzi", phi_pos=pos, is_phase=is_phase, lens=np.array(lens),
+             shifts=np.array(shifts), perm=perm_rows, p=flat_to_grid(net.p_phase[:n_cr * 2], lens, shifts, N, 2),
+             ph=net.p_phase[n_cr * 2:], s=flat_to_grid(net.p_splitter, lens, shifts, N, 2), x=x, y=y,
+             dp_dir=flat_to_grid(dp_full[:n_cr * 2], lens, shifts, N, 2), dph_dir=dp_full[n_cr * 2:], dy=dy.T,
+             g=g, dJdp=flat_to_grid(dJdp[:n_cr * 2], lens, shifts, N, 2), dJdph=dJdp[n_cr * 2:], g_in=dJdv.T)
+
+    # PILOSS mesh (piloss.py:18-57): a ClippedNetwork over a 2N-mode mesh of full aligned layers with a
+    # permutation before every layer and after the last, output phase screen; ClippedNetwork.dot and
+    # grad_L2 of the reference with random phases and splitting errors.
+    from meshes.piloss import PilossNetwork
+    n = 4
+    net = PilossNetwork(N=n)
+    full = net.full
+    n_cr = full.n_cr
+    full.p_phase[:] = rng.uniform(0, 2 * np.pi, full.p_phase.shape).astype(np.float32).astype(np.float64)
+    full.p_splitter = rng.normal(0, 0.02, (n_cr, 2)).astype(np.float32).astype(np.float64)
+    lens, shifts = list(map(int, full.lens)), list(map(int, full.shifts))
+    B = 3
+    x = (rng.standard_normal((n, B)) + 1j * rng.standard_normal((n, B)))
+    y = net.dot(x)
+    Z = rng.standard_normal((net.M, n)) + 1j * rng.standard_normal((net.M, n))
+    J, dJdp = net.grad_L2(Z)
+    perm_rows = np.array([np.arange(full.N) if r is None else r for r in full.perm])
+    save("piloss_N%d" % n, N=full.N, L=full.L, lens=np.array(lens), shifts=np.array(shifts), perm=perm_rows,
+         phi_pos=full.phi_pos, p=flat_to_grid(full.p_crossing, lens, shifts, full.N, 2), ph=full.phi_out,
+         s=flat_to_grid(full.p_splitter, lens, shifts, full.N, 2), idx_in=np.arange(full.N)[net.idx_in],
+         idx_out=np.arange(full.N)[net.idx_out], x=x, y=y, U_target=Z, J=J,
+         dJdp=flat_to_grid(dJdp[:n_cr * 2].reshape(n_cr, 2), lens, shifts, full.N, 2), dJdph=dJdp[n_cr * 2:])
+
     print("wrote", *written, sep="\n  ")
 
 

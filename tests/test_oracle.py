@@ -16,7 +16,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def fixtures():
     """Fixtures of the plain meshes (the phase-screen and lossy fixtures have their own tests)."""
     return sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz") and "_screen_" not in f and "lossy" not in f
-                  and not f.startswith("clipped_"))
+                  and not f.startswith(("clipped_", "perm_", "piloss_")))
 
 
 def load(name):
@@ -213,6 +213,57 @@ def test_clipped_mesh_matches_reference_fixtures(name):
     E = np.zeros((n_in, Nf), complex)
     E[np.arange(n_in), f["idx_in"]] = 1
     U = O.propagate_screened(om, E, f["ph"], pos)                  # rows: U[:, idx_in[k]]
+    dU = U[:, f["idx_out"]].T - f["U_target"]
+    assert abs(np.sum(np.abs(dU) ** 2) - float(f["J"])) < 1e-12 * float(f["J"])
+    G = np.zeros_like(U)
+    G[:, f["idx_out"]] = 2 * dU.T
+    dp, dph, _ = O.grad_screened(om, U, G, f["ph"], pos)
+    assert O.rel_err(dp, f["dJdp"]) < 1e-12 and O.rel_err(dph, f["dJdph"]) < 1e-12
+
+
+def _perm_mesh(f):
+    return O.OracleMesh(N=int(f["N"]), L=int(f["L"]), crossing="mzi", lens=list(f["lens"]), shifts=list(f["shifts"]),
+                        p=f["p"], s=f["s"], perm=f["perm"])
+
+
+@pytest.mark.parametrize("name", ["perm_mzi_N8_split.npz", "perm_mzi_N8_screen_in.npz"])
+def test_permuted_mesh_matches_reference_fixtures(name):
+    """Permutations between layers (c/dot.cpp:29-40,150-153,289-292): forward, forward-mode derivative and
+    dot_vjp (inverse permutations in reverse, mesh.py:382) of the reference, with and without a screen."""
+    f = np.load(os.path.join(GOLDEN, name))
+    om = _perm_mesh(f)
+    if bool(f["is_phase"]):
+        pos = str(f["phi_pos"])
+        y = O.propagate_screened(om, f["x"], f["ph"], pos)
+        _, dy = O.fwddiff_screened(om, f["x"], f["ph"], pos, f["dp_dir"], f["dph_dir"])
+        dp, dph, gin = O.grad_screened(om, f["y"], f["g"], f["ph"], pos)
+        assert O.rel_err(dph, f["dJdph"]) < 1e-12
+    else:
+        y = O.propagate(om, f["x"])
+        _, dy = O.fwddiff(om, f["x"], f["dp_dir"])
+        G, xr, gin = O.vjp_unitary(om, f["y"], f["g"])
+        dp = O.contract_dp(om, G)
+        assert O.rel_err(xr, f["x"]) < 1e-12
+        G2, gin2 = O.vjp_stored(om, f["x"], f["g"])
+        assert O.rel_err(O.contract_dp(om, G2), f["dJdp"]) < 1e-12 and O.rel_err(gin2, f["g_in"]) < 1e-12
+    assert O.rel_err(y, f["y"]) < 1e-13
+    assert O.rel_err(dy, f["dy"]) < 1e-12
+    assert O.rel_err(dp, f["dJdp"]) < 1e-12
+    assert O.rel_err(gin, f["g_in"]) < 1e-12
+
+
+def test_piloss_matches_reference_fixture():
+    """PILOSS mesh (piloss.py:18-57): a ClippedNetwork over a permuted full mesh with an output screen."""
+    f = np.load(os.path.join(GOLDEN, "piloss_N4.npz"))
+    pos = str(f["phi_pos"])
+    om = _perm_mesh(f)
+    Nf, n_in = int(f["N"]), len(f["idx_in"])
+    X = np.zeros((f["x"].shape[1], Nf), complex)
+    X[:, f["idx_in"]] = f["x"].T
+    assert O.rel_err(O.propagate_screened(om, X, f["ph"], pos)[:, f["idx_out"]].T, f["y"]) < 1e-13
+    E = np.zeros((n_in, Nf), complex)
+    E[np.arange(n_in), f["idx_in"]] = 1
+    U = O.propagate_screened(om, E, f["ph"], pos)
     dU = U[:, f["idx_out"]].T - f["U_target"]
     assert abs(np.sum(np.abs(dU) ** 2) - float(f["J"])) < 1e-12 * float(f["J"])
     G = np.zeros_like(U)
