@@ -235,3 +235,141 @@ class LossyMeshFunction(torch.autograd.Function):
         gx = g if ctx.needs_input_grad[0] else None
         gT = dT.to(ctx.T_dtype) if ctx.needs_input_grad[1] else None
         return gx, gT, None
+
+
+class GenericMeshGPU:
+    """The MeshNetworkGPU API (``dot``, ``grad_phi``, ``L2norm``, ``grad_phi_target``, ``matrix``; reference
+    gpu/mesh.py:21-297) for a mesh of any crossing in ``crossings.SIZES`` - the reference's other
+    parameterisations (crossing.py:292-611), which its GPU path does not run.
+
+    T(p, s) is built per slot by ``crossings.transfer`` (differentiable, float64), propagated by the GPU
+    kernels' generic precomputed-T path, and differentiated with the checkpointed stored-activation adjoint,
+    which is exact for lossy and lossless crossings alike; dJ/dp follows from dJ/dT through PyTorch's
+    autograd of T.  Parameter layout as MeshNetworkGPU: p_phase = the (L, N/2, n_phase) grid flattened,
+    followed by N screen phases when ``is_phase``; p_splitter (L, N/2, n_splitter).  Fields are (N, B).
+    """
+
+    def __init__(self, N: int, L: int, lens=None, shifts=None, p_phase=None, p_splitter=None, X: str = "mzi_generic",
+                 phi_pos: str = "out", is_phase: bool = False, strides=None, device=None,
+                 segment: Optional[int] = None):
+        from .crossings import SIZES
+        if X not in SIZES:
+            raise ValueError("unknown crossing %r" % X)
+        assert phi_pos in ("in", "out")
+        self.mesh = LossyMesh(N, lens, shifts, strides, device, segment)
+        assert self.mesh.L == L, "L=%d does not match the geometry (%d layers)" % (L, self.mesh.L)
+        self.N, self.L, self.X = int(N), int(L), X
+        self.phi_pos, self.is_phase = phi_pos, bool(is_phase)
+        self.device = self.mesh.device
+        self.X_np, self.X_ns = SIZES[X]
+        self.n_cr = self.L * (self.N // 2)
+        n_phase = self.n_cr * self.X_np + (self.N if self.is_phase else 0)
+        self.p_phase = self._param(np.zeros(n_phase) if p_phase is None else p_phase).reshape(-1)
+        assert self.p_phase.numel() == n_phase, "p_phase has %d entries, expected %d" % (self.p_phase.numel(), n_phase)
+        self.p_splitter = None if p_splitter is None else self._param(p_splitter).reshape(self.L, self.N // 2, self.X_ns)
+        # inactive slots take parameters inside every crossing's domain (the kernels use the identity there)
+        self._safe_p = torch.zeros(self.X_np, dtype=torch.float64, device=self.device)
+        if X == "cartesian":
+            self._safe_p[0] = 2.0
+        self.dtype = torch.complex64
+
+    @property
+    def n_phase(self) -> int:
+        return self.p_phase.numel()
+
+    def _param(self, x) -> torch.Tensor:
+        if isinstance(x, torch.Tensor):
+            return x.detach().to(device=self.device, dtype=torch.float64)
+        return torch.as_tensor(np.asarray(x, dtype=np.float64), device=self.device)
+
+    def transfer(self, p: torch.Tensor, s: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """T (L, N/2, 2, 2) complex128 of the crossing parameters p (L, N/2, n_phase), identity on inactive slots."""
+        from .crossings import transfer
+        act = self.mesh.active[..., None]
+        T = transfer(self.X, torch.where(act, p, self._safe_p), s)
+        eye = torch.eye(2, dtype=T.dtype, device=T.device)
+        return torch.where(act[..., None], T, eye)
+
+    def _forward(self, x: torch.Tensor, p: torch.Tensor, s: Optional[torch.Tensor]) -> torch.Tensor:
+        """y (B, N) for x (B, N) and the flat parameter vector p (differentiable in both)."""
+        ncp = self.n_cr * self.X_np
+        if self.is_phase and self.phi_pos == "in":
+            x = x * torch.exp(1j * p[ncp:])
+        y = self.mesh(x, self.transfer(p[:ncp].reshape(self.L, self.N // 2, self.X_np), s))
+        if self.is_phase and self.phi_pos == "out":
+            y = y * torch.exp(1j * p[ncp:])
+        return y
+
+    def _rows(self, v) -> torch.Tensor:
+        v = v if isinstance(v, torch.Tensor) else torch.as_tensor(np.asarray(v))
+        v = v.to(device=self.device)
+        assert v.dim() == 2 and v.shape[0] == self.N, "v must be (N, B) with N=%d" % self.N
+        return v.t().to(torch.complex64).contiguous()
+
+    def _args(self, p_phase, p_splitter):
+        p = self.p_phase if p_phase is None else self._param(p_phase).reshape(-1)
+        s = self.p_splitter if p_splitter is None else self._param(p_splitter).reshape(self.L, self.N // 2, self.X_ns)
+        assert p.numel() == self.n_phase
+        return p, s
+
+    def dot(self, v, p_phase=None, p_splitter=None) -> torch.Tensor:
+        """y = U v for v (N, B); returns (N, B) complex64."""
+        p, s = self._args(p_phase, p_splitter)
+        with torch.no_grad():
+            y = self._forward(self._rows(v), p, s)
+        return y.to(torch.complex64).t()
+
+    def grad_phi(self, v, dJdv, p_phase=None, p_splitter=None, out_dp=None, out_dJdv=None, vpos: str = "in"):
+        """(dJ/dp, dJ/dv_in*·2) for J(v_out) with v the INPUT fields; dJdv is 2 dJ/dv_out* or a callable of
+        v_out, as MeshNetworkGPU.grad_phi.  vpos 'out' (rebuilding the input from the output by T^H, what
+        the reference does) is refused: it is exact only for unitary crossings."""
+        if vpos != "in":
+            raise NotImplementedError("generic crossings back-propagate from the input fields (vpos='in')")
+        p, s = self._args(p_phase, p_splitter)
+        p = p.clone().requires_grad_(True)
+        x = self._rows(v).requires_grad_(True)
+        with torch.enable_grad():
+            y = self._forward(x, p, s)
+            yv = y.detach().to(torch.complex64).t()
+            g = dJdv(yv) if callable(dJdv) else dJdv
+            g = self._rows(g).to(y.dtype)
+            dp, gx = torch.autograd.grad(y, (p, x), g)
+        dp = dp.to(torch.float32)
+        if out_dp is not None:
+            out_dp += dp.reshape(out_dp.shape)
+            dp = out_dp
+        gx = gx.to(torch.complex64).t()
+        if out_dJdv is not None:
+            out_dJdv.copy_(gx)
+            gx = out_dJdv
+        return dp, gx
+
+    def matrix(self, p_phase=None, p_splitter=None) -> torch.Tensor:
+        return self.dot(torch.eye(self.N, dtype=torch.complex64, device=self.device), p_phase, p_splitter)
+
+    def _L2norm_fn(self, J):
+        def f(U):
+            V = U - torch.eye(self.N, dtype=U.dtype, device=U.device)
+            if not self.is_phase:
+                V = V - torch.diag(torch.diagonal(V))
+            J[0] = float(torch.linalg.norm(V) ** 2)
+            return 2 * V
+        return f
+
+    def L2norm(self, U_target, p_phase=None, p_splitter=None) -> float:
+        """||U U_t^H - I||^2 (off-diagonal only without a screen), as MeshNetworkGPU.L2norm."""
+        J = [0.0]
+        self._L2norm_fn(J)(self.dot(self._adjoint(U_target), p_phase, p_splitter))
+        return J[0]
+
+    def grad_phi_target(self, U_target, p_phase=None, p_splitter=None):
+        J = [0.0]
+        dp = self.grad_phi(self._adjoint(U_target), self._L2norm_fn(J), p_phase, p_splitter)[0]
+        return J[0], dp
+
+    def _adjoint(self, U) -> torch.Tensor:
+        U = U if isinstance(U, torch.Tensor) else torch.as_tensor(np.asarray(U))
+        return U.to(device=self.device, dtype=torch.complex64).t().conj()
+
+    def status(self, clear: bool = True) -> int:
+        return self.mesh.status(clear)

@@ -502,9 +502,11 @@ def from_structured(net, device=None) -> MeshNetworkGPU:
         from .clipped import ClippedMeshGPU
         return ClippedMeshGPU(from_structured(net.full, device), net.idx_in, net.idx_out)
     name = type(net.X).__name__
+    N, L = int(net.N), int(net.L)
+    if name not in ("MZICrossing", "SymCrossing"):
+        return _from_structured_generic(net, name, device)
     X = {"MZICrossing": "mzi", "SymCrossing": "sym"}[name]
     n_p, n_s = _NP_NS[X]
-    N, L = int(net.N), int(net.L)
     p = np.nan_to_num(np.asarray(net.grid_phase, dtype=np.float32))
     s = np.nan_to_num(np.asarray(net.grid_splitter, dtype=np.float32))
     perm = list(net.perm)
@@ -521,3 +523,24 @@ def from_structured(net, device=None) -> MeshNetworkGPU:
                               phi_pos=net.phi_pos, is_phase=True, device=device, perm=perm)
     return MeshNetworkGPU(N, L, np.array(net.lens), np.array(net.shifts), p, s if s.size else None, X,
                           phi_pos="out", is_phase=False, device=device, perm=perm)
+
+
+def _from_structured_generic(net, name: str, device=None):
+    """A StructuredMeshNetwork of another crossing class (crossing.py:292-611) as a lossy.GenericMeshGPU:
+    T(p, s) per slot on the generic precomputed-T path (float64 parameters, as the reference keeps them)."""
+    from .crossings import CLASS_NAMES
+    from .lossy import GenericMeshGPU
+    if name not in CLASS_NAMES:
+        raise ValueError("crossing class %s has no GPU counterpart" % name)
+    if any(x is not None for x in net.perm):
+        raise ValueError("meshes of generic crossings take no permutations")
+    X = CLASS_NAMES[name]
+    N, L = int(net.N), int(net.L)
+    p = np.nan_to_num(np.asarray(net.grid_phase, dtype=np.float64)).reshape(-1)
+    sp = np.asarray(net.grid_splitter, dtype=np.float64)
+    is_phase = bool(getattr(net, "is_phase", False))
+    if is_phase:
+        p = np.concatenate([p, np.asarray(net.phi_out, dtype=np.float64).reshape(-1)])
+    return GenericMeshGPU(N, L, np.array(net.lens), np.array(net.shifts), p,
+                          np.nan_to_num(sp) if sp.size else None, X, phi_pos=net.phi_pos, is_phase=is_phase,
+                          device=device)

@@ -39,7 +39,10 @@ from typing import Optional, Sequence
 import numpy as np
 
 # (n_p, n_s): gpu/mesh.py:72-73; the lossy generic MZI has 14 splitter entries (crossing.py:448-452)
-CROSSINGS = {"mzi": (2, 2), "sym": (2, 1), "orth": (1, 0), "mzi_generic": (2, 14)}
+CROSSINGS = {"mzi": (2, 2), "sym": (2, 1), "orth": (1, 0), "mzi_generic": (2, 14),
+             # the reference's other parameterisations (crossing.py:292-357, 384-442, 493-611)
+             "mzi_balanced": (2, 2), "mzi_outphase": (2, 2), "mzi3": (2, 3), "mzi3_outphase": (2, 3),
+             "mzi_generic_outphase": (2, 14), "cartesian": (2, 2), "bell": (2, 2)}
 
 
 # ----------------------------------------------------------------------------------------------
@@ -211,7 +214,94 @@ def dT_mzi_generic(p, s=None):
     return np.array([dth, dph])
 
 
-T_FN = {"mzi": T_mzi, "sym": T_sym, "orth": T_orth, "mzi_generic": T_mzi_generic}
+def _splits(s, k, n):
+    return np.zeros((k, n)) if s is None else np.asarray(s, dtype=np.float64).reshape(k, n)
+
+
+def _coupler(eta):
+    """(2, 2, k) [[cos eta, i sin eta], [i sin eta, cos eta]]."""
+    c, sn = np.cos(eta), np.sin(eta)
+    return np.array([[c, 1j * sn], [1j * sn, c]])
+
+
+def _mm(A, B):
+    return np.einsum("ijk,jlk->ilk", A, B)
+
+
+def T_mzi_balanced(p, s=None):
+    """crossing.py:301-305: the MZI with +-theta/2 in the arms, T_mzi exp(-i theta/2)."""
+    p = np.asarray(p, dtype=np.float64).reshape(-1, 2)
+    return T_mzi(p, s) * np.exp(-0.5j * p[:, 0])
+
+
+def T_mzi_outphase(p, s=None):
+    """crossing.py:329-337: phase shifters on the outputs.  T(theta, phi, a, b) is the input-phase MZI with
+    splitters (b + pi/2, a - pi/2), both indices reversed and transposed: T[i][j] = T_in[1-j][1-i]."""
+    p = np.asarray(p, dtype=np.float64).reshape(-1, 2)
+    ab = _splits(s, p.shape[0], 2)
+    Ti = T_mzi(p, np.stack([ab[:, 1] + np.pi / 2, ab[:, 0] - np.pi / 2], 1))
+    return Ti[::-1, ::-1].transpose(1, 0, 2)
+
+
+def T_mzi3(p, s=None):
+    """crossing.py:397-416: an extra coupler eta before the MZI, T = T_mzi(a, b) C(eta); s = (a, b, eta)."""
+    p = np.asarray(p, dtype=np.float64).reshape(-1, 2)
+    sp = _splits(s, p.shape[0], 3)
+    return _mm(T_mzi(p, sp[:, :2]), _coupler(sp[:, 2]))
+
+
+def T_mzi3_outphase(p, s=None):
+    """crossing.py:397-406, 425-442: the output-phase MZI followed by the coupler, C(eta) T_out(a, b)."""
+    p = np.asarray(p, dtype=np.float64).reshape(-1, 2)
+    sp = _splits(s, p.shape[0], 3)
+    return _mm(_coupler(sp[:, 2]), T_mzi_outphase(p, sp[:, :2]))
+
+
+def T_mzi_generic_outphase(p, s=None):
+    """crossing.py:476-481 (out_phase True): the generic MZI flipped, T = R(D1) S(alpha) R(D2) S(beta) with
+    R(D) the diagonal D with its entries swapped (same parameters as T_mzi_generic)."""
+    p = np.asarray(p, dtype=np.float64).reshape(-1, 2)
+    k = p.shape[0]
+    sp = _splits(s, k, 14)
+    th, ph = p[:, 0], p[:, 1]
+    d1 = (np.exp(1j * (ph + sp[:, 2] + sp[:, 6]) + sp[:, 10] / 2), np.exp(1j * (sp[:, 3] + sp[:, 7]) + sp[:, 11] / 2))
+    d2 = (np.exp(1j * (th + sp[:, 4] + sp[:, 8]) + sp[:, 12] / 2), np.exp(1j * (sp[:, 5] + sp[:, 9]) + sp[:, 13] / 2))
+    z = np.zeros(k)
+    R1 = np.array([[d1[1], z], [z, d1[0]]])
+    R2 = np.array([[d2[1], z], [z, d2[0]]])
+    return _mm(R1, _mm(_coupler(np.pi / 4 + sp[:, 0]), _mm(R2, _coupler(np.pi / 4 + sp[:, 1]))))
+
+
+def T_cartesian(p, s=None):
+    """crossing.py:540-544: p = (x, y) in the unit disk around (2, 0) (s = x + iy - 2, T = [[s, i r],
+    [i r, s*]]) or around (-2, 0) (t = x + iy + 2, T = [[i r, t], [t*, i r]]), r = sqrt(1 - |.|^2)."""
+    p = np.asarray(p, dtype=np.float64).reshape(-1, 2)
+    x, y = p[:, 0], p[:, 1]
+    right = x > 0
+    z = (x + 1j * y) - np.where(right, 2.0, -2.0)
+    ir = 1j * np.sqrt(1 - np.abs(z) ** 2)
+    return np.array([[np.where(right, z, ir), np.where(right, ir, z)],
+                     [np.where(right, ir, z.conj()), np.where(right, z.conj(), ir)]])
+
+
+def T_bell(p, s=None):
+    """crossing.py:590-594: the compressed MZI (phases theta, phi in the two arms between the splitters),
+    T = exp(i(theta + phi)/2) [[-C Sp + i Cm S, -Sm S + i Cp C], [Sm S + i Cp C, -C Sp - i Cm S]] with
+    C, S = cos, sin((theta - phi)/2), Cp, Sp = cos, sin(a + b), Cm, Sm = cos, sin(a - b)."""
+    p = np.asarray(p, dtype=np.float64).reshape(-1, 2)
+    th, ph = p[:, 0], p[:, 1]
+    ab = _splits(s, p.shape[0], 2)
+    a, b = ab[:, 0], ab[:, 1]
+    Cp, Cm, C = np.cos(a + b), np.cos(a - b), np.cos((th - ph) / 2)
+    Sp, Sm, S = np.sin(a + b), np.sin(a - b), np.sin((th - ph) / 2)
+    return np.exp(0.5j * (th + ph)) * np.array([[-C * Sp + 1j * Cm * S, -Sm * S + 1j * Cp * C],
+                                                 [Sm * S + 1j * Cp * C, -C * Sp - 1j * Cm * S]])
+
+
+T_FN = {"mzi": T_mzi, "sym": T_sym, "orth": T_orth, "mzi_generic": T_mzi_generic,
+        "mzi_balanced": T_mzi_balanced, "mzi_outphase": T_mzi_outphase, "mzi3": T_mzi3,
+        "mzi3_outphase": T_mzi3_outphase, "mzi_generic_outphase": T_mzi_generic_outphase,
+        "cartesian": T_cartesian, "bell": T_bell}
 DT_FN = {"mzi": dT_mzi, "sym": dT_sym, "orth": dT_orth, "mzi_generic": dT_mzi_generic}
 
 

@@ -287,6 +287,54 @@ def main(ref_path):
          idx_out=np.arange(full.N)[net.idx_out], x=x, y=y, U_target=Z, J=J,
          dJdp=flat_to_grid(dJdp[:n_cr * 2].reshape(n_cr, 2), lens, shifts, full.N, 2), dJdph=dJdp[n_cr * 2:])
 
+    # The reference's other crossing parameterisations (crossing.py:292-611): T of each class on random
+    # parameters, and a small Clements mesh of each through StructuredMeshNetwork.dot (and dot_vjp where the
+    # class has dT).
+    from meshes import crossing as cr
+    classes = [("mzi_balanced", cr.MZICrossingBalanced, 2, False), ("mzi_outphase", cr.MZICrossingOutPhase, 2, True),
+               ("mzi3", cr.MZICrossing3, 3, False), ("mzi3_outphase", cr.MZICrossing3OutPhase, 3, False),
+               ("mzi_generic_outphase", cr.MZICrossingGenericOutPhase, 14, False),
+               ("cartesian", cr.CartesianCrossing, 2, True), ("bell", cr.MZICrossingBell, 2, True)]
+
+    def draw(name, k, n_s):
+        if name == "cartesian":        # inside the unit disks around (+2, 0) and (-2, 0)
+            rho, ang = 0.95 * np.sqrt(rng.uniform(0, 1, k)), rng.uniform(0, 2 * np.pi, k)
+            side = np.where(rng.uniform(0, 1, k) < 0.5, 2.0, -2.0)
+            pp = np.stack([side + rho * np.cos(ang), rho * np.sin(ang)], 1)
+        else:
+            pp = rng.uniform(0, 2 * np.pi, (k, 2))
+        ss = rng.normal(0, 0.05, (k, n_s))
+        if n_s == 14:
+            ss[:, 10:] = -np.abs(rng.normal(0.1, 0.05, (k, 4)))
+        return pp.astype(np.float32).astype(np.float64), ss.astype(np.float32).astype(np.float64)
+
+    out = {}
+    for name, cls, n_s, _ in classes:
+        pp, ss = draw(name, 7, n_s)
+        out[name + "_p"], out[name + "_s"] = pp, ss
+        out[name + "_T"] = np.moveaxis(np.asarray(cls().T(pp, ss)), -1, 0)        # (k, 2, 2)
+    save("crossings_T", **out)
+    for name, cls, n_s, has_dT in classes:
+        N = 6
+        lens, shifts = [int(x) for x in ClementsNetwork(N=N).lens], [int(x) for x in ClementsNetwork(N=N).shifts]
+        n_cr = sum(lens)
+        pp, ss = draw(name, n_cr, n_s)
+        net = StructuredMeshNetwork(N, lens, shifts, p_splitter=ss, X=cls(), is_phase=False)
+        net.p_phase[:] = pp.reshape(-1)
+        B = 4
+        x = (rng.standard_normal((B, N)) + 1j * rng.standard_normal((B, N)))
+        x /= np.linalg.norm(x, axis=1, keepdims=True)
+        y = net.dot(x.T).T
+        extra = {}
+        if has_dT:
+            t = (rng.standard_normal((B, N)) + 1j * rng.standard_normal((B, N)))
+            g = 2 * (y - t)
+            dJdp, dJdv = net.dot_vjp(y.T, g.T)
+            extra = dict(g=g, dJdp=flat_to_grid(dJdp.reshape(n_cr, 2), lens, shifts, N, 2), g_in=dJdv.T)
+        save("xmesh_%s_N%d" % (name, N), N=N, L=len(lens), crossing=name, lens=np.array(lens),
+             shifts=np.array(shifts), p=flat_to_grid(pp, lens, shifts, N, 2), s=flat_to_grid(ss, lens, shifts, N, n_s),
+             x=x, y=y, **extra)
+
     print("wrote", *written, sep="\n  ")
 
 

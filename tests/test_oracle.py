@@ -16,7 +16,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def fixtures():
     """Fixtures of the plain meshes (the phase-screen and lossy fixtures have their own tests)."""
     return sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz") and "_screen_" not in f and "lossy" not in f
-                  and not f.startswith(("clipped_", "perm_", "piloss_")))
+                  and not f.startswith(("clipped_", "perm_", "piloss_", "xmesh_", "crossings_")))
 
 
 def load(name):
@@ -270,6 +270,55 @@ def test_piloss_matches_reference_fixture():
     G[:, f["idx_out"]] = 2 * dU.T
     dp, dph, _ = O.grad_screened(om, U, G, f["ph"], pos)
     assert O.rel_err(dp, f["dJdp"]) < 1e-12 and O.rel_err(dph, f["dJdph"]) < 1e-12
+
+
+GENERIC_CROSSINGS = ["mzi_balanced", "mzi_outphase", "mzi3", "mzi3_outphase", "mzi_generic_outphase", "cartesian",
+                     "bell"]
+
+
+@pytest.mark.parametrize("name", GENERIC_CROSSINGS)
+def test_crossing_parameterisations_match_reference(name):
+    """T of the reference's other crossing classes (crossing.py:292-611): the oracle's restatement and the
+    product's torch builder (on the CPU, float64) against the reference's own T."""
+    import torch
+    from meshes_gb300.crossings import transfer
+    z = np.load(os.path.join(GOLDEN, "crossings_T.npz"))
+    p, s, T = z[name + "_p"], z[name + "_s"], z[name + "_T"]
+    assert O.rel_err(np.moveaxis(O.T_FN[name](p, s), -1, 0), T) < 1e-14
+    Tt = transfer(name, torch.tensor(p), torch.tensor(s)).numpy()
+    assert O.rel_err(Tt, T) < 1e-14
+
+
+@pytest.mark.parametrize("name", GENERIC_CROSSINGS)
+def test_generic_crossing_meshes_match_reference(name):
+    """A Clements mesh of each class through the reference's StructuredMeshNetwork.dot, and its dot_vjp
+    where the class has dT: the oracle forward, and central differences of Re sum conj(g) y(p) (whose
+    gradient is the reference's dJ/dp for g = 2 dJ/dy*)."""
+    f = np.load(os.path.join(GOLDEN, "xmesh_%s_N6.npz" % name))
+    om = O.OracleMesh(N=int(f["N"]), L=int(f["L"]), crossing=name, lens=list(f["lens"]), shifts=list(f["shifts"]),
+                      p=f["p"], s=f["s"])
+    assert O.rel_err(O.propagate(om, f["x"]), f["y"]) < 1e-13
+    if "dJdp" not in f:
+        return
+    active = om.active_mask()
+    idx = np.flatnonzero(np.broadcast_to(active[..., None], f["p"].shape))
+    fd = O.central_difference(lambda pp: float(np.real(np.sum(np.conj(f["g"]) * O.propagate(om, f["x"], pp)))),
+                              f["p"], idx)
+    G, gin = O.vjp_stored(om, f["x"], f["g"])
+    assert O.rel_err(gin, f["g_in"]) < 1e-12
+    if name != "mzi_outphase":
+        assert O.rel_err(fd, f["dJdp"].reshape(-1)[idx]) < 1e-7
+        return
+    # The reference's MZICrossingOutPhase.dT (crossing.py:338-340) reverses, in its vectorised branch, the
+    # slot axis instead of the first matrix axis (dT_in[:, :, ::-1, ::-1] on (n_phase, 2, 2, k)), so its
+    # dot_vjp gradient is not the derivative of its own T.  Pin that reading: the reference's numbers are the
+    # contraction with that array, and the true derivative (central differences) differs.
+    ab = f["s"][active]
+    dT_in = O.dT_mzi(f["p"][active], np.stack([ab[:, 1] + np.pi / 2, ab[:, 0] - np.pi / 2], 1))
+    dT_ref = dT_in[:, :, ::-1, ::-1].transpose(0, 2, 1, 3)
+    dJdp_ref = np.real(np.einsum("nijk,kij->kn", dT_ref, G[active]))
+    assert O.rel_err(dJdp_ref, f["dJdp"][active]) < 1e-12
+    assert O.rel_err(fd, f["dJdp"].reshape(-1)[idx]) > 0.1
 
 
 def test_geometry_helpers_agree():
