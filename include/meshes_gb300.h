@@ -59,7 +59,7 @@ extern "C" {
 
 /* Tile configuration of one launch: modes per lane M (2..16), vectors per lane V, warps per CTA W,
  * layers per pipeline stage CL, pipeline stages S.  Zero fields are filled by the built-in
- * heuristic; the autotuner (meshes_gb300/autotune.py) measures and stores better choices. */
+ * heuristic; the autotuner (mg_autotune, driven by meshes_gb300/autotune.py) measures better choices. */
 typedef struct mg_config {
   int M, V, W, CL, S;
   int split;   /* 0: automatic, 1: two CTA kinds per SM (V and V-1 vectors per lane group), 2: uniform CTAs */
@@ -88,6 +88,21 @@ int mg_read_status(void* workspace, int clear, void* stream);
  * calls that pass no config then use it instead of the heuristic.  cfg = NULL removes the entries of
  * that (op, crossing, geometry, N) (N = 0: all N).  Filled by meshes_gb300.autotune. */
 int mg_set_tuned(int op, int crossing, int geometry, int N, int B_lo, int B_hi, const mg_config* cfg);
+
+/* Autotuner: time the tile configurations of (op in {MG_OP_FWD, MG_OP_FWDDIFF, MG_OP_BWD}, N, L, B, crossing,
+ * geometry) on the caller's mesh (lens/shifts or strides, p/ldp, s/lds: device pointers as for
+ * mg_build_tiles) and return the fastest in *best (its median time in *best_ms).  Stage 1 varies the
+ * register blocking and CTA width (M, V, W); stage 2 varies layers per stage and stages (CL, S) around the
+ * winner and, for forward propagation, the split launch.  Each candidate: tiles built once, two warm-up
+ * launches, `reps` launches timed with CUDA events, the L2 flushed (256 MB write) before each; candidates
+ * whose launches fail or record a kernel status are dropped.  Allocates its scratch stream-ordered, frees it
+ * and synchronises the stream before returning.  record != 0 registers the winner for batch size B
+ * (mg_set_tuned).  tried / tried_ms (may be NULL) receive up to max_tried timed candidates; *n_tried (may
+ * be NULL) their count. */
+int mg_autotune(int op, int N, int L, int B, int crossing, int geometry, const int* lens, const int* shifts,
+                const int* strides, const float* p, int ldp, const float* s, int lds, int reps, int record,
+                mg_config* best, float* best_ms, mg_config* tried, float* tried_ms, int max_tried, int* n_tried,
+                void* stream);
 
 /* The configuration the heuristic picks (filled into *out). */
 int mg_default_config(int op, int N, int B, int crossing, mg_config* out);

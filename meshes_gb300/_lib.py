@@ -8,7 +8,7 @@ from __future__ import annotations
 import ctypes
 import os
 import threading
-from ctypes import POINTER, Structure, c_char_p, c_int, c_size_t, c_uint, c_void_p
+from ctypes import POINTER, Structure, c_char_p, c_float, c_int, c_size_t, c_uint, c_void_p
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libmeshes_gb300.so")
@@ -83,6 +83,9 @@ _SIGS = {
     "mg_build_tiles": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int,
                                c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_int, POINTER(mg_config), c_void_p,
                                c_size_t, c_void_p]),
+    "mg_autotune": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
+                            c_void_p, c_int, c_int, c_int, POINTER(mg_config), POINTER(c_float), POINTER(mg_config),
+                            POINTER(c_float), c_int, POINTER(c_int), c_void_p]),
     "mg_build_perms": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, POINTER(mg_config), c_void_p,
                                c_size_t, c_void_p]),
     "mg_propagate": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int,

@@ -1,10 +1,10 @@
 """Autotuner of the propagation kernels' tile configuration.
 
-For a shape (op, crossing, geometry, N, L, B) it times the valid candidates on the GPU - tiles built
-once, CUDA events on the launch stream, L2 flushed between repetitions - in two stages: the register
-blocking and CTA width (modes per lane M, vectors per lane V, warps per CTA W), then, around the
-winner, layers per pipeline stage CL, stages S and (forward) the split launch - and keeps the
-fastest.
+For a shape (op, crossing, geometry, N, L, B) the library's native tuner ``mg_autotune`` times the valid
+candidates on the GPU - tiles built once, CUDA events on the launch stream, L2 flushed between
+repetitions - in two stages: the register blocking and CTA width (modes per lane M, vectors per lane V,
+warps per CTA W), then, around the winner, layers per pipeline stage CL, stages S and (forward) the split
+launch - and keeps the fastest.  This module supplies a random mesh of the shape and keeps the table.
 Results live in ``tuned_configs.json`` next to this file (keyed by op/crossing/geometry/N and a batch
 range) and are loaded into the library's tuning table by ``load_table()`` (called on import of the
 package), so every call that passes no explicit configuration - the reference-shaped entry points
@@ -15,11 +15,11 @@ included - uses them.
 from __future__ import annotations
 
 import argparse
-import itertools
+import ctypes
 import json
 import os
 import statistics
-from typing import Dict, List, Optional, Tuple
+from typing import Dict, Optional, Tuple
 
 import numpy as np
 
@@ -52,24 +52,6 @@ def load_table(path: str = TABLE) -> int:
     return n
 
 
-def candidates(op: int, N: int, real: bool) -> List[Tuple[int, ...]]:
-    """Stage 1: the register blocking and CTA width (M, V, W), pipeline and schedule left to the heuristic."""
-    Np = 1 << max(1, (N - 1).bit_length())
-    Ms = [m for m in (2, 4, 8, 16) if m <= Np and Np // m <= 32]
-    Vs = {OP_FWD: (2, 4, 8), OP_FWDDIFF: (1, 2, 4), OP_BWD: (1, 2, 4)}[op]
-    return [(M, V, W, 0, 0, 2) for M, V, W in itertools.product(Ms, Vs, (2, 4, 8))]
-
-
-def refinements(c: Tuple[int, ...], op: int = OP_FWD) -> List[Tuple[int, ...]]:
-    """Stage 2 around a stage-1 winner: layers per pipeline stage CL and stages S; for forward
-    propagation also the split launch (two 4-warp CTAs per SM with V and V-1 vectors per lane group)."""
-    M, V, W = c[:3]
-    out = [(M, V, W, CL, S, 2) for CL, S in itertools.product((0, 4, 8, 16), (2, 3))]
-    if op == OP_FWD and V >= 2:
-        out += [(M, V, 4, CL, S, 1) for CL, S in itertools.product((0, 4, 6, 8, 12), (2, 3))]
-    return out
-
-
 def tune(op: int, N: int, L: int, B: int, crossing: int = 0, geometry: int = 0, reps: int = 5,
          cands: Optional[list] = None, device=None) -> Tuple[Tuple[int, ...], Dict]:
     """Time the candidates on a random mesh of this shape; returns (best config, {config: ms})."""
@@ -93,6 +75,26 @@ def tune(op: int, N: int, L: int, B: int, crossing: int = 0, geometry: int = 0, 
         geo_args = (None, None, st_d.data_ptr())
     p = torch.tensor(rng.uniform(0, 6.28, (L, N // 2, n_p)).astype(np.float32), device=dev)
     s = torch.tensor(rng.normal(0, .02, (L, N // 2, max(n_s, 1))).astype(np.float32), device=dev) if n_s else None
+    if cands:
+        return _time_given(op, N, L, B, crossing, geometry, geo_args, p, s, n_p, n_s, reps, cands, dev, st)
+    best = _lib.mg_config()
+    best_ms = ctypes.c_float()
+    tried = (_lib.mg_config * 256)()
+    tried_ms = (ctypes.c_float * 256)()
+    n = ctypes.c_int()
+    check(lib.mg_autotune(op, N, L, B, crossing, geometry, *geo_args, p.data_ptr(), N // 2 * n_p,
+                          None if s is None else s.data_ptr(), N // 2 * n_s, reps, 0, ctypes.byref(best),
+                          ctypes.byref(best_ms), tried, tried_ms, 256, ctypes.byref(n), st), "mg_autotune")
+    as_tuple = (lambda c: (c.M, c.V, c.W, c.CL, c.S, c.split))
+    results = {as_tuple(tried[i]): float(tried_ms[i]) for i in range(min(n.value, 256))}
+    return as_tuple(best), results
+
+
+def _time_given(op, N, L, B, crossing, geometry, geo_args, p, s, n_p, n_s, reps, cands, dev, st):
+    """Time an explicit candidate list (for comparisons of chosen configurations)."""
+    import torch
+    lib = load()
+    real = crossing == 2
     dt = torch.float32 if real else torch.complex64
     x = torch.randn(B, N, dtype=dt, device=dev)
     y = torch.empty_like(x)
@@ -100,18 +102,17 @@ def tune(op: int, N: int, L: int, B: int, crossing: int = 0, geometry: int = 0, 
     gi = torch.empty_like(x)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     results = {}
-
-    def measure(c):
+    for c in cands:
         cfg = _lib.config(*c)
         nb = lib.mg_workspace_bytes(op, N, L, B, crossing, geometry, _lib.cfg_ptr(cfg))
         if nb == 0:
-            return
+            continue
         ws = torch.empty(nb, dtype=torch.uint8, device=dev)
         lib.mg_workspace_init(ws.data_ptr(), nb, st)
         if lib.mg_build_tiles(op, N, L, geometry, *geo_args, crossing, p.data_ptr(), N // 2 * n_p,
                               None if s is None else s.data_ptr(), N // 2 * n_s, p.data_ptr() if op == OP_FWDDIFF
                               else None, None, None, B, _lib.cfg_ptr(cfg), ws.data_ptr(), nb, st):
-            return
+            continue
         args = {OP_FWD: (x.data_ptr(), None, y.data_ptr(), None), OP_FWDDIFF: (x.data_ptr(), g.data_ptr(),
                 y.data_ptr(), gi.data_ptr()), OP_BWD: (y.data_ptr(), g.data_ptr(), None, gi.data_ptr())}[op]
 
@@ -120,7 +121,7 @@ def tune(op: int, N: int, L: int, B: int, crossing: int = 0, geometry: int = 0, 
                                     ws.data_ptr(), nb, st)
 
         if run():
-            return
+            continue
         ts = []
         for _ in range(reps):
             flush.zero_()
@@ -132,13 +133,6 @@ def tune(op: int, N: int, L: int, B: int, crossing: int = 0, geometry: int = 0, 
             ts.append(e0.elapsed_time(e1))
         if lib.mg_read_status(ws.data_ptr(), 1, st) == 0:
             results[c] = statistics.median(ts)
-
-    for c in (cands or candidates(op, N, real)):
-        measure(c)
-    if not cands and results:
-        for c in refinements(min(results, key=results.get), op):
-            if c not in results:
-                measure(c)
     best = min(results, key=results.get)
     return best, results
 
