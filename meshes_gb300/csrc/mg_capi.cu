@@ -349,8 +349,11 @@ int run_prop(const Plan& P, const void* in0, const void* in1, void* out0, void* 
   lc.stream = st;
   cudaError_t e;
   a.nA = P.nA;
-  e = P.split ? launch_prop_split(P.op, P.real, P.M, P.V, P.G == 32, P.gr, lc, a)
-              : launch_prop(P.op, P.real, P.M, P.V, P.G == 32, P.gr, lc, a);
+  if (!P.perm && P.geometry == GEO_NN && P.G == 32 && nn_instantiated(P.op, P.real, P.M, P.V, P.gr, P.split))
+    e = launch_prop_nn(P.op, P.real, P.M, P.V, P.gr, P.split, lc, a);
+  else
+    e = P.split ? launch_prop_split(P.op, P.real, P.M, P.V, P.G == 32, P.gr, lc, a)
+                : launch_prop(P.op, P.real, P.M, P.V, P.G == 32, P.gr, lc, a);
   if (e != cudaSuccess) return cuda_fail(e, "prop_kernel launch");
   if (P.op == OP_BWD && dp && P.L > 0) {
     const int n = P.L * P.np2;

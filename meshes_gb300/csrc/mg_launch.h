@@ -37,20 +37,20 @@ inline cudaError_t ensure_smem_attr(K kernel, std::atomic<unsigned long long>& d
   return cudaSuccess;
 }
 
-template <int OP, int M, int V, bool REAL, int GT, int GR, bool PERM = false>
+template <int OP, int M, int V, bool REAL, int GT, int GR, bool PERM = false, bool NN = false>
 inline cudaError_t launch_one(const LaunchCfg& lc, const PropArgs& a) {
   static std::atomic<unsigned long long> done{0};
-  auto k = prop_kernel<OP, M, V, REAL, GT, GR, PERM>;
+  auto k = prop_kernel<OP, M, V, REAL, GT, GR, PERM, NN>;
   cudaError_t e = ensure_smem_attr(k, done);
   if (e != cudaSuccess) return e;
   k<<<lc.grid, lc.block, lc.smem, lc.stream>>>(a);
   return cudaGetLastError();
 }
 
-template <int OP, int M, int V, bool REAL, int GT, int GR>
+template <int OP, int M, int V, bool REAL, int GT, int GR, bool NN = false>
 inline cudaError_t launch_split(const LaunchCfg& lc, const PropArgs& a) {
   static std::atomic<unsigned long long> done{0};
-  auto k = prop_split_kernel<OP, M, V, REAL, GT, GR>;
+  auto k = prop_split_kernel<OP, M, V, REAL, GT, GR, NN>;
   cudaError_t e = ensure_smem_attr(k, done);
   if (e != cudaSuccess) return e;
   k<<<lc.grid, lc.block, lc.smem, lc.stream>>>(a);
@@ -73,6 +73,11 @@ cudaError_t launch_prop(int op, bool real, int M, int V, bool full, int gr, cons
 // (op, M) and the gradient mode of each crossing (mg_prop_perm_*.cu)
 bool perm_instantiated(int op, bool real, int M, int V, int gr);
 cudaError_t launch_prop_perm(int op, bool real, int M, int V, int gr, const LaunchCfg& lc, const PropArgs& a);
+// nearest-neighbour instantiations (layer kinds 0 and odd-shift only) of the full-warp configurations in
+// nn_instantiated(), uniform or split (mg_prop_nn.cu)
+bool nn_instantiated(int op, bool real, int M, int V, int gr, bool split);
+cudaError_t launch_prop_nn(int op, bool real, int M, int V, int gr, bool split, const LaunchCfg& lc,
+                           const PropArgs& a);
 // split launches (two CTA kinds per SM); instantiated only for the full-warp configurations in
 // split_instantiated()
 bool split_instantiated(int op, bool real, int M, int V, bool full, int gr);

@@ -385,10 +385,16 @@ __device__ __forceinline__ void layer_xl(const float4* tl, int d, int G, int j, 
   }
 }
 
-// ---- one layer of any kind
-template <int OP, int M, int V, bool REAL, int GR, typename F>
+// ---- one layer of any kind; NN (nearest-neighbour instantiations): kinds 0 and KIND_MIS only, which keeps
+// the strided and butterfly bodies, and their registers, out of the kernel
+template <int OP, int M, int V, bool REAL, int GR, bool NN = false, typename F>
 __device__ __forceinline__ void layer_any(int kind, const float4* tl, int G, int j, int r, F (&u)[V][M],
                                           F (&w)[V][M], float4* gl) {
+  if constexpr (NN) {
+    if (kind == KIND_MIS) layer_mis<OP, M, V, REAL, GR>(tl, G, j, r, u, w, gl);
+    else layer_local<OP, M, V, REAL, GR, 1>(tl, G, j, r, u, w, gl);
+    return;
+  }
   switch (kind) {
     case 0: layer_local<OP, M, V, REAL, GR, 1>(tl, G, j, r, u, w, gl); break;
     case 1: if constexpr (M >= 4) layer_local<OP, M, V, REAL, GR, 2>(tl, G, j, r, u, w, gl); break;
@@ -651,7 +657,7 @@ struct PropTraits {
 // layer's input to a.act before applying it, back-propagation reloads it in place of T^H reconstruction.
 // PERM (the permuted-mesh instantiations): a layer whose kind carries KIND_PERM is preceded by the gather of
 // its row of pa.perm (the shared-memory copy of the kinds carries the flags).
-template <int OP, int M, int V, bool REAL, int GR, bool PERM, typename F>
+template <int OP, int M, int V, bool REAL, int GR, bool PERM, bool NN, typename F>
 __device__ __forceinline__ void run_chunk(const PropArgs& pa, int vb0, const int* kinds, const unsigned char* st,
                                           unsigned layer_bytes, int lo, int hi, unsigned char* gst_warp,
                                           size_t gst_layer, int G, int j, int r, F (&u)[V][M], F (&w)[V][M],
@@ -699,14 +705,14 @@ __device__ __forceinline__ void run_chunk(const PropArgs& pa, int vb0, const int
         continue;
       }
     }
-    layer_any<OP, M, V, REAL, GR>(k0, t0, G, j, r, u, w, g0);
+    layer_any<OP, M, V, REAL, GR, NN>(k0, t0, G, j, r, u, w, g0);
     i += 1;
   }
 }
 
 // One batch tile of one mesh: vectors [a.v0, a.vend), all L layers, by the W warps of the CTA.
 // Shared by the one-mesh kernel (prop_kernel) and the persistent multi-mesh kernel (mg_batched.cu).
-template <int OP, int M, int V, bool REAL, int GT, int GR, bool PERM = false>
+template <int OP, int M, int V, bool REAL, int GT, int GR, bool PERM = false, bool NN = false>
 __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem) {
   using F = typename Fld<REAL>::T;
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -806,8 +812,8 @@ __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem
       if (tid == 0) issue_d(c);
     }
     const unsigned char* st = ring + (size_t)(c % a.S) * a.CL * a.layer_bytes;
-    run_chunk<OP, M, V, REAL, GR, PERM>(a, vb0, kinds, st, a.layer_bytes, lo, hi, gst_warp, gst_layer, G, j, r, u, w,
-                                        pscr);
+    run_chunk<OP, M, V, REAL, GR, PERM, NN>(a, vb0, kinds, st, a.layer_bytes, lo, hi, gst_warp, gst_layer, G, j, r, u,
+                                            w, pscr);
     __syncthreads();
     if constexpr (OP == OP_BWD && kDirect) chunk_reduce_direct<M, GR>(a, kinds, lo, hi - lo, gst, np2, G);
     if constexpr (OP == OP_BWD && GR == 4) chunk_reduce_raw<M>(a, kinds, lo, hi - lo, gst, np2, G);
@@ -837,7 +843,7 @@ __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem
   if constexpr (OP != OP_FWD) store_fields<M, V, REAL>(w, a.out1, vb0, a.vend, a.N, a.ldu, j);
 }
 
-template <int OP, int M, int V, bool REAL, int GT, int GR, bool PERM = false>
+template <int OP, int M, int V, bool REAL, int GT, int GR, bool PERM = false, bool NN = false>
 __global__ void __launch_bounds__(PropTraits<OP, M, V, REAL>::kMaxThreads)
 prop_kernel(const PropArgs a0) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -846,14 +852,14 @@ prop_kernel(const PropArgs a0) {
   a.v0 = blockIdx.x * (a.W * (32 / G) * V);
   a.vend = a.B;
   if (OP == OP_BWD) a.partial = a0.partial + (size_t)blockIdx.x * a.L * ((G * M) >> 1) * (GR == 4 ? 4 : 1);
-  prop_body<OP, M, V, REAL, GT, GR, PERM>(a, smem);
+  prop_body<OP, M, V, REAL, GT, GR, PERM, NN>(a, smem);
 }
 
 // Split launch for a batch that one wave of full CTAs cannot spread evenly: two CTAs per SM, the first
 // nA CTAs with V vectors per lane group, the others with V-1, so that each SM scheduler carries one
 // warp of each kind (2V-1 vectors) instead of two full warps on some SMs and none on others.  The two
 // bodies are separate code paths chosen once per CTA.
-template <int OP, int M, int V, bool REAL, int GT, int GR>
+template <int OP, int M, int V, bool REAL, int GT, int GR, bool NN = false>
 __global__ void __launch_bounds__(PropTraits<OP, M, V, REAL>::kMaxThreads, 1)
 prop_split_kernel(const PropArgs a0) {
   static_assert(V >= 2, "a split launch needs V >= 2");
@@ -865,10 +871,10 @@ prop_split_kernel(const PropArgs a0) {
   if (OP == OP_BWD) a.partial = a0.partial + (size_t)blockIdx.x * a.L * ((G * M) >> 1) * (GR == 4 ? 4 : 1);
   if ((int)blockIdx.x < a.nA) {
     a.v0 = blockIdx.x * groups * V;
-    prop_body<OP, M, V, REAL, GT, GR>(a, smem);
+    prop_body<OP, M, V, REAL, GT, GR, false, NN>(a, smem);
   } else {
     a.v0 = a.nA * groups * V + (blockIdx.x - a.nA) * groups * (V - 1);
-    prop_body<OP, M, V - 1, REAL, GT, GR>(a, smem);
+    prop_body<OP, M, V - 1, REAL, GT, GR, false, NN>(a, smem);
   }
 }
 
