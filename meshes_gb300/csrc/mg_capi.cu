@@ -665,6 +665,8 @@ int mg_propagate(int op, int N, int L, int B, int crossing, int geometry, const 
     TRY(make_plan(OP_BWD, N, L, B, crossing, geometry, cfg, &Pb));
     TRY(check_ws(Pb, ws, wsb));
     mg_config cf = {Pb.M, 0, 0, 0, 0, cfg ? cfg->split : 0};
+    mg_config tf;   // a measured forward configuration of this shape applies if its M matches the tiles'
+    if (!cfg && !Pb.perm && lookup_tuned(OP_FWD, crossing, Pb.geometry, N, B, &tf) && tf.M == Pb.M) cf = tf;
     TRY(make_plan(OP_FWD, N, L, B, crossing, geometry, &cf, &Pf));
     Pf.lb = Pb.lb;
     Pf.off_kinds = Pb.off_kinds;
@@ -676,7 +678,7 @@ int mg_propagate(int op, int N, int L, int B, int crossing, int geometry, const 
       Pf.smem = launch_smem(Pf, OP_FWD, 0, L);
       if (Pf.smem <= budget && (size_t)Pf.CL * Pf.lb < (1u << 20)) break;
       if (Pf.CL == 1) return fail(MG_E_CONFIG, "no pipeline depth fits shared memory");
-      Pf.CL = std::max(1, Pf.CL / 2);
+      Pf.CL -= 1;   // the back-propagation tiles are larger than the forward ones the plan was sized for
     }
     TRY(check_ldu(Pf, ldu));
     TRY(check_field(in0, "in0", Pf.real, B > 0));

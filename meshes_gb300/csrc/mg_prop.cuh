@@ -692,13 +692,16 @@ __device__ __forceinline__ void run_chunk(const PropArgs& pa, int vb0, const int
       const int k1 = kinds[l1];
       const float4* t1 = reinterpret_cast<const float4*>(st + (size_t)(l1 - lo) * layer_bytes);
       float4* g1 = reinterpret_cast<float4*>(gst_warp + (size_t)(l1 - lo) * gst_layer);
-      if (k0 == 0 && k1 == KIND_MIS) {
+      // the nearest-neighbour instantiations fuse only the order their walk meets in an alternating mesh
+      // (aligned then odd-shift going forward, odd-shift then aligned going back): the second fused body
+      // made the back-propagation kernel spill (measured on GB300: 5% slower with both bodies)
+      if ((!NN || OP != OP_BWD) && k0 == 0 && k1 == KIND_MIS) {
         layer_local<OP, M, V, REAL, GR, 1>(t0, G, j, r, u, w, g0);
         layer_mis<OP, M, V, REAL, GR>(t1, G, j, r, u, w, g1);
         i += 2;
         continue;
       }
-      if (k0 == KIND_MIS && k1 == 0) {
+      if ((!NN || OP == OP_BWD) && k0 == KIND_MIS && k1 == 0) {
         layer_mis<OP, M, V, REAL, GR>(t0, G, j, r, u, w, g0);
         layer_local<OP, M, V, REAL, GR, 1>(t1, G, j, r, u, w, g1);
         i += 2;
