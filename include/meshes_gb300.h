@@ -204,6 +204,10 @@ int mg_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_co
  * zeroed by the caller before each launch, e.g. a memset node of a captured CUDA graph) in array
  * order, so items sorted longest-first balance the load.  Back-propagation items write partials
  * at mesh.partial + part * L * Np/2 (float2); mg_batched_reduce sums them in order into mesh.dp. */
+/* OR-ed into mg_batched_propagate's op: every mesh of the launch is nearest-neighbour (lens/shifts), so
+ * the launch runs the kernel bodies without strided layers (fewer registers); an item whose mesh has
+ * another layer kind records MG_ST_BAD_GEOMETRY and is skipped. */
+#define MG_BATCH_NN 16
 #define MG_BCLS_C8 0
 #define MG_BCLS_C16 1
 #define MG_BCLS_R8 2

@@ -17,6 +17,7 @@ MZI, SYM, ORTH, GENERIC = 0, 1, 2, 3
 OP_FWD, OP_FWDDIFF, OP_BWD, OP_FWD_BWDTILES, OP_BWD_STORED = 0, 1, 2, 3, 4
 GEO_NN, GEO_FFT = 0, 1
 GEO_PERM = 4          # OR-ed into a geometry: permutations between layers (mg_build_perms)
+BATCH_NN = 16         # OR-ed into mg_batched_propagate's op: all meshes nearest-neighbour
 CROSSING_CODES = {"mzi": MZI, "sym": SYM, "orth": ORTH, "generic": GENERIC}
 STATUS_NAMES = {0: "ok", 1: "timeout", 2: "bad geometry", 3: "bad work item"}
 

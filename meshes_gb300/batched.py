@@ -17,7 +17,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._lib import OP_BWD, OP_FWD, check, load, mg_batch_item, mg_batch_mesh, mg_plan_info
+from ._lib import BATCH_NN, GEO_NN, OP_BWD, OP_FWD, check, load, mg_batch_item, mg_batch_mesh, mg_plan_info
 from .mesh import MeshNetworkGPU, _stream
 
 BCLS_C8, BCLS_C16, BCLS_R8 = 0, 1, 2
@@ -176,7 +176,9 @@ class BatchedMeshes:
         lib = _bind()
         stream = _stream(self.device)
         self.head.zero_()
-        check(lib.mg_batched_propagate(op, self.desc[op].data_ptr(), len(self.states), self.items.data_ptr(),
+        # all meshes nearest-neighbour: the kernel bodies without strided layers (MG_BATCH_NN)
+        nn = BATCH_NN if all(st.mesh.geometry == GEO_NN for st in self.states) else 0
+        check(lib.mg_batched_propagate(op | nn, self.desc[op].data_ptr(), len(self.states), self.items.data_ptr(),
                                        self.n_items, self.head.data_ptr(), self.grid, self.smem[op],
                                        self.status.data_ptr(), stream), "mg_batched_propagate")
         if op == OP_BWD:

@@ -19,7 +19,9 @@ constexpr int kBatchWarps = 8;
 
 __device__ __forceinline__ int cls_M(int cls) { return cls == MG_BCLS_C16 ? 16 : 8; }
 
-template <int OP>
+// NN: every mesh of the launch is nearest-neighbour (layer kinds 0 and odd-shift), so the bodies without
+// the strided and butterfly layers run (fewer registers; a mesh with another kind is refused per item)
+template <int OP, bool NN>
 __global__ void __launch_bounds__(kBatchWarps * 32, 1)
 batched_kernel(const mg_batch_mesh* __restrict__ meshes, int n_meshes, const mg_batch_item* __restrict__ items,
                int n_items, int* head, int* status) {
@@ -55,9 +57,9 @@ batched_kernel(const mg_batch_mesh* __restrict__ meshes, int n_meshes, const mg_
     a.target = nullptr;
     a.perm = a.pflags = a.perm_last = a.pflag_last = nullptr;   // batched meshes carry no permutations
     switch (md.cls) {
-      case MG_BCLS_C8: prop_body<OP, 8, 4, false, 0, (OP == OP_BWD ? 1 : 0)>(a, smem); break;
-      case MG_BCLS_C16: prop_body<OP, 16, 2, false, 0, (OP == OP_BWD ? 1 : 0)>(a, smem); break;
-      case MG_BCLS_R8: prop_body<OP, 8, 4, true, 0, (OP == OP_BWD ? 2 : 0)>(a, smem); break;
+      case MG_BCLS_C8: prop_body<OP, 8, 4, false, 0, (OP == OP_BWD ? 1 : 0), false, NN>(a, smem); break;
+      case MG_BCLS_C16: prop_body<OP, 16, 2, false, 0, (OP == OP_BWD ? 1 : 0), false, NN>(a, smem); break;
+      case MG_BCLS_R8: prop_body<OP, 8, 4, true, 0, (OP == OP_BWD ? 2 : 0), false, NN>(a, smem); break;
       default:
         if (threadIdx.x == 0) set_status(status, ST_BAD_WORK);
     }
@@ -97,8 +99,22 @@ __global__ void batched_reduce_kernel(const mg_batch_mesh* __restrict__ meshes) 
 
 using namespace mg;
 
+namespace {
+template <int OP, bool NN>
+cudaError_t launch_batched(const mg_batch_mesh* meshes, int n_meshes, const mg_batch_item* items, int n_items, int* head,
+                           int grid, size_t smem, int* status, cudaStream_t st) {
+  static std::atomic<unsigned long long> done{0};
+  cudaError_t e = ensure_smem_attr(batched_kernel<OP, NN>, done);
+  if (e == cudaSuccess)
+    batched_kernel<OP, NN><<<grid, kBatchWarps * 32, smem, st>>>(meshes, n_meshes, items, n_items, head, status);
+  return e;
+}
+}  // namespace
+
 extern "C" int mg_batched_propagate(int op, const mg_batch_mesh* meshes, int n_meshes, const mg_batch_item* items,
                                     int n_items, int* head, int grid, size_t smem, int* status, void* stream) {
+  const bool nn = (op & MG_BATCH_NN) != 0;
+  op &= ~MG_BATCH_NN;
   if (op != MG_OP_FWD && op != MG_OP_BWD) return set_last_error(MG_E_ARG, "batched op must be fwd or bwd");
   if (!meshes || n_meshes < 0 || (!items && n_items > 0) || !head || grid < 1)
     return set_last_error(MG_E_ARG, "batched launch: bad arguments");
@@ -110,15 +126,12 @@ extern "C" int mg_batched_propagate(int op, const mg_batch_mesh* meshes, int n_m
   (void)cudaGetLastError();   // start from a clean error state: launch errors below are this call's
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t e;
-  if (op == MG_OP_FWD) {
-    static std::atomic<unsigned long long> done{0};
-    e = ensure_smem_attr(batched_kernel<OP_FWD>, done);
-    if (e == cudaSuccess) batched_kernel<OP_FWD><<<grid, kBatchWarps * 32, smem, st>>>(meshes, n_meshes, items, n_items, head, status);
-  } else {
-    static std::atomic<unsigned long long> done{0};
-    e = ensure_smem_attr(batched_kernel<OP_BWD>, done);
-    if (e == cudaSuccess) batched_kernel<OP_BWD><<<grid, kBatchWarps * 32, smem, st>>>(meshes, n_meshes, items, n_items, head, status);
-  }
+  if (op == MG_OP_FWD)
+    e = nn ? launch_batched<OP_FWD, true>(meshes, n_meshes, items, n_items, head, grid, smem, status, st)
+           : launch_batched<OP_FWD, false>(meshes, n_meshes, items, n_items, head, grid, smem, status, st);
+  else
+    e = nn ? launch_batched<OP_BWD, true>(meshes, n_meshes, items, n_items, head, grid, smem, status, st)
+           : launch_batched<OP_BWD, false>(meshes, n_meshes, items, n_items, head, grid, smem, status, st);
   if (e == cudaSuccess) e = cudaGetLastError();
   return e == cudaSuccess ? MG_OK : set_last_error(MG_E_CUDA, "batched_kernel: %s", cudaGetErrorString(e));
 }

@@ -108,3 +108,44 @@ def test_many_items_per_cta():
         assert O.rel_err(st.y.cpu().numpy(), y_ref) < TOL, (om.N, om.crossing)
         assert O.rel_err(st.gx.cpu().numpy(), gin) < TOL, (om.N, om.crossing)
         assert O.rel_err(st.dp.cpu().numpy(), O.contract_dp(om, G)) < TOL, (om.N, om.crossing)
+
+
+def test_nearest_neighbour_launch():
+    """A batch of nearest-neighbour meshes only (Clements, Reck; mzi and orth) runs the nearest-neighbour
+    bodies (MG_BATCH_NN) with the same results as the oracle; forcing that launch on a batch holding a
+    butterfly mesh refuses the butterfly's items with a status and leaves the other results intact."""
+    from meshes_gb300 import _lib
+    from meshes_gb300.batched import BatchedMeshes, _bind
+    rng = np.random.default_rng(34)
+    specs = [("clements", "mzi", 256, 300), ("reck", "mzi", 64, 90), ("clements", "orth", 128, 50),
+             ("clements", "mzi", 512, 7), ("reck", "orth", 16, 33)]
+    oms = [O.random_mesh(rng, N, geo, cr, 0.01 if cr == "mzi" else 0.0) for geo, cr, N, _ in specs]
+    xs = [O.unit_columns(rng, om.N, B, real=om.crossing == "orth") for om, (*_, B) in zip(oms, specs)]
+    gs = [O.unit_columns(rng, om.N, B, real=om.crossing == "orth") for om, (*_, B) in zip(oms, specs)]
+    bm = BatchedMeshes([gpu_mesh(om) for om in oms], [x.shape[0] for x in xs])
+    for st, x in zip(bm.states, xs):
+        st.x.copy_(torch.tensor(x, dtype=st.x.dtype))
+    bm.forward()
+    for st, g in zip(bm.states, gs):
+        st.gy.copy_(torch.tensor(g, dtype=st.gy.dtype))
+    bm.backward()
+    assert bm.check_status() == 0
+    for om, st, x, g in zip(oms, bm.states, xs, gs):
+        y_ref = O.propagate(om, x)
+        G, _, gin = O.vjp_unitary(om, y_ref, g)
+        assert O.rel_err(st.y.cpu().numpy(), y_ref) < TOL, (om.N, om.crossing)
+        assert O.rel_err(st.gx.cpu().numpy(), gin) < TOL, (om.N, om.crossing)
+        assert O.rel_err(st.dp.cpu().numpy(), O.contract_dp(om, G)) < TOL, (om.N, om.crossing)
+
+    oms2 = [O.random_mesh(rng, 64, "clements", "mzi", 0.01), O.random_mesh(rng, 64, "fft", "mzi", 0.01)]
+    xs2 = [O.unit_columns(rng, 64, 40) for _ in oms2]
+    bm2 = BatchedMeshes([gpu_mesh(om) for om in oms2], [40, 40])
+    for st, x in zip(bm2.states, xs2):
+        st.x.copy_(torch.tensor(x, dtype=st.x.dtype))
+    lib = _bind()
+    bm2.head.zero_()
+    _lib.check(lib.mg_batched_propagate(_lib.OP_FWD | _lib.BATCH_NN, bm2.desc[0].data_ptr(), 2, bm2.items.data_ptr(),
+                                        bm2.n_items, bm2.head.data_ptr(), bm2.grid, bm2.smem[0], bm2.status.data_ptr(),
+                                        torch.cuda.current_stream().cuda_stream), "mg_batched_propagate")
+    assert bm2.check_status() == 2
+    assert O.rel_err(bm2.states[0].y.cpu().numpy(), O.propagate(oms2[0], xs2[0])) < TOL
