@@ -56,6 +56,19 @@ batched_kernel(const mg_batch_mesh* __restrict__ meshes, int n_meshes, const mg_
     a.v0 = it.v0; a.vend = it.vend;
     a.target = nullptr;
     a.perm = a.pflags = a.perm_last = a.pflag_last = nullptr;   // batched meshes carry no permutations
+    if constexpr (NN) {
+      // the nearest-neighbour bodies know layer kinds 0 and odd-shift only: an item whose mesh has another
+      // kind is refused (status, no output)
+      int bad = 0;
+      for (int l = threadIdx.x; l < md.L; l += blockDim.x) {
+        const int k = __ldg(md.kinds + l);
+        bad |= (k != 0 && k != KIND_MIS);
+      }
+      if (__syncthreads_or(bad)) {
+        if (threadIdx.x == 0) set_status(status, ST_BAD_GEOMETRY);
+        continue;
+      }
+    }
     switch (md.cls) {
       case MG_BCLS_C8: prop_body<OP, 8, 4, false, 0, (OP == OP_BWD ? 1 : 0), false, NN>(a, smem); break;
       case MG_BCLS_C16: prop_body<OP, 16, 2, false, 0, (OP == OP_BWD ? 1 : 0), false, NN>(a, smem); break;

@@ -349,8 +349,8 @@ int run_prop(const Plan& P, const void* in0, const void* in1, void* out0, void* 
   lc.stream = st;
   cudaError_t e;
   a.nA = P.nA;
-  if (!P.perm && P.geometry == GEO_NN && P.G == 32 && nn_instantiated(P.op, P.real, P.M, P.V, P.gr, P.split))
-    e = launch_prop_nn(P.op, P.real, P.M, P.V, P.gr, P.split, lc, a);
+  if (!P.perm && P.geometry == GEO_NN && nn_instantiated(P.op, P.real, P.M, P.V, P.gr, P.G == 32, P.split))
+    e = launch_prop_nn(P.op, P.real, P.M, P.V, P.gr, P.G == 32, P.split, lc, a);
   else
     e = P.split ? launch_prop_split(P.op, P.real, P.M, P.V, P.G == 32, P.gr, lc, a)
                 : launch_prop(P.op, P.real, P.M, P.V, P.G == 32, P.gr, lc, a);

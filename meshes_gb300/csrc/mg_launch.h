@@ -73,10 +73,10 @@ cudaError_t launch_prop(int op, bool real, int M, int V, bool full, int gr, cons
 // (op, M) and the gradient mode of each crossing (mg_prop_perm_*.cu)
 bool perm_instantiated(int op, bool real, int M, int V, int gr);
 cudaError_t launch_prop_perm(int op, bool real, int M, int V, int gr, const LaunchCfg& lc, const PropArgs& a);
-// nearest-neighbour instantiations (layer kinds 0 and odd-shift only) of the full-warp configurations in
+// nearest-neighbour instantiations (layer kinds 0 and odd-shift only) of the configurations in
 // nn_instantiated(), uniform or split (mg_prop_nn.cu)
-bool nn_instantiated(int op, bool real, int M, int V, int gr, bool split);
-cudaError_t launch_prop_nn(int op, bool real, int M, int V, int gr, bool split, const LaunchCfg& lc,
+bool nn_instantiated(int op, bool real, int M, int V, int gr, bool full, bool split);
+cudaError_t launch_prop_nn(int op, bool real, int M, int V, int gr, bool full, bool split, const LaunchCfg& lc,
                            const PropArgs& a);
 // split launches (two CTA kinds per SM); instantiated only for the full-warp configurations in
 // split_instantiated()

@@ -736,19 +736,7 @@ __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem
   uint64_t* bars = reinterpret_cast<uint64_t*>(gst + gst_bytes);   // [S] ring, [S] = dT/dp buffer
   int* skinds = reinterpret_cast<int*>(bars + a.S + 1);
   const int* kinds = a.kinds;
-  if constexpr (NN) {
-    // the nearest-neighbour bodies know kinds 0 and KIND_MIS only: a mesh with any other kind is refused
-    // (status, no output) before the pipeline starts
-    int bad = 0;
-    for (int l = tid; l < a.L; l += blockDim.x) {
-      const int k = __ldg(a.kinds + l);
-      bad |= (k != 0 && k != KIND_MIS);
-    }
-    if (__syncthreads_or(bad)) {
-      if (tid == 0) set_status(a.status, ST_BAD_GEOMETRY);
-      return;
-    }
-  }
+
   if (a.L <= kMaxSmemKinds) {
     for (int l = tid; l < a.L; l += blockDim.x) {
       int k = __ldg(a.kinds + l);

@@ -1,28 +1,41 @@
-// Nearest-neighbour instantiations of the propagation kernel (layer kinds 0 and odd-shift only): the
-// full-warp configurations of the Clements and Reck meshes, uniform and split.  Without the strided and
-// butterfly layer bodies the back-propagation kernel spills less; measured on GB300 at N=256, L=256,
-// B=4096 it runs 3% faster than the general instantiation, with identical results.
+// Nearest-neighbour instantiations of the propagation kernel (layer kinds 0 and odd-shift only) for the
+// Clements and Reck meshes: the full-warp configurations (uniform and split) and the main runtime
+// lane-group ones.  Without the strided and butterfly layer bodies, and with one fused pair order, the
+// back-propagation kernel does not spill; measured on GB300 at N=256, L=256, B=4096 it runs 9% faster than
+// the general instantiation, with identical results.
 #include "mg_launch.h"
 
 namespace mg {
 
 namespace {
-// (op, real, M, V, gr): the instantiated set (split: forward only)
-constexpr int kNN[][5] = {{OP_FWD, 0, 8, 4, 0}, {OP_FWD, 0, 16, 2, 0}, {OP_FWD, 1, 8, 4, 0},
-                          {OP_BWD, 0, 8, 4, 1}, {OP_BWD, 0, 16, 2, 1}, {OP_BWD, 1, 8, 4, 2}};
+// (op, real, M, V, gr, full): the instantiated set (split: forward, full only)
+constexpr int kNN[][6] = {{OP_FWD, 0, 8, 4, 0, 1}, {OP_FWD, 0, 16, 2, 0, 1}, {OP_FWD, 1, 8, 4, 0, 1},
+                          {OP_BWD, 0, 8, 4, 1, 1}, {OP_BWD, 0, 16, 2, 1, 1}, {OP_BWD, 1, 8, 4, 2, 1},
+                          {OP_FWD, 0, 8, 4, 0, 0}, {OP_FWD, 1, 8, 4, 0, 0}, {OP_BWD, 0, 8, 4, 1, 0},
+                          {OP_BWD, 1, 8, 4, 2, 0}};
 }  // namespace
 
-bool nn_instantiated(int op, bool real, int M, int V, int gr, bool split) {
-  if (split && op != OP_FWD) return false;
+bool nn_instantiated(int op, bool real, int M, int V, int gr, bool full, bool split) {
+  if (split && (op != OP_FWD || !full)) return false;
   for (const auto& k : kNN)
-    if (k[0] == op && k[1] == (real ? 1 : 0) && k[2] == M && k[3] == V && k[4] == gr) return true;
+    if (k[0] == op && k[1] == (real ? 1 : 0) && k[2] == M && k[3] == V && k[4] == gr && k[5] == (full ? 1 : 0))
+      return true;
   return false;
 }
 
-cudaError_t launch_prop_nn(int op, bool real, int M, int V, int gr, bool split, const LaunchCfg& lc,
+cudaError_t launch_prop_nn(int op, bool real, int M, int V, int gr, bool full, bool split, const LaunchCfg& lc,
                            const PropArgs& a) {
-  if (!nn_instantiated(op, real, M, V, gr, split)) return cudaErrorInvalidConfiguration;
+  if (!nn_instantiated(op, real, M, V, gr, full, split)) return cudaErrorInvalidConfiguration;
   const int key = op * 10000 + (real ? 1000 : 0) + M * 10 + V;
+  if (!full) {
+    switch (key) {
+      case 84: return launch_one<OP_FWD, 8, 4, false, 0, 0, false, true>(lc, a);
+      case 1084: return launch_one<OP_FWD, 8, 4, true, 0, 0, false, true>(lc, a);
+      case 20084: return launch_one<OP_BWD, 8, 4, false, 0, 1, false, true>(lc, a);
+      case 21084: return launch_one<OP_BWD, 8, 4, true, 0, 2, false, true>(lc, a);
+      default: return cudaErrorInvalidConfiguration;
+    }
+  }
   if (split) {
     switch (key) {
       case 84: return launch_split<OP_FWD, 8, 4, false, 32, 0, true>(lc, a);
