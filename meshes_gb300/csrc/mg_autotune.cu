@@ -37,10 +37,13 @@ extern "C" int mg_autotune(int op, int N, int L, int B, int crossing, int geomet
   std::vector<mg_config> cands;
   static const int vs[3][3] = {{2, 4, 8}, {1, 2, 4}, {1, 2, 4}};
   for (int M : {2, 4, 8, 16}) {
-    if (M > Np || Np / M > 32) continue;
+    if (N > 512 || M > Np || Np / M > 32) continue;
     for (int V : vs[op])
       for (int W : {2, 4, 8}) cands.push_back(mg_config{M, V, W, 0, 0, 2});
   }
+  if (N > 512)   // wide meshes: 20 modes per lane
+    for (int V : {1, 2})
+      for (int W : {2, 4, 8}) cands.push_back(mg_config{mg::kWideM, V, W, 0, 0, 2});
 
   // scratch (stream-ordered, freed before returning): fields x, dx / g, y, dy / g_in, dJ/dp, an L2 flush
   // buffer and the workspace of the largest candidate so far

@@ -151,7 +151,10 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   if (perm) geometry &= ~MG_GEO_PERM;
   if (geometry < 0 || geometry > 1) return fail(MG_E_ARG, "geometry %d not in {0,1} (| MG_GEO_PERM)", geometry);
   if (N < 2 || N % 2) return fail(MG_E_ARG, "N=%d must be even and >= 2 (reference gpu/mesh.py:67)", N);
-  if (N > 512) return fail(MG_E_ARG, "N=%d above the supported maximum 512", N);
+  // wide meshes (512 < N <= 640, the reference's limit, gpu/mesh.py:83): 20 modes in each of 32 lanes,
+  // nearest-neighbour geometry only (kWideM)
+  if (N > 640) return fail(MG_E_ARG, "N=%d above the supported maximum 640", N);
+  if (N > 512 && geometry != GEO_NN) return fail(MG_E_ARG, "N=%d > 512 needs nearest-neighbour geometry", N);
   if (L < 0 || B < 0) return fail(MG_E_ARG, "L=%d, B=%d must be non-negative", L, B);
   // the permutation flags travel in the shared-memory copy of the layer kinds
   if (perm && L > kMaxSmemKinds) return fail(MG_E_ARG, "permuted meshes take at most %d layers", kMaxSmemKinds);
@@ -164,22 +167,26 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   p.perm = perm;
   p.real = crossing == CR_ORTH;
   p.gr = stored ? 4 : (op != OP_BWD) ? 0 : (crossing == CR_MZI ? 1 : (crossing == CR_ORTH ? 2 : 0));
-  const int Np = pow2ceil(N);
-  int M = (cfg && cfg->M) ? cfg->M : std::max(std::min(8, Np), Np / 32);
-  if (M < 2 || M > 16 || (M & (M - 1))) return fail(MG_E_CONFIG, "modes per lane M=%d not in {2,4,8,16}", M);
+  const bool wide = N > 512;
+  const int Np = wide ? 32 * kWideM : pow2ceil(N);
+  int M = (cfg && cfg->M) ? cfg->M : (wide ? kWideM : std::max(std::min(8, Np), Np / 32));
+  if (wide ? M != kWideM : (M < 2 || M > 16 || (M & (M - 1))))
+    return fail(MG_E_CONFIG, "modes per lane M=%d not in %s", M, wide ? "{20} for N > 512" : "{2,4,8,16}");
   if (M > Np) M = Np;
   const int G = Np / M;
   if (G > 32) return fail(MG_E_CONFIG, "N=%d needs more than 32 lanes at M=%d", N, M);
   int V = (cfg && cfg->V) ? cfg->V : 0;
   if (!V) {
     static const int vd[3][5] = {{8, 8, 4, 2, 0}, {4, 4, 2, 1, 0}, {4, 4, 4, 2, 0}};   // by ilog2(M)-1
-    V = stored ? stored_default_v(OP_BWD, M) : vd[op][ilog2(M) - 1];
+    static const int vw[3] = {2, 1, 1};                                                // M = kWideM
+    V = wide ? ((op == OP_BWD && p.real) ? 2 : vw[op]) : stored ? stored_default_v(OP_BWD, M) : vd[op][ilog2(M) - 1];
   }
   if (perm && stored) return fail(MG_E_ARG, "stored-activation back-propagation takes no permutations");
-  if (perm ? !perm_instantiated(op, crossing == CR_ORTH, M, V, p.gr)
-           : (stored ? !instantiated_stored(OP_BWD, M, V) : !instantiated(op, M, V)))
-    return fail(MG_E_CONFIG, "no %skernel instantiated for op=%d M=%d V=%d", perm ? "permuted-mesh " : "",
-                stored ? MG_OP_BWD_STORED : op, M, V);
+  if (wide ? (perm || stored || !wide_instantiated(op, crossing == CR_ORTH, V, p.gr))
+           : perm ? !perm_instantiated(op, crossing == CR_ORTH, M, V, p.gr)
+                  : (stored ? !instantiated_stored(OP_BWD, M, V) : !instantiated(op, M, V)))
+    return fail(MG_E_CONFIG, "no %skernel instantiated for op=%d M=%d V=%d",
+                wide ? "wide-mesh " : perm ? "permuted-mesh " : "", stored ? MG_OP_BWD_STORED : op, M, V);
   p.M = M; p.V = V; p.G = G; p.logG = ilog2(G); p.R = 32 / G; p.np2 = G * M / 2;
   // split launch: when one wave of uniform CTAs cannot cover the SMs evenly (B between SMs x 4 warps x V
   // and SMs x 4 warps x (2V-1) vectors), run two 4-warp CTAs per SM holding V and V-1 vectors per lane
@@ -349,7 +356,9 @@ int run_prop(const Plan& P, const void* in0, const void* in1, void* out0, void* 
   lc.stream = st;
   cudaError_t e;
   a.nA = P.nA;
-  if (!P.perm && P.geometry == GEO_NN && nn_instantiated(P.op, P.real, P.M, P.V, P.gr, P.G == 32, P.split))
+  if (P.M == kWideM)
+    e = launch_prop_wide(P.op, P.real, P.V, P.gr, lc, a);
+  else if (!P.perm && P.geometry == GEO_NN && nn_instantiated(P.op, P.real, P.M, P.V, P.gr, P.G == 32, P.split))
     e = launch_prop_nn(P.op, P.real, P.M, P.V, P.gr, P.G == 32, P.split, lc, a);
   else
     e = P.split ? launch_prop_split(P.op, P.real, P.M, P.V, P.G == 32, P.gr, lc, a)

@@ -78,6 +78,10 @@ cudaError_t launch_prop_perm(int op, bool real, int M, int V, int gr, const Laun
 bool nn_instantiated(int op, bool real, int M, int V, int gr, bool full, bool split);
 cudaError_t launch_prop_nn(int op, bool real, int M, int V, int gr, bool full, bool split, const LaunchCfg& lc,
                            const PropArgs& a);
+// wide nearest-neighbour meshes (512 < N <= 640): kWideM modes in each of 32 lanes (mg_prop_wide.cu)
+constexpr int kWideM = 20;
+bool wide_instantiated(int op, bool real, int V, int gr);
+cudaError_t launch_prop_wide(int op, bool real, int V, int gr, const LaunchCfg& lc, const PropArgs& a);
 // split launches (two CTA kinds per SM); instantiated only for the full-warp configurations in
 // split_instantiated()
 bool split_instantiated(int op, bool real, int M, int V, bool full, int gr);

@@ -96,6 +96,9 @@ CASES = [
     ("fft", "mzi", 512, 4, 0.02), ("butterfly", "mzi", 16, 7, 0.02), ("butterfly", "mzi", 64, 12, 0.02),
     ("fft", "sym", 128, 6, 0.02), ("fft", "orth", 32, 10, 0.0), ("fft", "orth", 256, 3, 0.0),
     ("butterfly", "orth", 32, 5, 0.0),
+    # wide nearest-neighbour meshes (512 < N <= 640, 20 modes per lane)
+    ("clements", "mzi", 640, 9, 0.02), ("reck", "mzi", 600, 4, 0.02), ("clements", "sym", 520, 6, 0.02),
+    ("clements", "orth", 640, 5, 0.0), ("clements", "mzi", 514, 3, 0.0),
 ]
 
 
@@ -238,6 +241,18 @@ def test_bad_geometry_reports_status():
                           out.data_ptr(), N, 0, ws.data_ptr(), nb, st) == 0
     assert lib.mg_read_status(ws.data_ptr(), 1, st) == 2
     assert lib.mg_read_status(ws.data_ptr(), 0, st) == 0
+
+
+def test_width_limits():
+    """N up to 640 (the reference's limit, gpu/mesh.py:83) for nearest-neighbour meshes; beyond, or a
+    butterfly above 512, is refused before any launch."""
+    from meshes_gb300 import _lib
+    lib = _lib.load()
+    assert lib.mg_workspace_bytes(0, 640, 640, 8, 0, 0, None) > 0
+    assert lib.mg_workspace_bytes(2, 600, 10, 8, 2, 0, None) > 0
+    assert lib.mg_workspace_bytes(0, 642, 640, 8, 0, 0, None) == 0
+    assert "640" in _lib.last_error()
+    assert lib.mg_workspace_bytes(0, 1024, 10, 8, 0, 1, None) == 0
 
 
 def test_argument_errors():
