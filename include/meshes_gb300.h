@@ -337,8 +337,9 @@ int mg_generic_mzi_T_vjp(int n, const double* p, const double* s, const void* gT
  * independent FMAs; writes one float per thread to `sink`.  Used by bench.py to measure the FP32
  * CUDA-core peak of the device it runs on. */
 int mg_fma_probe(float* sink, int blocks, int threads, int iters, void* stream);
-/* Self-check of the coefficient precompute's double-precision sin/cos: out[2i], out[2i+1] = the
- * differences (sin, cos)(x[i]) own - library, for n device doubles x (used by the tests). */
+/* Self-check of the coefficient precompute's double-precision sin/cos: out[4i..4i+3] = the differences
+ * (sin, cos)(x[i]) own - library for the full-precision version and for the tile-precision version (results
+ * rounded to float32), for n device doubles x (used by the tests). */
 int mg_trig_check(const double* x, double* out, int n, void* stream);
 /* The same probe with packed FP32 pairs (fma.rn.f32x2, sm_100+): 128 FMAs per thread-iteration. */
 int mg_fma2_probe(float* sink, int blocks, int threads, int iters, void* stream);

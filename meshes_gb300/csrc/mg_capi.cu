@@ -518,15 +518,19 @@ __global__ void fma_probe_kernel(float* sink, int iters, float m) {
   sink[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
-// sincos_d (the coefficient precompute's own double sin/cos) against the library sincos
+// sincos_d and sincos_c (the coefficient precompute's own double sin/cos, full and tile precision)
+// against the library sincos
 __global__ void trig_check_kernel(const double* x, double* out, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double s, c, s2, c2;
+  double s, c, s2, c2, s3, c3;
   sincos_d(x[i], &s, &c);
   sincos(x[i], &s2, &c2);
-  out[2 * i] = s - s2;
-  out[2 * i + 1] = c - c2;
+  sincos_c(x[i], &s3, &c3);
+  out[4 * i] = s - s2;
+  out[4 * i + 1] = c - c2;
+  out[4 * i + 2] = s3 - s2;
+  out[4 * i + 3] = c3 - c2;
 }
 
 // The same chains with packed FP32 pairs (one fma.rn.f32x2 = two FMAs per lane): whether the FMA pipe

@@ -42,7 +42,9 @@ struct CoefArgs {
 __host__ __device__ inline int crossing_np(int c) { return c == CR_ORTH ? 1 : 2; }
 __host__ __device__ inline int crossing_ns(int c) { return c == CR_MZI ? 2 : (c == CR_SYM ? 1 : 0); }
 
-__device__ __forceinline__ void slot_T(const CoefArgs& a, int l, int q, bool active, C2x2& T, C2x2& D0, C2x2& D1) {
+// csb (MZI crossings): receives (cos, sin)(pi/4 + beta) of an active slot
+__device__ __forceinline__ void slot_T(const CoefArgs& a, int l, int q, bool active, C2x2& T, C2x2& D0, C2x2& D1,
+                                       float2* csb = nullptr) {
   if (!active) {
     T = c2x2_identity(); D0 = c2x2_zero(); D1 = c2x2_zero();
     return;
@@ -70,7 +72,7 @@ __device__ __forceinline__ void slot_T(const CoefArgs& a, int l, int q, bool act
     D1 = c2x2_zero();
   }
   if (a.crossing == CR_MZI) {
-    mzi_T(pp[0], pp[1], ss ? ss[0] : 0.f, ss ? ss[1] : 0.f, &T, need_d ? &D0 : nullptr, need_d ? &D1 : nullptr);
+    mzi_T(pp[0], pp[1], ss ? ss[0] : 0.f, ss ? ss[1] : 0.f, &T, need_d ? &D0 : nullptr, need_d ? &D1 : nullptr, csb);
   } else {   // CR_SYM
     sym_T(pp[0], pp[1], ss ? ss[0] : 0.f, &T, need_d ? &D0 : nullptr, need_d ? &D1 : nullptr);
   }
@@ -139,15 +141,9 @@ __global__ void coef_kernel(const CoefArgs a) {
   const int j = q / (M / 2), e = q % (M / 2);
   if (!real) {
     C2x2 T, D0, D1;
-    slot_T(a, l, q, active, T, D0, D1);
-    if (a.op == OP_BWD && a.gr == 1) {   // (cos, sin)(pi/4 + beta) of the slot, for the direct MZI gradient
-      float2 csv = make_float2(0.f, 0.f);
-      if (active) {
-        const float be = a.s ? a.s[(size_t)l * a.lds + (size_t)q * 2 + 1] : 0.f;
-        double sb, cb;
-        sincos_d(0.78539816339744830962 + (double)be, &sb, &cb);
-        csv = make_float2((float)cb, (float)sb);
-      }
+    float2 csv = make_float2(0.f, 0.f);   // (cos, sin)(pi/4 + beta) for the direct MZI gradient; 0 if inactive
+    slot_T(a, l, q, active, T, D0, D1, (a.op == OP_BWD && a.gr == 1) ? &csv : nullptr);
+    if (a.op == OP_BWD && a.gr == 1) {
       float2* cs = reinterpret_cast<float2*>(tl + M * G);
       if (!xl) cs[e * G + j] = csv;
       else {

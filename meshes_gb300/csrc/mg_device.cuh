@@ -218,18 +218,66 @@ __device__ __forceinline__ void sincos_d(double x, double* s, double* c) {
   }
 }
 
+// sin and cos for the coefficient tiles, whose entries are rounded to float32: the same reduction with a
+// shorter series (sin to r^13, cos to r^14 on |r| <= pi/4: truncation below 2e-14), so that every value
+// is correct to ~1e-13 before its float32 rounding - far below the float32 half-unit of 3e-8, so the
+// rounding stays unbiased (a systematically biased single-precision sin/cos made the forward error grow
+// linearly with depth) - at two thirds of the FP64 operations of sincos_d.
+__device__ __forceinline__ void sincos_c(double x, double* s, double* c) {
+  if (!(fabs(x) < 1048576.0)) {
+    sincos(x, s, c);
+    return;
+  }
+  const double k = rint(x * 0.63661977236758134308);
+  const double r = fma(-k, 1.5893254773528196e-08, fma(-k, 1.5707963109016418, x));
+  const double r2 = r * r;
+  double ps = 1.6059043836821613e-10;                                     // 1/13!
+  ps = fma(ps, r2, -2.505210838544172e-08);                               // 1/11!
+  ps = fma(ps, r2, 2.7557319223985893e-06);                               // 1/9!
+  ps = fma(ps, r2, -1.984126984126984e-04);                               // 1/7!
+  ps = fma(ps, r2, 8.333333333333333e-03);                                // 1/5!
+  ps = fma(ps, r2, -0.16666666666666666);                                 // 1/3!
+  const double sr = fma(r * r2, ps, r);
+  double pc = -1.1470745597729725e-11;                                    // 1/14!
+  pc = fma(pc, r2, 2.08767569878681e-09);                                 // 1/12!
+  pc = fma(pc, r2, -2.755731922398589e-07);                               // 1/10!
+  pc = fma(pc, r2, 2.48015873015873e-05);                                 // 1/8!
+  pc = fma(pc, r2, -1.388888888888889e-03);                               // 1/6!
+  pc = fma(pc, r2, 0.041666666666666664);                                 // 1/4!
+  pc = fma(pc, r2, -0.5);                                                 // 1/2!
+  const double cr = fma(r2, pc, 1.0);
+  switch (static_cast<int>(k) & 3) {
+    case 0: *s = sr; *c = cr; break;
+    case 1: *s = cr; *c = -sr; break;
+    case 2: *s = -sr; *c = -cr; break;
+    default: *s = -cr; *c = sr; break;
+  }
+}
+
 // Standard MZI T = S(beta) P(theta) S(alpha) P(phi) (reference crossing.py:216-221):
 //   T = e^{i th/2} [[e^{i ph}(i S Cm - C Sp),  i C Cp - S Sm],
 //                   [e^{i ph}(i C Cp + S Sm), -i S Cm - C Sp]]
 // with C,S = cos,sin(th/2) and C+-,S+- = cos,sin(alpha +- beta).  D0 = dT/dth, D1 = dT/dph
-// (crossing.py:223-231): dE/dth = (i/2)E for both exponentials, dT/dph = T diag(i, 0).
-__device__ __forceinline__ void mzi_T(float th, float ph, float al, float be, C2x2* T, C2x2* D0, C2x2* D1) {
-  double S, C, Sph, Cph, Sp = 0.0, Cp = 1.0, Sm = 0.0, Cm = 1.0;
-  sincos_d(0.5 * (double)th, &S, &C);
-  sincos_d((double)ph, &Sph, &Cph);
+// (crossing.py:223-231): dE/dth = (i/2)E for both exponentials, dT/dph = T diag(i, 0).  The splitter
+// terms come from sin/cos of alpha and beta by the angle-sum formulas; csb, when given, receives
+// (cos, sin)(pi/4 + beta) = ((cos b - sin b), (cos b + sin b)) / sqrt 2 for the direct MZI gradient.
+__device__ __forceinline__ void mzi_T(float th, float ph, float al, float be, C2x2* T, C2x2* D0, C2x2* D1,
+                                      float2* csb = nullptr) {
+  double S, C, Sph, Cph, Sp = 0.0, Cp = 1.0, Sm = 0.0, Cm = 1.0, sb = 0.0, cb = 1.0;
+  sincos_c(0.5 * (double)th, &S, &C);
+  sincos_c((double)ph, &Sph, &Cph);
   if (al != 0.f || be != 0.f) {
-    sincos_d((double)al + (double)be, &Sp, &Cp);
-    sincos_d((double)al - (double)be, &Sm, &Cm);
+    double sa, ca;
+    sincos_c((double)al, &sa, &ca);
+    sincos_c((double)be, &sb, &cb);
+    Cp = ca * cb - sa * sb;
+    Sp = sa * cb + ca * sb;
+    Cm = ca * cb + sa * sb;
+    Sm = sa * cb - ca * sb;
+  }
+  if (csb) {
+    constexpr double kRsqrt2 = 0.70710678118654752440;
+    *csb = make_float2((float)(kRsqrt2 * (cb - sb)), (float)(kRsqrt2 * (cb + sb)));
   }
   const Z E0 = {C, S};                                      // e^{i th/2}
   const Z E1 = zmul(E0, Z{Cph, Sph});                       // e^{i(th/2+ph)}
@@ -256,9 +304,9 @@ __device__ __forceinline__ void mzi_T(float th, float ph, float al, float be, C2
 //   T = [[e^{i ph}(S + i C sin2a), i C cos2a], [i C cos2a, e^{-i ph}(S - i C sin2a)]]
 __device__ __forceinline__ void sym_T(float th, float ph, float al, C2x2* T, C2x2* D0, C2x2* D1) {
   double S, C, Sph, Cph, S2a = 0.0, C2a = 1.0;
-  sincos_d(0.5 * (double)th, &S, &C);
-  sincos_d((double)ph, &Sph, &Cph);
-  if (al != 0.f) sincos_d(2.0 * (double)al, &S2a, &C2a);
+  sincos_c(0.5 * (double)th, &S, &C);
+  sincos_c((double)ph, &Sph, &Cph);
+  if (al != 0.f) sincos_c(2.0 * (double)al, &S2a, &C2a);
   const Z e = {Cph, Sph}, em = {Cph, -Sph};
   const Z T00 = zmul(e, Z{S, C * S2a}), T11 = zmul(em, Z{S, -C * S2a});
   T->t00 = zf(T00);
@@ -279,7 +327,7 @@ __device__ __forceinline__ void sym_T(float th, float ph, float al, C2x2* T, C2x
 // Real orthogonal crossing (reference gpu/crossing.cu:132-148): T = [[S, -C], [C, S]], S,C of th/2.
 __device__ __forceinline__ void orth_T(float th, R2x2* T, R2x2* D0) {
   double S, C;
-  sincos_d(0.5 * (double)th, &S, &C);
+  sincos_c(0.5 * (double)th, &S, &C);
   T->t00 = (float)S; T->t01 = (float)-C; T->t10 = (float)C; T->t11 = (float)S;
   if (D0) {
     D0->t00 = (float)(0.5 * C); D0->t01 = (float)(0.5 * S); D0->t10 = (float)(-0.5 * S); D0->t11 = (float)(0.5 * C);

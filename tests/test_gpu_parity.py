@@ -414,7 +414,8 @@ def test_split_launch_parity(cr, N, B):
 
 def test_coefficient_trigonometry_matches_library():
     """The coefficient precompute's own double sin/cos (Cody-Waite reduction + Taylor series) agrees with
-    the CUDA library's to a few units in the last place, over phase-like, small and large arguments."""
+    the CUDA library's to a few units in the last place, over phase-like, small and large arguments; its
+    tile-precision version (values rounded to float32 afterwards) to 1e-13."""
     from meshes_gb300 import _lib
     lib = _lib.load()
     rng = np.random.default_rng(77)
@@ -422,9 +423,11 @@ def test_coefficient_trigonometry_matches_library():
                         rng.normal(0, 0.02, 20000), rng.uniform(-1e5, 1e5, 5000),
                         np.arange(-64, 65) * np.pi / 4, [0.0, 1e-30, -1e-30, 0.125, -0.125, 2.0 ** 20, 3e7]])
     xd = torch.tensor(x, dtype=torch.float64, device="cuda")
-    out = torch.empty(2 * x.size, dtype=torch.float64, device="cuda")
+    out = torch.empty(4 * x.size, dtype=torch.float64, device="cuda")
     assert lib.mg_trig_check(xd.data_ptr(), out.data_ptr(), x.size, torch.cuda.current_stream().cuda_stream) == 0
-    assert out.abs().max().item() < 1e-15
+    out = out.view(-1, 4).abs()
+    assert out[:, :2].max().item() < 1e-15
+    assert out[:, 2:].max().item() < 1e-13
 
 
 @pytest.mark.parametrize("name", ["clipped_squarenet_N4.npz", "clipped_qrnet_N4.npz"])
