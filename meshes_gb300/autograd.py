@@ -115,11 +115,23 @@ class MeshFunction(torch.autograd.Function):
         return gx, dp.view_as(p), None
 
 
-def mesh_apply(mesh: MeshNetworkGPU, x: torch.Tensor, p: Optional[torch.Tensor] = None) -> torch.Tensor:
-    """Differentiable y = U(p) x; x (B, N), p (L, N/2, n_p) (defaults to the mesh's own phases)."""
+def mesh_apply(mesh: MeshNetworkGPU, x: torch.Tensor, p: Optional[torch.Tensor] = None,
+               ph: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """Differentiable y = U(p) x; x (B, N), p (L, N/2, n_p) (defaults to the mesh's own phases).
+
+    A mesh with a phase screen (is_phase) applies D = diag(exp(i ph)) before (phi_pos 'in') or after
+    ('out') the layers, as the reference's CPU path does (c/dot.cpp:97-143); ph (N,) defaults to the
+    screen phases of the mesh and receives its gradient through PyTorch's autograd of the product."""
     if p is None:
         p = mesh.p_crossing
     dtype = mesh.dtype
     if x.dtype != dtype:
         x = x.to(dtype)
-    return MeshFunction.apply(x, p, mesh)
+    if not mesh.is_phase:
+        return MeshFunction.apply(x, p, mesh)
+    if ph is None:
+        ph = mesh.p_phase[mesh.n_cr * mesh.X_np:]
+    d = torch.polar(torch.ones_like(ph, dtype=torch.float32), ph.to(torch.float32))
+    if mesh.phi_pos == "in":
+        return MeshFunction.apply(x * d, p, mesh)
+    return MeshFunction.apply(x, p, mesh) * d

@@ -47,6 +47,34 @@ def test_autograd_matches_oracle(geo, cr, N, B):
     assert O.rel_err(xd.grad.cpu().numpy(), gin) < 1e-5
 
 
+@pytest.mark.parametrize("pos", ["out", "in"])
+def test_autograd_with_phase_screen(pos):
+    """mesh_apply on a mesh with a phase screen: the screen phases get their gradient too."""
+    from meshes_gb300 import MeshNetworkGPU
+    from meshes_gb300.autograd import mesh_apply
+    rng = np.random.default_rng(91 if pos == "out" else 92)
+    N, B = 64, 21
+    om = O.random_mesh(rng, N, "clements", "mzi", 0.02)
+    ph = rng.uniform(0, 2 * np.pi, N)
+    m = MeshNetworkGPU(N, om.L, om.lens, om.shifts, np.concatenate([np.asarray(om.p, np.float32).reshape(-1),
+                                                                   ph.astype(np.float32)]),
+                       np.asarray(om.s, np.float32), "mzi", phi_pos=pos, is_phase=True)
+    x = O.unit_columns(rng, N, B)
+    t = O.unit_columns(rng, N, B)
+    xd = torch.tensor(x, dtype=torch.complex64, device="cuda", requires_grad=True)
+    pd = torch.tensor(om.p, dtype=torch.float32, device="cuda", requires_grad=True)
+    phd = torch.tensor(ph, dtype=torch.float32, device="cuda", requires_grad=True)
+    y = mesh_apply(m, xd, pd, phd)
+    loss = ((y - torch.tensor(t, dtype=torch.complex64, device="cuda")).abs() ** 2).sum()
+    loss.backward()
+    y_ref = O.propagate_screened(om, x, ph.astype(np.float32), pos)
+    dp_ref, dph_ref, gin_ref = O.grad_screened(om, y_ref, 2 * (y_ref - t), ph.astype(np.float32), pos)
+    assert O.rel_err(y.detach().cpu().numpy(), y_ref) < 1e-5
+    assert O.rel_err(pd.grad.cpu().numpy(), dp_ref) < 1e-5
+    assert O.rel_err(phd.grad.cpu().numpy(), dph_ref) < 1e-5
+    assert O.rel_err(xd.grad.cpu().numpy(), gin_ref) < 1e-5
+
+
 def _loss_from_layer(om, acts, l, T, t):
     """sum |y - t|^2 propagating from the input of layer l with transfer matrices T (complex128)."""
     u = np.ascontiguousarray(acts[l].T).copy()
