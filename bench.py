@@ -17,7 +17,6 @@ on the same workload, on rank 0 only.
 from __future__ import annotations
 
 import argparse
-import ctypes
 import json
 import os
 import statistics

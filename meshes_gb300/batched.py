@@ -13,7 +13,6 @@ from __future__ import annotations
 import ctypes
 from typing import List, Optional, Sequence
 
-import numpy as np
 import torch
 
 from . import _lib

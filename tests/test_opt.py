@@ -1,7 +1,6 @@
 """MeshOptimizer (reference gpu/opt.py): scipy fitting of a mesh to a target with GPU gradients."""
 import numpy as np
 import pytest
-import torch
 
 from oracle import meshes_oracle as O
 

@@ -5,7 +5,6 @@ geometry and crossing, through MeshNetworkGPU, the autograd function and the C A
 
 Tolerances as in test_gpu_parity.py: relative Frobenius error 1e-5.
 """
-import ctypes
 import os
 import zlib
 

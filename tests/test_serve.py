@@ -4,11 +4,9 @@ Failures are made on the host (bad requests, an over-budget request, a cancelled
 thread that dies mid-stream); nothing here faults or hangs the GPU.
 """
 import threading
-import time
 
 import numpy as np
 import pytest
-import torch
 
 from oracle import meshes_oracle as O
 
