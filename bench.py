@@ -238,16 +238,17 @@ def run_ours(args, rank, world, local_rank):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # > 129 MB L2
     launches_per_step = 4          # coefficient tiles, forward, back-propagation with fused L2, gradient reduce
 
-    def step(xx, yy_t):
+    def step(xx, yy_t, dp_out=None):
         """One training step through the programmed-mesh C ABI: the back-propagation tiles are built once
         and serve the forward pass too; dJ/dy* = 2 (y - y_t) is formed inside the backward kernel."""
+        dp_out = dp if dp_out is None else dp_out
         _lib.check(lib.mg_build_tiles(2, N, L, 0, lens_d.data_ptr(), shifts_d.data_ptr(), None, 0, p_d.data_ptr(), ldp,
                                       s_d.data_ptr(), lds, None, None, None, B, None, ws_b.data_ptr(), wsb_b, st),
                    "mg_build_tiles")
         _lib.check(lib.mg_propagate(3, N, L, B, 0, 0, xx.data_ptr(), None, y.data_ptr(), None, N, None, 0, 0, None,
                                     ws_b.data_ptr(), wsb_b, st), "mg_propagate")
         _lib.check(lib.mg_propagate_l2(N, L, B, 0, 0, y.data_ptr(), yy_t.data_ptr(), None, gin.data_ptr(), N,
-                                       dp.data_ptr(), ldp, 0, None, ws_b.data_ptr(), wsb_b, st), "mg_propagate_l2")
+                                       dp_out.data_ptr(), ldp, 0, None, ws_b.data_ptr(), wsb_b, st), "mg_propagate_l2")
 
     def step_dropin(xx, yy_t):
         """The same step through the reference-shaped entry points (mg_fwdprop, mg_backdiff)."""
@@ -339,14 +340,20 @@ def run_ours(args, rank, world, local_rank):
     h2d = 2 * x.numel() * 8
     d2h = dp.numel() * 4
 
-    # the same steps as a training loop runs them: the next step's inputs are copied on a second stream
-    # into the other of two buffers while the current step computes (every copy still inside the timed
-    # region; one pair of events around all K steps)
-    copy_stream = torch.cuda.Stream(dev)
+    # the same steps as a training loop runs them: on copy streams, the next step's inputs are copied into
+    # the other of two buffers, and each step's dJ/dp (written to one of two device buffers) is copied back,
+    # while the compute stream runs the next step (every copy still inside the timed region; one pair of
+    # events around all K steps, the last read-back included)
+    copy_stream = torch.cuda.Stream(dev)          # host -> device
+    back_stream = torch.cuda.Stream(dev)          # device -> host (its own queue: a read-back waiting for its
+                                                  # step must not hold up the next step's input copy)
     xs = [torch.empty_like(x) for _ in range(2)]
     yts = [torch.empty_like(yt) for _ in range(2)]
+    dps = [torch.empty_like(dp) for _ in range(2)]
+    dp_pins = [torch.empty(dp.numel(), dtype=torch.float32).pin_memory() for _ in range(2)]
     ev_in = [torch.cuda.Event() for _ in range(2)]
     ev_used = [torch.cuda.Event() for _ in range(2)]
+    ev_out = [torch.cuda.Event() for _ in range(2)]
 
     def e2e_loop(k_steps):
         for k in range(k_steps):
@@ -357,11 +364,16 @@ def run_ours(args, rank, world, local_rank):
                 yts[i].copy_(yt_pin, non_blocking=True)
                 ev_in[i].record(copy_stream)
             stream.wait_event(ev_in[i])
-            step(xs[i], yts[i])
+            stream.wait_event(ev_out[i])                     # step k-2's dJ/dp has left dps[i]
+            step(xs[i], yts[i], dps[i])
             ev_used[i].record(stream)
-            dp_pin.copy_(dp, non_blocking=True)
+            back_stream.wait_event(ev_used[i])
+            with torch.cuda.stream(back_stream):
+                dp_pins[i].copy_(dps[i], non_blocking=True)  # the step's result: dJ/dp
+                ev_out[i].record(back_stream)
+        stream.wait_event(ev_out[(k_steps - 1) & 1])
 
-    for e in ev_used:
+    for e in ev_used + ev_out:
         e.record(stream)
     e2e_loop(max(2, args.warmup))
     barrier()
@@ -453,7 +465,7 @@ def run_ours(args, rank, world, local_rank):
                          "frac": bwd_bytes / t_bwd / 1e9 / hbm_peak, "traffic": traffic,
                          "peak_source": hbm_src, "algorithmic_bytes_per_launch": bwd_bytes},
         "e2e": {"value": units / t_e2e, "unit": "MZI-apps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "pipelined": "next step's H2D on a second stream during the current step",
+                "pipelined": "next step's H2D and previous step's D2H on copy streams during the current step",
                 "serialized_value": units / t_e2e_serial},
         "gpu_launches": launches_per_step * args.steps,
         "clocks": cs.summary(),
