@@ -44,7 +44,7 @@ batched_kernel(const mg_batch_mesh* __restrict__ meshes, int n_meshes, const mg_
       if (threadIdx.x == 0) set_status(status, ST_BAD_WORK);
       continue;
     }
-    PropArgs a;
+    PropArgs a{};
     a.N = md.N; a.L = md.L; a.B = md.B; a.ldu = md.ldu;
     a.G = md.G; a.logG = 31 - __clz(md.G); a.W = kBatchWarps; a.CL = md.CL; a.S = md.S;
     a.layer_bytes = md.layer_bytes; a.dlayer_bytes = 0;

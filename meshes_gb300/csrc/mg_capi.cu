@@ -334,9 +334,10 @@ void set_perm_args(const Plan& P, unsigned char* ws, int l0, int l1, PropArgs& a
 }
 
 int run_prop(const Plan& P, const void* in0, const void* in1, void* out0, void* out1, int ldu, float* dp, int ldp,
-             int accumulate, unsigned char* ws, cudaStream_t st, const void* target = nullptr) {
+             int accumulate, unsigned char* ws, cudaStream_t st, const void* target = nullptr, void* ckpt = nullptr,
+             int ckpt_every = 0) {
   if (P.B == 0) return MG_OK;
-  PropArgs a;
+  PropArgs a{};
   a.target = target;
   a.act = nullptr;
   a.act_plane = 0;
@@ -348,6 +349,9 @@ int run_prop(const Plan& P, const void* in0, const void* in1, void* out0, void* 
   a.in0 = in0; a.in1 = in1; a.out0 = out0; a.out1 = out1;
   a.partial = reinterpret_cast<float2*>(ws + P.off_partial);
   a.status = reinterpret_cast<int*>(ws);
+  a.ckpt = ckpt;
+  a.ckpt_every = ckpt_every;
+  a.ckpt_plane = (size_t)P.B * ldu;
   set_perm_args(P, ws, 0, P.L, a);
   LaunchCfg lc;
   lc.grid = dim3(P.grid);
@@ -790,10 +794,16 @@ int mg_propagate_l2(int N, int L, int B, int crossing, int geometry, const void*
                   static_cast<cudaStream_t>(stream), target);
 }
 
-int mg_propagate_range(int op, int N, int L, int l0, int l1, int B, int crossing, int geometry, const void* in0,
-                       const void* in1, void* out0, void* out1, int ldu, void* act, void* dT, int accumulate,
-                       const mg_config* cfg, void* ws, size_t wsb, void* stream) {
-  g_err.clear();
+}  // extern "C"
+
+namespace {
+
+// Layer range [l0, l1) (mg_propagate_range).  With keep_partials, a stored-activation back-propagation
+// leaves its per-CTA dJ/dT partials at their layers' places in the full-depth partial buffer (per-CTA blocks
+// of L layers) and reduces nothing: the caller reduces all ranges at once (reduce_raw).
+int range_impl(int op, int N, int L, int l0, int l1, int B, int crossing, int geometry, const void* in0,
+               const void* in1, void* out0, void* out1, int ldu, void* act, void* dT, int accumulate,
+               const mg_config* cfg, void* ws, size_t wsb, void* stream, bool keep_partials) {
   if (op != OP_FWD && op != MG_OP_BWD_STORED) return fail(MG_E_ARG, "op %d not in {MG_OP_FWD, MG_OP_BWD_STORED}", op);
   if (l0 < 0 || l1 < l0 || l1 > L) return fail(MG_E_ARG, "layer range [%d, %d) outside [0, %d)", l0, l1, L);
   // layer ranges run uniform CTAs (the stored-activation kernels have no split form)
@@ -813,7 +823,7 @@ int mg_propagate_range(int op, int N, int L, int l0, int l1, int B, int crossing
   TRY(check_field(out0, "out0", P.real, false));
   TRY(check_field(in1, "in1", P.real, bwd && B > 0));
   TRY(check_field(out1, "out1", P.real, bwd && B > 0));
-  if (bwd && !dT && B > 0 && l1 > l0) return fail(MG_E_ARG, "dT is NULL");
+  if (bwd && !dT && B > 0 && l1 > l0 && !keep_partials) return fail(MG_E_ARG, "dT is NULL");
   if (dT && (reinterpret_cast<uintptr_t>(dT) & 7)) return fail(MG_E_ARG, "dT not 8-byte aligned");
   if (act && !bwd) {   // the forward kernel's store mode has its own (M, V) instantiations
     if (!(cfg && cfg->V)) P.V = stored_default_v(OP_FWD, P.M);
@@ -845,7 +855,7 @@ int mg_propagate_range(int op, int N, int L, int l0, int l1, int B, int crossing
   unsigned char* w = static_cast<unsigned char*>(ws);
   const int* kinds_full = reinterpret_cast<const int*>(w + P.off_kinds);
   P.smem = launch_smem(P, P.op, bwd ? 32 : 0, nl);
-  PropArgs a;
+  PropArgs a{};
   a.target = nullptr;
   a.N = N; a.L = nl; a.B = B; a.ldu = ldu;
   a.G = P.G; a.logG = P.logG; a.W = P.W; a.CL = P.CL; a.S = P.S;
@@ -857,7 +867,8 @@ int mg_propagate_range(int op, int N, int L, int l0, int l1, int B, int crossing
   a.in1 = bwd ? in1 : nullptr;
   a.out0 = bwd ? nullptr : out0;
   a.out1 = bwd ? out1 : nullptr;
-  a.partial = reinterpret_cast<float2*>(w + P.off_partial);
+  a.partial = reinterpret_cast<float2*>(w + P.off_partial) + (keep_partials ? (size_t)l0 * 4 * P.np2 : 0);
+  a.pstride = keep_partials ? L : 0;
   a.status = reinterpret_cast<int*>(w);
   a.act = act;
   a.act_plane = (size_t)B * ldu;
@@ -870,7 +881,7 @@ int mg_propagate_range(int op, int N, int L, int l0, int l1, int B, int crossing
   lc.stream = static_cast<cudaStream_t>(stream);
   cudaError_t e = launch_prop(P.op, P.real, P.M, P.V, P.G == 32, act ? 4 : 0, lc, a);
   if (e != cudaSuccess) return cuda_fail(e, "prop_kernel launch");
-  if (bwd) {
+  if (bwd && !keep_partials) {
     const int n = nl * P.np2;
     raw_reduce_kernel<<<(4 * n + kReduceCols - 1) / kReduceCols, kReduceCols * kReduceRows, 0, lc.stream>>>(
         a.partial, P.grid, nl, P.np2, P.M, P.G, N,
@@ -880,6 +891,37 @@ int mg_propagate_range(int op, int N, int L, int l0, int l1, int B, int crossing
     if (e != cudaSuccess) return cuda_fail(e, "raw_reduce_kernel launch");
   }
   return MG_OK;
+}
+
+// dT (complex64 [L][N/2][2][2]) from the stored-activation partials that every range launch of a lossy
+// back-propagation left at its layers' places (range_impl with keep_partials): one reduction over all layers
+int reduce_raw(int N, int L, int B, int geometry, void* dT, int accumulate, void* ws, size_t wsb, void* stream) {
+  Plan P;
+  mg_config cu{0, 0, 0, 0, 0, 2};
+  TRY(make_plan(MG_OP_BWD_STORED, N, L, B, CR_GENERIC, geometry, &cu, &P));
+  TRY(check_ws(P, ws, wsb));
+  if (!dT) return fail(MG_E_ARG, "dT is NULL");
+  if (reinterpret_cast<uintptr_t>(dT) & 7) return fail(MG_E_ARG, "dT not 8-byte aligned");
+  unsigned char* w = static_cast<unsigned char*>(ws);
+  const int n = L * P.np2;
+  raw_reduce_kernel<<<(4 * n + kReduceCols - 1) / kReduceCols, kReduceCols * kReduceRows, 0,
+                      static_cast<cudaStream_t>(stream)>>>(reinterpret_cast<const float2*>(w + P.off_partial), P.grid, L,
+                                                           P.np2, P.M, P.G, N, static_cast<float2*>(dT), accumulate,
+                                                           reinterpret_cast<const int*>(w + P.off_kinds) + L);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MG_OK : cuda_fail(e, "raw_reduce_kernel launch");
+}
+
+}  // namespace
+
+extern "C" {
+
+int mg_propagate_range(int op, int N, int L, int l0, int l1, int B, int crossing, int geometry, const void* in0,
+                       const void* in1, void* out0, void* out1, int ldu, void* act, void* dT, int accumulate,
+                       const mg_config* cfg, void* ws, size_t wsb, void* stream) {
+  g_err.clear();
+  return range_impl(op, N, L, l0, l1, B, crossing, geometry, in0, in1, out0, out1, ldu, act, dT, accumulate, cfg, ws,
+                    wsb, stream, false);
 }
 
 int mg_lossy_forward(int N, int L, int B, int geometry, int seg, const void* x, void* y, void* ckpt, int ldu, void* ws,
@@ -895,16 +937,21 @@ int mg_lossy_forward(int N, int L, int B, int geometry, int seg, const void* x, 
     return MG_OK;
   }
   if (L > seg && !ckpt && B > 0) return fail(MG_E_ARG, "ckpt is NULL");
-  const size_t plane = (size_t)B * ldu;
-  const void* cur = x;
-  for (int l0 = 0, k = 0; l0 < L; l0 += seg, ++k) {
-    const int l1 = std::min(L, l0 + seg);
-    void* out = (l1 < L) ? static_cast<void*>(static_cast<float2*>(ckpt) + (size_t)k * plane) : y;
-    TRY(mg_propagate_range(OP_FWD, N, L, l0, l1, B, CR_GENERIC, geometry, cur, nullptr, out, nullptr, ldu, nullptr,
-                           nullptr, 0, nullptr, ws, wsb, stream));
-    cur = out;
-  }
-  return MG_OK;
+  // one launch over all layers; the kernel writes the field after every seg layers into ckpt (chunks of
+  // layers are cut so that they end on those layers)
+  Plan P;
+  TRY(make_plan(OP_FWD, N, L, B, CR_GENERIC, geometry, nullptr, &P));
+  TRY(check_ws(P, ws, wsb));
+  TRY(check_ldu(P, ldu));
+  TRY(check_field(x, "x", false, B > 0));
+  TRY(check_field(y, "y", false, B > 0));
+  TRY(check_field(ckpt, "ckpt", false, false));
+  int cl = std::min(P.CL, seg);
+  while (seg % cl) --cl;
+  P.CL = cl;
+  P.smem = launch_smem(P, OP_FWD, 0, L);
+  return run_prop(P, x, nullptr, y, nullptr, ldu, nullptr, 0, 0, static_cast<unsigned char*>(ws),
+                  static_cast<cudaStream_t>(stream), nullptr, L > seg ? ckpt : nullptr, seg);
 }
 
 int mg_lossy_backward(int N, int L, int B, int geometry, int seg, const void* x, const void* ckpt, const void* gy,
@@ -929,15 +976,17 @@ int mg_lossy_backward(int N, int L, int B, int geometry, int seg, const void* x,
     const int l0 = k * seg, l1 = std::min(L, l0 + seg);
     const void* in = (k == 0) ? x : static_cast<const void*>(static_cast<const float2*>(ckpt) + (size_t)(k - 1) * plane);
     // the layer inputs of the segment, recomputed from its checkpoint
-    TRY(mg_propagate_range(OP_FWD, N, L, l0, l1, B, CR_GENERIC, geometry, in, nullptr, nullptr, nullptr, ldu, act,
-                           nullptr, 0, nullptr, ws_fwd, wsb_fwd, stream));
-    // back-propagation through them; gradients alternate between gx and gtmp and end in gx
+    TRY(range_impl(OP_FWD, N, L, l0, l1, B, CR_GENERIC, geometry, in, nullptr, nullptr, nullptr, ldu, act, nullptr, 0,
+                   nullptr, ws_fwd, wsb_fwd, stream, false));
+    // back-propagation through them (its dJ/dT partials kept in place); gradients alternate between gx and
+    // gtmp and end in gx
     void* out = (k % 2 == 0) ? gx : gtmp;
-    TRY(mg_propagate_range(MG_OP_BWD_STORED, N, L, l0, l1, B, CR_GENERIC, geometry, nullptr, g, nullptr, out, ldu,
-                           act, dT, 0, nullptr, ws_bwd, wsb_bwd, stream));
+    TRY(range_impl(MG_OP_BWD_STORED, N, L, l0, l1, B, CR_GENERIC, geometry, nullptr, g, nullptr, out, ldu, act,
+                   nullptr, 0, nullptr, ws_bwd, wsb_bwd, stream, true));
     g = out;
   }
-  return MG_OK;
+  // dJ/dT of all layers from the partials of every segment, in one reduction
+  return reduce_raw(N, L, B, geometry, dT, 0, ws_bwd, wsb_bwd, stream);
 }
 
 int mg_fma_probe(float* sink, int blocks, int threads, int iters, void* stream) {

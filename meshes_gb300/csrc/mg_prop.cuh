@@ -68,6 +68,13 @@ struct PropArgs {
   const int* pflags;
   const int* perm_last;
   const int* pflag_last;
+  // forward checkpoints: after layer l (l + 1 < L, (l + 1) % ckpt_every == 0) the field is also written to
+  // ckpt + ((l + 1) / ckpt_every - 1) * ckpt_plane; chunk boundaries must fall on those layers
+  void* ckpt;
+  size_t ckpt_plane;
+  int ckpt_every;
+  // layers per CTA block of the partial buffer (0: L); lets layer ranges keep every range's partials
+  int pstride;
 };
 
 template <bool REAL> struct Fld { using T = float2; using C = C2x2; };
@@ -818,6 +825,11 @@ __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem
     const unsigned char* st = ring + (size_t)(c % a.S) * a.CL * a.layer_bytes;
     run_chunk<OP, M, V, REAL, GR, PERM, NN>(a, vb0, kinds, st, a.layer_bytes, lo, hi, gst_warp, gst_layer, G, j, r, u,
                                             w, pscr);
+    if constexpr (OP == OP_FWD && GR == 0) {
+      if (a.ckpt != nullptr && hi < a.L && hi % a.ckpt_every == 0)
+        store_fields<M, V, REAL>(u, static_cast<F*>(a.ckpt) + (size_t)(hi / a.ckpt_every - 1) * a.ckpt_plane, vb0,
+                                 a.vend, a.N, a.ldu, j);
+    }
     __syncthreads();
     if constexpr (OP == OP_BWD && kDirect) chunk_reduce_direct<M, GR>(a, kinds, lo, hi - lo, gst, np2, G);
     if constexpr (OP == OP_BWD && GR == 4) chunk_reduce_raw<M>(a, kinds, lo, hi - lo, gst, np2, G);
@@ -855,7 +867,8 @@ prop_kernel(const PropArgs a0) {
   const int G = GT ? GT : a.G;
   a.v0 = blockIdx.x * (a.W * (32 / G) * V);
   a.vend = a.B;
-  if (OP == OP_BWD) a.partial = a0.partial + (size_t)blockIdx.x * a.L * ((G * M) >> 1) * (GR == 4 ? 4 : 1);
+  if (OP == OP_BWD)
+    a.partial = a0.partial + (size_t)blockIdx.x * (a.pstride ? a.pstride : a.L) * ((G * M) >> 1) * (GR == 4 ? 4 : 1);
   prop_body<OP, M, V, REAL, GT, GR, PERM, NN>(a, smem);
 }
 
@@ -872,7 +885,8 @@ prop_split_kernel(const PropArgs a0) {
   const int G = GT ? GT : a.G;
   const int groups = a.W * (32 / G);
   a.vend = a.B;
-  if (OP == OP_BWD) a.partial = a0.partial + (size_t)blockIdx.x * a.L * ((G * M) >> 1) * (GR == 4 ? 4 : 1);
+  if (OP == OP_BWD)
+    a.partial = a0.partial + (size_t)blockIdx.x * (a.pstride ? a.pstride : a.L) * ((G * M) >> 1) * (GR == 4 ? 4 : 1);
   if ((int)blockIdx.x < a.nA) {
     a.v0 = blockIdx.x * groups * V;
     prop_body<OP, M, V, REAL, GT, GR, false, NN>(a, smem);
