@@ -70,8 +70,11 @@ batched_kernel(const mg_batch_mesh* __restrict__ meshes, int n_meshes, const mg_
       }
     }
     switch (md.cls) {
-      case MG_BCLS_C8: prop_body<OP, 8, 4, false, 0, (OP == OP_BWD ? 1 : 0), false, NN>(a, smem); break;
-      case MG_BCLS_C16: prop_body<OP, 16, 2, false, 0, (OP == OP_BWD ? 1 : 0), false, NN>(a, smem); break;
+      // one-vector crossings here: with three class bodies in one kernel the packed forms made
+      // back-propagation spill and gained nothing going forward (measured on GB300: the batched engine
+      // 13% and 3.5% slower)
+      case MG_BCLS_C8: prop_body<OP, 8, 4, false, 0, (OP == OP_BWD ? 1 : 0), false, NN, false>(a, smem); break;
+      case MG_BCLS_C16: prop_body<OP, 16, 2, false, 0, (OP == OP_BWD ? 1 : 0), false, NN, false>(a, smem); break;
       case MG_BCLS_R8: prop_body<OP, 8, 4, true, 0, (OP == OP_BWD ? 2 : 0), false, NN>(a, smem); break;
       default:
         if (threadIdx.x == 0) set_status(status, ST_BAD_WORK);

@@ -40,6 +40,40 @@ __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y
 __device__ __forceinline__ float2 cscale(float s, float2 a) { return make_float2(s * a.x, s * a.y); }
 __device__ __forceinline__ float2 ci(float2 a) { return make_float2(-a.y, a.x); }  // i*a
 
+// ---------------------------------------------------------------------------------------------
+// packed pairs: one float2 holds the same component of two vectors and goes through the f32x2
+// arithmetic of sm_100 and later (fma.rn.f32x2 etc.: one instruction, two results, each rounded
+// exactly as the scalar fmaf / mul / sub would round it)
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) {   // a*b + c
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+      "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 psub(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 pdup(float x) { return make_float2(x, x); }
+
 // real "complex" overloads used by the real (orth) instantiation of the same templates
 __device__ __forceinline__ float cmul(float a, float b) { return a * b; }
 __device__ __forceinline__ float cfma(float a, float b, float c) { return fmaf(a, b, c); }

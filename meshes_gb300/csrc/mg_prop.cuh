@@ -161,6 +161,62 @@ __device__ __forceinline__ void x_bwd_direct(const R2x2& t, float2, float& a, fl
   const float nga = fmaf(t.t10, gb, t.t00 * ga), ngb = fmaf(t.t11, gb, t.t01 * ga);
   a = xa; b = xb; ga = nga; gb = ngb;
 }
+
+// ---- the complex crossings on two vectors at once (vectors v, v+1 of the lane, same crossing).
+// Each scalar FMA of the one-vector forms above becomes one packed f32x2 FMA with the same operands in
+// the same order, so every field result is bitwise the one-vector result; half the instructions issue.
+// Coefficients enter as pairs (re, re), (im, im), (-im, -im) built once per crossing.
+struct PC {
+  float2 r, i, n;
+};
+__device__ __forceinline__ PC pc(float2 c) { return PC{pdup(c.x), pdup(c.y), pdup(-c.y)}; }
+// y = c1 b + c0 a:  cfma(c1, b, cmul(c0, a))
+__device__ __forceinline__ void p_lin(const PC& c0, const PC& c1, float2 ar, float2 ai, float2 br, float2 bi,
+                                      float2& yr, float2& yi) {
+  yr = pfma(c1.r, br, pfma(c1.n, bi, pfma(c0.r, ar, pmul(c0.n, ai))));
+  yi = pfma(c1.r, bi, pfma(c1.i, br, pfma(c0.r, ai, pmul(c0.i, ar))));
+}
+// y = conj(c1) b + conj(c0) a:  ccfma(c1, b, ccmul(c0, a))
+__device__ __forceinline__ void p_clin(const PC& c0, const PC& c1, float2 ar, float2 ai, float2 br, float2 bi,
+                                       float2& yr, float2& yi) {
+  yr = pfma(c1.r, br, pfma(c1.i, bi, pfma(c0.r, ar, pmul(c0.i, ai))));
+  yi = pfma(c1.r, bi, pfma(c1.n, br, pfma(c0.r, ai, pmul(c0.n, ar))));
+}
+__device__ __forceinline__ void x_fwd2(const PC (&c)[4], float2& a0, float2& b0, float2& a1, float2& b1) {
+  const float2 ar = make_float2(a0.x, a1.x), ai = make_float2(a0.y, a1.y);
+  const float2 br = make_float2(b0.x, b1.x), bi = make_float2(b0.y, b1.y);
+  float2 yar, yai, ybr, ybi;
+  p_lin(c[0], c[1], ar, ai, br, bi, yar, yai);   // ya = t01 b + t00 a
+  p_lin(c[2], c[3], ar, ai, br, bi, ybr, ybi);   // yb = t11 b + t10 a
+  a0 = make_float2(yar.x, yai.x); a1 = make_float2(yar.y, yai.y);
+  b0 = make_float2(ybr.x, ybi.x); b1 = make_float2(ybr.y, ybi.y);
+}
+// x_bwd_direct on two vectors; cc = (c, c), (s, s), (-s, -s), (-c, -c).  The dJ/dth terms use
+// -h0x = fmaf(-c, ga.x, -s * gb.y), the exact negation of h0x; the dJ/dph terms of the pair are kept as
+// two sums (+nga.y xa.x and +nga.x xa.y) that the caller subtracts once per crossing.
+__device__ __forceinline__ void x_bwd_direct2(const PC (&c)[4], const float2 (&cc)[4], float2& a0, float2& b0,
+                                              float2& ga0, float2& gb0, float2& a1, float2& b1, float2& ga1,
+                                              float2& gb1, float2& ath, float2& aph_p, float2& aph_q) {
+  const float2 ar = make_float2(a0.x, a1.x), ai = make_float2(a0.y, a1.y);
+  const float2 br = make_float2(b0.x, b1.x), bi = make_float2(b0.y, b1.y);
+  const float2 gar = make_float2(ga0.x, ga1.x), gai = make_float2(ga0.y, ga1.y);
+  const float2 gbr = make_float2(gb0.x, gb1.x), gbi = make_float2(gb0.y, gb1.y);
+  const float2 m0x = pfma(cc[0], ar, pmul(cc[1], bi)), m0y = pfma(cc[0], ai, pmul(cc[2], br));
+  const float2 nh0x = pfma(cc[3], gar, pmul(cc[2], gbi)), h0y = pfma(cc[0], gai, pmul(cc[2], gbr));
+  ath = pfma(h0y, m0x, pfma(nh0x, m0y, ath));
+  float2 xar, xai, xbr, xbi, gxar, gxai, gxbr, gxbi;
+  p_clin(c[0], c[2], ar, ai, br, bi, xar, xai);       // xa = conj(t10) b + conj(t00) a
+  p_clin(c[1], c[3], ar, ai, br, bi, xbr, xbi);       // xb = conj(t11) b + conj(t01) a
+  p_clin(c[0], c[2], gar, gai, gbr, gbi, gxar, gxai);
+  p_clin(c[1], c[3], gar, gai, gbr, gbi, gxbr, gxbi);
+  aph_p = pfma(gxai, xar, aph_p);
+  aph_q = pfma(gxar, xai, aph_q);
+  a0 = make_float2(xar.x, xai.x); a1 = make_float2(xar.y, xai.y);
+  b0 = make_float2(xbr.x, xbi.x); b1 = make_float2(xbr.y, xbi.y);
+  ga0 = make_float2(gxar.x, gxai.x); ga1 = make_float2(gxar.y, gxai.y);
+  gb0 = make_float2(gxbr.x, gxbi.x); gb1 = make_float2(gxbr.y, gxbi.y);
+}
+
 // stage a warp's (dJ/dth, dJ/dph) of one slot position
 __device__ __forceinline__ void acc2_stage(float2* gl2, int pos, int G, int r, float ath, float aph, bool store) {
   for (int off = G; off < 32; off <<= 1) {
@@ -218,10 +274,16 @@ struct Lanes {
   }
 };
 
-// ---- one crossing entry e of a layer (local modes a, b), applied to all V vectors of the lane
-template <int OP, int M, int V, bool REAL, int GR, typename F>
-__device__ __forceinline__ void entry(const float4* tl, int doff, int e, int a, int b, int G, int j, int r,
-                                      F (&u)[V][M], F (&w)[V][M], float4* gl) {
+#ifndef MG_PACKED_CROSSINGS
+#define MG_PACKED_CROSSINGS 1   // 0: every crossing in its one-vector form (for comparisons)
+#endif
+// ---- one crossing entry e of a layer applied to all V vectors of the lane; ua(v), ub(v) (wa, wb: the
+// second field) name the vector's two modes.  Complex forward (M >= 4, M*V >= 16) and direct MZI
+// back-propagation take the vectors two at a time through the packed forms: measured on GB300 over
+// Clements, Reck and FFT meshes of N = 32..600, back-propagation 4-17% and forward 1-10% faster.
+template <int OP, int M, int V, bool REAL, int GR, bool PK, typename UA, typename UB, typename WA, typename WB>
+__device__ __forceinline__ void crossing(const float4* tl, int doff, int e, int G, int j, int r, UA ua, UB ub, WA wa,
+                                         WB wb, float4* gl) {
   using CT = typename Fld<REAL>::C;
   CT t, d, acc;
   ld_coef(tl, e, G, j, t);
@@ -229,36 +291,64 @@ __device__ __forceinline__ void entry(const float4* tl, int doff, int e, int a, 
     float2 cs = make_float2(0.f, 0.f);
     if constexpr (GR == 1) cs = reinterpret_cast<const float2*>(tl + cs_off<M>(G))[e * G + j];
     float ath = 0.f, aph = 0.f;
+    if constexpr (PK && MG_PACKED_CROSSINGS && !REAL && GR == 1 && V >= 2) {
+      const PC c[4] = {pc(t.t00), pc(t.t01), pc(t.t10), pc(t.t11)};
+      const float2 cc[4] = {pdup(cs.x), pdup(cs.y), pdup(-cs.y), pdup(-cs.x)};
+      float2 ath2 = make_float2(0.f, 0.f), aph_p = ath2, aph_q = ath2;
 #pragma unroll
-    for (int v = 0; v < V; ++v) x_bwd_direct(t, cs, u[v][a], u[v][b], w[v][a], w[v][b], ath, aph);
+      for (int v = 0; v + 1 < V; v += 2)
+        x_bwd_direct2(c, cc, ua(v), ub(v), wa(v), wb(v), ua(v + 1), ub(v + 1), wa(v + 1), wb(v + 1), ath2, aph_p,
+                      aph_q);
+      const float2 dph = psub(aph_p, aph_q);
+      ath = ath2.x + ath2.y;
+      aph = dph.x + dph.y;
+      if constexpr (V & 1) x_bwd_direct(t, cs, ua(V - 1), ub(V - 1), wa(V - 1), wb(V - 1), ath, aph);
+    } else {
+#pragma unroll
+      for (int v = 0; v < V; ++v) x_bwd_direct(t, cs, ua(v), ub(v), wa(v), wb(v), ath, aph);
+    }
     acc2_stage(reinterpret_cast<float2*>(gl), e * G + j, G, r, ath, aph, true);
+  } else if constexpr (PK && MG_PACKED_CROSSINGS && OP == OP_FWD && !REAL && V >= 2 && M >= 4 && M * V >= 16) {
+    // (smaller forward tiles keep the one-vector form: the coefficient pairs made them spill; measured on
+    // GB300 at N = 32 and 64: 7% slower)
+    const PC c[4] = {pc(t.t00), pc(t.t01), pc(t.t10), pc(t.t11)};
+#pragma unroll
+    for (int v = 0; v + 1 < V; v += 2) x_fwd2(c, ua(v), ub(v), ua(v + 1), ub(v + 1));
+    if constexpr (V & 1) x_fwd(t, ua(V - 1), ub(V - 1));
   } else {
     if constexpr (OP == OP_FWDDIFF) ld_coef(tl + doff, e, G, j, d);
     if constexpr (OP == OP_BWD) acc_zero(acc);
 #pragma unroll
-    for (int v = 0; v < V; ++v) xop<OP, GR>(t, d, u[v][a], u[v][b], w[v][a], w[v][b], acc);
+    for (int v = 0; v < V; ++v) xop<OP, GR>(t, d, ua(v), ub(v), wa(v), wb(v), acc);
     if constexpr (OP == OP_BWD) acc_stage(gl, e, G, j, r, acc);
   }
 }
+// ---- entry e between the lane's own modes a and b
+template <int OP, int M, int V, bool REAL, int GR, bool PK, typename F>
+__device__ __forceinline__ void entry(const float4* tl, int doff, int e, int a, int b, int G, int j, int r,
+                                      F (&u)[V][M], F (&w)[V][M], float4* gl) {
+  crossing<OP, M, V, REAL, GR, PK>(
+      tl, doff, e, G, j, r, [&](int v) -> F& { return u[v][a]; }, [&](int v) -> F& { return u[v][b]; },
+      [&](int v) -> F& { return w[v][a]; }, [&](int v) -> F& { return w[v][b]; }, gl);
+}
 
 // ---- layer with all pairs inside the lane: (a, a+SS), a = 2*SS*(e/SS) + e%SS
-template <int OP, int M, int V, bool REAL, int GR, int SS, typename F>
+template <int OP, int M, int V, bool REAL, int GR, int SS, bool PK = true, typename F>
 __device__ __forceinline__ void layer_local(const float4* tl, int G, int j, int r, F (&u)[V][M], F (&w)[V][M],
                                             float4* gl) {
   const int doff = dt_off<REAL, M>(G);
 #pragma unroll
   for (int e = 0; e < M / 2; ++e) {
     const int a = 2 * SS * (e / SS) + (e % SS);
-    entry<OP, M, V, REAL, GR>(tl, doff, e, a, a + SS, G, j, r, u, w, gl);
+    entry<OP, M, V, REAL, GR, PK>(tl, doff, e, a, a + SS, G, j, r, u, w, gl);
   }
 }
 
 // ---- nearest-neighbour layer with odd shift: pairs (2e+1, 2e+2) and the lane-boundary pair
 // (mode M-1 of lane j, mode 0 of lane j+1) computed by lane j (reference gpu/fwdprop.cu:98-106)
-template <int OP, int M, int V, bool REAL, int GR, typename F>
+template <int OP, int M, int V, bool REAL, int GR, bool PK = true, typename F>
 __device__ __forceinline__ void layer_mis(const float4* tl, int G, int j, int r, F (&u)[V][M], F (&w)[V][M],
                                           float4* gl) {
-  using CT = typename Fld<REAL>::C;
   const int doff = dt_off<REAL, M>(G);
   F nu[V], nw[V];
 #pragma unroll
@@ -267,26 +357,10 @@ __device__ __forceinline__ void layer_mis(const float4* tl, int G, int j, int r,
     if constexpr (OP != OP_FWD) nw[v] = shfl_down(w[v][0], 1, G);
   }
 #pragma unroll
-  for (int e = 0; e < M / 2 - 1; ++e) entry<OP, M, V, REAL, GR>(tl, doff, e, 2 * e + 1, 2 * e + 2, G, j, r, u, w, gl);
-  {
-    constexpr int e = M / 2 - 1;
-    CT t, d, acc;
-    ld_coef(tl, e, G, j, t);
-    if constexpr (OP == OP_BWD && (GR == 1 || GR == 2)) {
-      float2 cs = make_float2(0.f, 0.f);
-      if constexpr (GR == 1) cs = reinterpret_cast<const float2*>(tl + cs_off<M>(G))[e * G + j];
-      float ath = 0.f, aph = 0.f;
-#pragma unroll
-      for (int v = 0; v < V; ++v) x_bwd_direct(t, cs, u[v][M - 1], nu[v], w[v][M - 1], nw[v], ath, aph);
-      acc2_stage(reinterpret_cast<float2*>(gl), e * G + j, G, r, ath, aph, true);
-    } else {
-      if constexpr (OP == OP_FWDDIFF) ld_coef(tl + doff, e, G, j, d);
-      if constexpr (OP == OP_BWD) acc_zero(acc);
-#pragma unroll
-      for (int v = 0; v < V; ++v) xop<OP, GR>(t, d, u[v][M - 1], nu[v], w[v][M - 1], nw[v], acc);
-      if constexpr (OP == OP_BWD) acc_stage(gl, e, G, j, r, acc);
-    }
-  }
+  for (int e = 0; e < M / 2 - 1; ++e) entry<OP, M, V, REAL, GR, PK>(tl, doff, e, 2 * e + 1, 2 * e + 2, G, j, r, u, w, gl);
+  crossing<OP, M, V, REAL, GR, PK>(
+      tl, doff, M / 2 - 1, G, j, r, [&](int v) -> F& { return u[v][M - 1]; }, [&](int v) -> F& { return nu[v]; },
+      [&](int v) -> F& { return w[v][M - 1]; }, [&](int v) -> F& { return nw[v]; }, gl);
 #pragma unroll
   for (int v = 0; v < V; ++v) {
     const F bu = shfl_up(nu[v], 1, G);
@@ -394,20 +468,20 @@ __device__ __forceinline__ void layer_xl(const float4* tl, int d, int G, int j, 
 
 // ---- one layer of any kind; NN (nearest-neighbour instantiations): kinds 0 and KIND_MIS only, which keeps
 // the strided and butterfly bodies, and their registers, out of the kernel
-template <int OP, int M, int V, bool REAL, int GR, bool NN = false, typename F>
+template <int OP, int M, int V, bool REAL, int GR, bool NN = false, bool PK = true, typename F>
 __device__ __forceinline__ void layer_any(int kind, const float4* tl, int G, int j, int r, F (&u)[V][M],
                                           F (&w)[V][M], float4* gl) {
   if constexpr (NN) {
-    if (kind == KIND_MIS) layer_mis<OP, M, V, REAL, GR>(tl, G, j, r, u, w, gl);
-    else layer_local<OP, M, V, REAL, GR, 1>(tl, G, j, r, u, w, gl);
+    if (kind == KIND_MIS) layer_mis<OP, M, V, REAL, GR, PK>(tl, G, j, r, u, w, gl);
+    else layer_local<OP, M, V, REAL, GR, 1, PK>(tl, G, j, r, u, w, gl);
     return;
   }
   switch (kind) {
-    case 0: layer_local<OP, M, V, REAL, GR, 1>(tl, G, j, r, u, w, gl); break;
-    case 1: if constexpr (M >= 4) layer_local<OP, M, V, REAL, GR, 2>(tl, G, j, r, u, w, gl); break;
-    case 2: if constexpr (M >= 8) layer_local<OP, M, V, REAL, GR, 4>(tl, G, j, r, u, w, gl); break;
-    case 3: if constexpr (M >= 16) layer_local<OP, M, V, REAL, GR, 8>(tl, G, j, r, u, w, gl); break;
-    case KIND_MIS: layer_mis<OP, M, V, REAL, GR>(tl, G, j, r, u, w, gl); break;
+    case 0: layer_local<OP, M, V, REAL, GR, 1, PK>(tl, G, j, r, u, w, gl); break;
+    case 1: if constexpr (M >= 4) layer_local<OP, M, V, REAL, GR, 2, PK>(tl, G, j, r, u, w, gl); break;
+    case 2: if constexpr (M >= 8) layer_local<OP, M, V, REAL, GR, 4, PK>(tl, G, j, r, u, w, gl); break;
+    case 3: if constexpr (M >= 16) layer_local<OP, M, V, REAL, GR, 8, PK>(tl, G, j, r, u, w, gl); break;
+    case KIND_MIS: layer_mis<OP, M, V, REAL, GR, PK>(tl, G, j, r, u, w, gl); break;
     default: layer_xl<OP, M, V, REAL, GR>(tl, 1 << (kind - KIND_XL - ilog2_const(M)), G, j, r, u, w, gl);
   }
 }
@@ -664,7 +738,7 @@ struct PropTraits {
 // layer's input to a.act before applying it, back-propagation reloads it in place of T^H reconstruction.
 // PERM (the permuted-mesh instantiations): a layer whose kind carries KIND_PERM is preceded by the gather of
 // its row of pa.perm (the shared-memory copy of the kinds carries the flags).
-template <int OP, int M, int V, bool REAL, int GR, bool PERM, bool NN, typename F>
+template <int OP, int M, int V, bool REAL, int GR, bool PERM, bool NN, bool PK, typename F>
 __device__ __forceinline__ void run_chunk(const PropArgs& pa, int vb0, const int* kinds, const unsigned char* st,
                                           unsigned layer_bytes, int lo, int hi, unsigned char* gst_warp,
                                           size_t gst_layer, int G, int j, int r, F (&u)[V][M], F (&w)[V][M],
@@ -677,7 +751,7 @@ __device__ __forceinline__ void run_chunk(const PropArgs& pa, int vb0, const int
       F* plane = static_cast<F*>(pa.act) + (size_t)l * pa.act_plane;
       if constexpr (OP == OP_BWD) load_fields<M, V, REAL>(u, plane, vb0, pa.vend, pa.N, pa.ldu, j);
       else store_fields<M, V, REAL>(u, plane, vb0, pa.vend, pa.N, pa.ldu, j);
-      layer_any<OP, M, V, REAL, GR>(kinds[l], reinterpret_cast<const float4*>(st + (size_t)(l - lo) * layer_bytes), G,
+      layer_any<OP, M, V, REAL, GR, false, PK>(kinds[l], reinterpret_cast<const float4*>(st + (size_t)(l - lo) * layer_bytes), G,
                                     j, r, u, w, reinterpret_cast<float4*>(gst_warp + (size_t)(l - lo) * gst_layer));
     }
     return;
@@ -703,28 +777,32 @@ __device__ __forceinline__ void run_chunk(const PropArgs& pa, int vb0, const int
       // (aligned then odd-shift going forward, odd-shift then aligned going back): the second fused body
       // made the back-propagation kernel spill (measured on GB300: 5% slower with both bodies)
       if ((!NN || OP != OP_BWD) && k0 == 0 && k1 == KIND_MIS) {
-        layer_local<OP, M, V, REAL, GR, 1>(t0, G, j, r, u, w, g0);
-        layer_mis<OP, M, V, REAL, GR>(t1, G, j, r, u, w, g1);
+        layer_local<OP, M, V, REAL, GR, 1, PK>(t0, G, j, r, u, w, g0);
+        layer_mis<OP, M, V, REAL, GR, PK>(t1, G, j, r, u, w, g1);
         i += 2;
         continue;
       }
       if ((!NN || OP == OP_BWD) && k0 == KIND_MIS && k1 == 0) {
-        layer_mis<OP, M, V, REAL, GR>(t0, G, j, r, u, w, g0);
-        layer_local<OP, M, V, REAL, GR, 1>(t1, G, j, r, u, w, g1);
+        layer_mis<OP, M, V, REAL, GR, PK>(t0, G, j, r, u, w, g0);
+        layer_local<OP, M, V, REAL, GR, 1, PK>(t1, G, j, r, u, w, g1);
         i += 2;
         continue;
       }
     }
-    layer_any<OP, M, V, REAL, GR, NN>(k0, t0, G, j, r, u, w, g0);
+    layer_any<OP, M, V, REAL, GR, NN, PK>(k0, t0, G, j, r, u, w, g0);
     i += 1;
   }
 }
 
 // One batch tile of one mesh: vectors [a.v0, a.vend), all L layers, by the W warps of the CTA.
 // Shared by the one-mesh kernel (prop_kernel) and the persistent multi-mesh kernel (mg_batched.cu).
-template <int OP, int M, int V, bool REAL, int GT, int GR, bool PERM = false, bool NN = false>
+// PK: complex forward and direct back-propagation crossings take vectors in pairs (packed f32x2 forms).
+// Permuted and stored-activation kernels, and forward kernels of lane groups narrower than the warp, keep
+// the one-vector forms: measured on GB300 the packed forms made them 3-14% slower (more registers, spills).
+template <int OP, int M, int V, bool REAL, int GT, int GR, bool PERM = false, bool NN = false, bool PK = true>
 __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem) {
   using F = typename Fld<REAL>::T;
+  constexpr bool kPacked = PK && !PERM && GR != 4 && (OP != OP_FWD || GT == 32);
   const int tid = threadIdx.x, warp = tid >> 5;
   const Lanes<GT> ln(a.G, a.logG);
   const int G = ln.G, j = ln.j, r = ln.r, R = 32 / G;
@@ -823,7 +901,7 @@ __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem
       if (tid == 0) issue_d(c);
     }
     const unsigned char* st = ring + (size_t)(c % a.S) * a.CL * a.layer_bytes;
-    run_chunk<OP, M, V, REAL, GR, PERM, NN>(a, vb0, kinds, st, a.layer_bytes, lo, hi, gst_warp, gst_layer, G, j, r, u,
+    run_chunk<OP, M, V, REAL, GR, PERM, NN, kPacked>(a, vb0, kinds, st, a.layer_bytes, lo, hi, gst_warp, gst_layer, G, j, r, u,
                                             w, pscr);
     if constexpr (OP == OP_FWD && GR == 0) {
       if (a.ckpt != nullptr && hi < a.L && hi % a.ckpt_every == 0)
