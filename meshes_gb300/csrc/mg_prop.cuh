@@ -182,6 +182,11 @@ __device__ __forceinline__ void p_clin(const PC& c0, const PC& c1, float2 ar, fl
   yr = pfma(c1.r, br, pfma(c1.i, bi, pfma(c0.r, ar, pmul(c0.i, ai))));
   yi = pfma(c1.r, bi, pfma(c1.n, br, pfma(c0.r, ai, pmul(c0.n, ar))));
 }
+// acc += c x:  cfma(c, x, acc)
+__device__ __forceinline__ void p_acc(const PC& c, float2 xr, float2 xi, float2& accr, float2& acci) {
+  accr = pfma(c.r, xr, pfma(c.n, xi, accr));
+  acci = pfma(c.r, xi, pfma(c.i, xr, acci));
+}
 __device__ __forceinline__ void x_fwd2(const PC (&c)[4], float2& a0, float2& b0, float2& a1, float2& b1) {
   const float2 ar = make_float2(a0.x, a1.x), ai = make_float2(a0.y, a1.y);
   const float2 br = make_float2(b0.x, b1.x), bi = make_float2(b0.y, b1.y);
@@ -190,6 +195,24 @@ __device__ __forceinline__ void x_fwd2(const PC (&c)[4], float2& a0, float2& b0,
   p_lin(c[2], c[3], ar, ai, br, bi, ybr, ybi);   // yb = t11 b + t10 a
   a0 = make_float2(yar.x, yai.x); a1 = make_float2(yar.y, yai.y);
   b0 = make_float2(ybr.x, ybi.x); b1 = make_float2(ybr.y, ybi.y);
+}
+// x_fwddiff on two vectors (dc: the packed dT/dp coefficients)
+__device__ __forceinline__ void x_fwddiff2(const PC (&c)[4], const PC (&dc)[4], float2& a0, float2& b0, float2& da0,
+                                           float2& db0, float2& a1, float2& b1, float2& da1, float2& db1) {
+  const float2 ar = make_float2(a0.x, a1.x), ai = make_float2(a0.y, a1.y);
+  const float2 br = make_float2(b0.x, b1.x), bi = make_float2(b0.y, b1.y);
+  const float2 dar = make_float2(da0.x, da1.x), dai = make_float2(da0.y, da1.y);
+  const float2 dbr = make_float2(db0.x, db1.x), dbi = make_float2(db0.y, db1.y);
+  float2 nar, nai, nbr, nbi;
+  p_lin(c[0], c[1], dar, dai, dbr, dbi, nar, nai);   // nda = d01 b + d00 a + t01 db + t00 da
+  p_acc(dc[0], ar, ai, nar, nai);
+  p_acc(dc[1], br, bi, nar, nai);
+  p_lin(c[2], c[3], dar, dai, dbr, dbi, nbr, nbi);   // ndb = d11 b + d10 a + t11 db + t10 da
+  p_acc(dc[2], ar, ai, nbr, nbi);
+  p_acc(dc[3], br, bi, nbr, nbi);
+  da0 = make_float2(nar.x, nai.x); da1 = make_float2(nar.y, nai.y);
+  db0 = make_float2(nbr.x, nbi.x); db1 = make_float2(nbr.y, nbi.y);
+  x_fwd2(c, a0, b0, a1, b1);
 }
 // x_bwd_direct on two vectors; cc = (c, c), (s, s), (-s, -s), (-c, -c).  The dJ/dth terms use
 // -h0x = fmaf(-c, ga.x, -s * gb.y), the exact negation of h0x; the dJ/dph terms of the pair are kept as
@@ -315,6 +338,14 @@ __device__ __forceinline__ void crossing(const float4* tl, int doff, int e, int 
 #pragma unroll
     for (int v = 0; v + 1 < V; v += 2) x_fwd2(c, ua(v), ub(v), ua(v + 1), ub(v + 1));
     if constexpr (V & 1) x_fwd(t, ua(V - 1), ub(V - 1));
+  } else if constexpr (PK && MG_PACKED_CROSSINGS && OP == OP_FWDDIFF && !REAL && V >= 2 && M >= 4 && M * V >= 16) {
+    ld_coef(tl + doff, e, G, j, d);
+    const PC c[4] = {pc(t.t00), pc(t.t01), pc(t.t10), pc(t.t11)};
+    const PC dc[4] = {pc(d.t00), pc(d.t01), pc(d.t10), pc(d.t11)};
+#pragma unroll
+    for (int v = 0; v + 1 < V; v += 2)
+      x_fwddiff2(c, dc, ua(v), ub(v), wa(v), wb(v), ua(v + 1), ub(v + 1), wa(v + 1), wb(v + 1));
+    if constexpr (V & 1) x_fwddiff(t, d, ua(V - 1), ub(V - 1), wa(V - 1), wb(V - 1));
   } else {
     if constexpr (OP == OP_FWDDIFF) ld_coef(tl + doff, e, G, j, d);
     if constexpr (OP == OP_BWD) acc_zero(acc);
@@ -802,7 +833,7 @@ __device__ __forceinline__ void run_chunk(const PropArgs& pa, int vb0, const int
 template <int OP, int M, int V, bool REAL, int GT, int GR, bool PERM = false, bool NN = false, bool PK = true>
 __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem) {
   using F = typename Fld<REAL>::T;
-  constexpr bool kPacked = PK && !PERM && GR != 4 && (OP != OP_FWD || GT == 32);
+  constexpr bool kPacked = PK && !PERM && GR != 4 && (OP == OP_BWD || GT == 32);
   const int tid = threadIdx.x, warp = tid >> 5;
   const Lanes<GT> ln(a.G, a.logG);
   const int G = ln.G, j = ln.j, r = ln.r, R = 32 / G;
