@@ -412,6 +412,62 @@ def test_split_launch_parity(cr, N, B):
     assert O.rel_err(outs[2][1].cpu().numpy().reshape(om.L, N // 2, n_p), O.contract_dp(om, G)) < TOL
 
 
+@pytest.mark.parametrize("N,M", [(256, 8), (128, 4)])
+@pytest.mark.parametrize("V", [2, 4])
+def test_packed_crossing_tiles(N, M, V):
+    """Explicit full-warp tiles whose forward, forward-mode derivative and back-propagation take the vectors
+    two at a time (packed f32x2 crossings), on a ragged batch, against the oracle."""
+    from meshes_gb300 import _lib
+    import ctypes
+    lib = _lib.load()
+    B = 301
+    rng = np.random.default_rng(N * 31 + V)
+    om = O.random_mesh(rng, N, "clements", "mzi", 0.02)
+    x = O.unit_columns(rng, N, B)
+    dx = O.unit_columns(rng, N, B)
+    g = O.unit_columns(rng, N, B)
+    dpdir = rng.standard_normal((om.L, N // 2, 2)).astype(np.float32)
+    m = gpu_mesh(om)
+    xd, dxd, gd = (torch.tensor(a, dtype=torch.complex64, device="cuda") for a in (x, dx, g))
+    y, dy, gx = torch.empty_like(xd), torch.empty_like(xd), torch.empty_like(xd)
+    dpd = torch.tensor(dpdir.reshape(-1), device="cuda")
+    dp = torch.empty(m.p_phase.numel(), device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    s = m.p_splitter
+    ldp, lds = N // 2 * m.X_np, N // 2 * m.X_ns
+    for op in (0, 1, 2):
+        cfg = _lib.config(M, V, 8, 0, 2, 2)
+        info = _lib.mg_plan_info()
+        assert lib.mg_plan(op, N, om.L, B, m.crossing, 0, _lib.cfg_ptr(cfg), ctypes.byref(info)) == 0
+        assert (info.M, info.V, info.G) == (M, V, 32)
+        nb = info.total
+        ws = torch.zeros(nb, dtype=torch.uint8, device="cuda")
+        assert lib.mg_build_tiles(op, N, om.L, 0, m.lens.data_ptr(), m.shifts.data_ptr(), None, m.crossing,
+                                  m.p_phase.data_ptr(), ldp, s.data_ptr() if s.numel() else None, lds,
+                                  dpd.data_ptr() if op == 1 else None, None, None, B, _lib.cfg_ptr(cfg),
+                                  ws.data_ptr(), nb, st) == 0, _lib.last_error()
+        if op == 0:
+            rc = lib.mg_propagate(0, N, om.L, B, m.crossing, 0, xd.data_ptr(), None, y.data_ptr(), None, N, None, 0,
+                                  0, _lib.cfg_ptr(cfg), ws.data_ptr(), nb, st)
+        elif op == 1:
+            rc = lib.mg_propagate(1, N, om.L, B, m.crossing, 0, xd.data_ptr(), dxd.data_ptr(), y.data_ptr(),
+                                  dy.data_ptr(), N, None, 0, 0, _lib.cfg_ptr(cfg), ws.data_ptr(), nb, st)
+        else:
+            rc = lib.mg_propagate(2, N, om.L, B, m.crossing, 0, y.data_ptr(), gd.data_ptr(), None, gx.data_ptr(), N,
+                                  dp.data_ptr(), ldp, 0, _lib.cfg_ptr(cfg), ws.data_ptr(), nb, st)
+        assert rc == 0, _lib.last_error()
+        assert lib.mg_read_status(ws.data_ptr(), 0, st) == 0
+        if op == 1:
+            y_ref, dy_ref = O.fwddiff(om, x, dpdir, dx)
+            assert O.rel_err(y.cpu().numpy(), y_ref) < TOL
+            assert O.rel_err(dy.cpu().numpy(), dy_ref) < TOL
+    y_ref = O.propagate(om, x)
+    G, _, gin = O.vjp_unitary(om, y.cpu().numpy().astype(np.complex128), g)
+    assert O.rel_err(y.cpu().numpy(), y_ref) < TOL
+    assert O.rel_err(gx.cpu().numpy(), gin) < TOL
+    assert O.rel_err(dp.cpu().numpy().reshape(om.L, N // 2, 2), O.contract_dp(om, G)) < TOL
+
+
 def test_coefficient_trigonometry_matches_library():
     """The coefficient precompute's own double sin/cos (Cody-Waite reduction + Taylor series) agrees with
     the CUDA library's to a few units in the last place, over phase-like, small and large arguments; its
