@@ -135,3 +135,37 @@ def mesh_apply(mesh: MeshNetworkGPU, x: torch.Tensor, p: Optional[torch.Tensor] 
     if mesh.phi_pos == "in":
         return MeshFunction.apply(x * d, p, mesh)
     return MeshFunction.apply(x, p, mesh) * d
+
+
+class GraphedStep:
+    """A training step captured once in a CUDA graph and replayed.
+
+    ``step()`` takes no arguments, runs the forward pass (through ``mesh_apply``), the backward pass and
+    the optimizer update, and returns the loss tensor. A small mesh or batch makes such a step
+    launch-bound: a dozen kernels (coefficient tiles, forward, loss, back-propagation, reduction,
+    optimizer) and the Python around them. A replay costs one graph launch.
+
+    Requirements, as for any CUDA-graph capture:
+    - every tensor the step reads keeps its storage between replays (update inputs in place);
+    - the optimizer keeps its state on the device (``torch.optim.Adam(..., capturable=True)``).
+
+    The ``warmup`` calls before the capture are real steps; they also size the meshes' cached workspaces.
+    The mesh kernels launch on the current stream and never synchronise, so the capture records them.
+    """
+
+    def __init__(self, step, warmup: int = 3):
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            for _ in range(warmup):
+                step()
+        torch.cuda.current_stream().wait_stream(side)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.loss = step()
+
+    def __call__(self) -> torch.Tensor:
+        """Run one more step; returns the loss tensor of that step (the same storage on every call)."""
+        self.graph.replay()
+        return self.loss
+

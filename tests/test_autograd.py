@@ -171,3 +171,37 @@ def test_unitary_fitting_training_loop():
     assert abs(fid_gpu - fid_ref) < 1e-5             # the GPU's U is the complex128 U
     assert O.rel_err(U, U128) < 1e-5
     assert abs(loss_ref - loss_end) < 1e-4 * loss_ref
+
+
+@pytest.mark.parametrize("geo,N,B", [("clements", 32, 16), ("fft", 64, 24)])
+def test_graphed_training_step_matches_eager(geo, N, B):
+    """A training step captured in a CUDA graph (GraphedStep) and replayed follows the eager steps
+    exactly: same losses, bitwise the same phases after 3 warm-up and 12 replayed steps."""
+    from meshes_gb300.autograd import GraphedStep, mesh_apply
+    rng = np.random.default_rng(2024 + N)
+    om = O.random_mesh(rng, N, geo, "mzi", 0.02)
+    m = gpu_mesh(om)
+    x = torch.tensor(O.unit_columns(rng, N, B), dtype=torch.complex64, device="cuda")
+    target = torch.tensor(O.unit_columns(rng, N, B), dtype=torch.complex64, device="cuda")
+
+    def trainer():
+        p = torch.tensor(om.p, dtype=torch.float32, device="cuda", requires_grad=True)
+        opt = torch.optim.Adam([p], lr=1e-2, capturable=True)
+
+        def step():
+            opt.zero_grad(set_to_none=True)
+            loss = ((mesh_apply(m, x, p) - target).abs() ** 2).sum()
+            loss.backward()
+            opt.step()
+            return loss
+        return p, step
+
+    p_e, step_e = trainer()
+    eager = [float(step_e()) for _ in range(15)]
+    p_g, step_g = trainer()
+    g = GraphedStep(step_g, warmup=3)
+    graphed = [float(g()) for _ in range(12)]
+    assert graphed == eager[3:]
+    assert torch.equal(p_g.detach(), p_e.detach())
+    assert eager[-1] < eager[0]
+    assert m.status() == 0
