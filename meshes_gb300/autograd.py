@@ -151,6 +151,8 @@ class GraphedStep:
 
     The ``warmup`` calls before the capture are real steps; they also size the meshes' cached workspaces.
     The mesh kernels launch on the current stream and never synchronise, so the capture records them.
+    Their run-time status (a bounded wait that expired, a malformed geometry) accumulates in the mesh's
+    workspaces across replays: read it with ``mesh.status()`` between replays.
     """
 
     def __init__(self, step, warmup: int = 3):

@@ -456,8 +456,16 @@ class MeshNetworkGPU:
         return torch.stack([self.hvp_target(vi, U_target, p_phase, p_splitter, eps) for vi in vec])
 
     def status(self, clear=True) -> int:
-        """Run-time status recorded by the kernels (0 ok, 1 timeout, 2 bad geometry); synchronises."""
-        return max(ws.status(clear) for ws in self._ws.values())
+        """Run-time status recorded by the kernels (0 ok, 1 timeout, 2 bad geometry) in the workspaces of
+        the drop-in methods and of the autograd function (``mesh_apply``); synchronises."""
+        rc = max((ws.status(clear) for ws in self._ws.values()), default=0)
+        for plan in getattr(self, "_autograd_plans", {}).values():
+            if plan.buf is not None:
+                v = load().mg_read_status(plan.buf.data_ptr(), int(clear), _stream(self.device))
+                if v < 0:
+                    check(v, "mg_read_status")
+                rc = max(rc, v)
+        return rc
 
 
 def _perm_rows(perm, N: int, L: int):
