@@ -304,7 +304,7 @@ struct Lanes {
 // second field) name the vector's two modes.  Complex forward and forward-mode derivative (M >= 4,
 // M*V >= 16) and direct MZI back-propagation take the vectors two at a time through the packed forms:
 // measured on GB300 over Clements, Reck and FFT meshes of N = 32..600, back-propagation 4-18% and
-// forward up to 13% faster.
+// forward up to 16% faster.
 template <int OP, int M, int V, bool REAL, int GR, bool PK, typename UA, typename UB, typename WA, typename WB>
 __device__ __forceinline__ void crossing(const float4* tl, int doff, int e, int G, int j, int r, UA ua, UB ub, WA wa,
                                          WB wb, float4* gl) {
