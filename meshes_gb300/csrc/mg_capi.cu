@@ -310,7 +310,12 @@ int build_tiles(const Plan& P, const int* lens, const int* shifts, const int* st
   a.kinds = reinterpret_cast<int*>(ws + P.off_kinds);
   a.status = reinterpret_cast<int*>(ws);
   const int n = P.L * P.np2;
-  coef_kernel<<<(n + 255) / 256, 256, 0, st>>>(a);
+  // one thread per slot.  The pass is bound by each SM's narrow FP64 pipe, so a small mesh is spread over
+  // every SM in blocks of 32 to 256 threads rather than packed into a few 256-thread blocks.
+  const int sms = dev_info().sms;
+  int bt = 256;
+  if (n < 256 * sms) bt = std::max(32, std::min(256, ((n + sms - 1) / sms + 31) / 32 * 32));
+  coef_kernel<<<(n + bt - 1) / bt, bt, 0, st>>>(a);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MG_OK : cuda_fail(e, "coef_kernel launch");
 }
