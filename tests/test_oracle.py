@@ -349,3 +349,28 @@ def test_header_symbols_exported():
         assert hasattr(lib, name), name
     assert declared == set(_lib.exported_symbols())
     assert lib.mg_version().decode().startswith("meshes_gb300")
+
+
+def test_tuning_table_entries_are_valid_plans():
+    """Every configuration in the committed tuning table plans (mg_plan: host-side arithmetic only) at both
+    ends of its batch range, with the register tile it names; planning needs no GPU."""
+    import ctypes
+    import json
+    from meshes_gb300 import _lib
+    from meshes_gb300.build import build
+    build()
+    lib = _lib.load()
+    table = json.load(open(os.path.join(ROOT, "meshes_gb300", "tuned_configs.json")))
+    assert table
+    for key, entries in table.items():
+        op, crossing, geometry, N = (int(v) for v in key.split("/"))
+        for e in entries:
+            lo, hi = e["B"]
+            assert 1 <= lo <= hi
+            for B in (lo, hi):
+                info = _lib.mg_plan_info()
+                rc = lib.mg_plan(op, N, N, B, crossing, geometry, _lib.cfg_ptr(_lib.config(*e["cfg"])),
+                                 ctypes.byref(info))
+                assert rc == 0, (key, B, _lib.last_error())
+                assert (info.M, info.V, info.W) == tuple(e["cfg"][:3])
+                assert info.smem <= 227 * 1024 and info.grid >= 1
