@@ -1,18 +1,33 @@
 """Benchmark of the mesh-propagation hot path on GB300.
 
-Workload (one "step"): forward propagation plus back-propagation of phase gradients through an
-imperfect Clements MZI mesh, N=256 modes, L=256 layers (32640 MZIs), splitting errors
-alpha, beta ~ N(0, 0.02), B=4096 complex64 unit-norm input vectors, loss J = sum |y - y_t|^2:
-  mg_fwdprop (x -> y), g = 2 (y - y_t), mg_backdiff (y, g -> dJ/dp, dJ/dx*).
-Metric: MZI applications per second for fwd+bwd (n_MZI * B per step), with the fraction of the FP32
-CUDA-core peak at the reference's own FLOP counts (32 per MZI-application forward, 96 backward).
+The default run (``python bench.py [--gpus N] [--steps K] [--warmup W]``) prints ONE JSON line.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Headline: one training step (forward propagation plus back-propagation of phase gradients) through an
+imperfect Clements MZI mesh, N=256 modes, L=256 layers (32640 MZIs), splitting errors alpha, beta ~
+N(0, 0.02), B=4096 complex64 unit-norm vectors, J = sum |y - y_t|^2.  Metric: MZI applications per second
+(n_MZI * B per step), and the fraction of the FP32 CUDA-core peak at the reference's own FLOP counts (32 per
+MZI-application forward, 96 backward; reference gpu/test.py:208,220).
 
-Under torchrun (N > 1) every rank runs an independent replica on its own GPU (the path needs no
-collective); value = all ranks' MZI applications / max-over-ranks time.  ``--impl reference`` times
-the reference algorithm's CPU implementation (the oracle's C++ port of c/dot.cpp, all host threads)
-on the same workload, on rank 0 only.
+"configs" holds the other workloads of the same run, each with its error against a complex128 evaluation
+of the same mesh and its fraction of the FP32 roofline:
+  plain forward    Clements N=64 L=64 ideal splitters, B=1024, one reference-shaped call (mg_fwdprop);
+  batched          512 uneven meshes (Clements-mzi, Reck-mzi, Clements-orth; N in {8..256}; B in [1, 2048]),
+                   one mesh per call against one persistent launch replayed from a CUDA graph, forward and
+                   forward + backward;
+  unitary fit      Clements N=128 L=128 with splitting errors, Haar-random target, 2000 Adam steps;
+  serve            64 resident Clements / butterfly meshes (N in {16..512}), Poisson requests at 20k req/s for
+                   60 s, 80% forward / 20% gradient, p50/p99 latency;
+  lossy            the checkpointed adjoint of lossy generic MZIs on the N=256 mesh.
+
+The CPU leg (the ``cpu_*`` functions) is the only user of oracle/: the oracle's C++ restatement of the
+reference's c/dot.cpp is the timed CPU baseline, and the oracle (that port in complex128 and the numpy
+restatement of the reference's mesh code) checks every GPU result.  The GPU path never calls it.
+
+Under torchrun (N > 1) every rank runs an independent replica of the headline step on its own GPU (the path
+needs no collective); value = all ranks' MZI applications / max-over-ranks time; the other workloads run at
+N = 1 only.  ``--impl reference`` times the reference algorithm's CPU implementation (the oracle's C++ port of
+c/dot.cpp, first checked against the reference's own outputs stored in tests/golden/) on the full headline
+workload with all host threads, on rank 0 only; it imports neither torch nor this package.
 """
 from __future__ import annotations
 
@@ -24,6 +39,7 @@ import subprocess
 import sys
 import threading
 import time
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
@@ -31,7 +47,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N, B, SIGMA, SEED = 256, 4096, 0.02, 1002
-FLOP_FWD, FLOP_BWD = 32, 96           # reference gpu/test.py:208,220
+FLOPS = {"mzi": (32, 96), "sym": (32, 96), "orth": (8, 24)}   # per MZI-application, reference gpu/test.py:208,220
+FLOP_FWD, FLOP_BWD = FLOPS["mzi"]
+FP32_LANES_PER_SM = 128                                         # FP32 FMA lanes of one Blackwell SM
+TOL = 1e-5                                                      # relative Frobenius error bound vs complex128
 METRIC = "MZI-apps/s (fwd+bwd)"
 WORKLOAD = "clements_mzi_N256_L256_B4096_fwd+bwd"
 
@@ -43,35 +62,69 @@ def host_threads() -> int:
         return os.cpu_count() or 1
 
 
+# ---- geometry and seeded synthetic inputs (numpy only: the reference arm imports nothing else)
+def clements_layout(n: int):
+    """Clements rectangle: layer l holds (n - l%2)//2 MZIs starting at mode l%2 (reference clements.py:56-57)."""
+    return [(n - l % 2) // 2 for l in range(n)], [l % 2 for l in range(n)]
+
+
+def reck_layout(n: int):
+    """Reck triangle, 2n-3 layers (reference reck.py:47-48)."""
+    shifts = list(range(n - 2, 0, -1)) + list(range(0, n - 1))
+    return [(n - s) // 2 for s in shifts], shifts
+
+
+def fft_layout(n: int):
+    """log2(n)-layer butterfly: stride exponents 0..log2(n)-1."""
+    return list(range(int(round(np.log2(n)))))
+
+
+def active_mask(n: int, lens, shifts) -> np.ndarray:
+    m = np.zeros((len(lens), n // 2), dtype=bool)
+    for l, (ln, sh) in enumerate(zip(lens, shifts)):
+        m[l, sh // 2: sh // 2 + ln] = True
+    return m
+
+
+def unit_rows(rng, rows: int, n: int, real: bool = False) -> np.ndarray:
+    """(rows, n) vectors with iid N(0,1) entries (real and imaginary parts), each normalised to unit norm."""
+    x = rng.standard_normal((rows, n))
+    if not real:
+        x = x + 1j * rng.standard_normal((rows, n))
+    x = x / np.linalg.norm(x, axis=1, keepdims=True)
+    return x.astype(np.float32 if real else np.complex64)
+
+
 def make_problem():
-    """Seeded synthetic mesh and fields (numpy), independent of the oracle."""
-    from meshes_gb300 import geometry as gm
+    """The headline workload: lens, shifts, p, s (L, N/2, 2) float32, x, y_t (B, N) complex64, n_MZI."""
     rng = np.random.default_rng(SEED)
-    lens, shifts = gm.clements(N)
+    lens, shifts = clements_layout(N)
     L = len(lens)
-    mask = gm.active_mask_nn(N, lens, shifts)
+    mask = active_mask(N, lens, shifts)
     p = rng.uniform(0, 2 * np.pi, (L, N // 2, 2)).astype(np.float32)
     s = rng.normal(0, SIGMA, (L, N // 2, 2)).astype(np.float32)
     p[~mask] = 0
     s[~mask] = 0
-
-    def unit(rows):
-        x = rng.standard_normal((rows, N)) + 1j * rng.standard_normal((rows, N))
-        return (x / np.linalg.norm(x, axis=1, keepdims=True)).astype(np.complex64)
-
-    x = unit(B)
-    yt = unit(B)
+    x = unit_rows(rng, B, N)
+    yt = unit_rows(rng, B, N)
     return lens, shifts, p, s, x, yt, int(mask.sum())
 
 
+def step_config():
+    """config of the headline line (the same dict in both arms)."""
+    return {"workload": WORKLOAD, "N": N, "L": N, "B": B, "n_mzi": N * (N - 1) // 2, "splitter_sigma": SIGMA,
+            "l2": "GPU arm: flushed between timed steps (256 MB write)"}
+
+
+# ---- clocks
 class ClockSampler:
-    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    """nvidia-smi sampling of SM clocks and throttle reasons during a timed region."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index: int):
+    def __init__(self, index: str):
         self.index = index
         self.proc = None
         self.lines = []
@@ -129,44 +182,331 @@ def gpu_id(torch, dev) -> str:
         return str(dev.index or 0)
 
 
-def cpu_baseline(problem, seconds=10.0, with_c128=True):
-    """Reference algorithm on the host cores: the oracle's C++ port of c/dot.cpp (complex64, OpenMP),
-    forward (mode 0) + back-propagation (mode 2) on a bounded sample of the batch."""
+def max_sm_clock_mhz(sel: str) -> float | None:
+    try:
+        out = subprocess.run(["nvidia-smi", "-i", sel, "--query-gpu=clocks.max.sm", "--format=csv,noheader,nounits"],
+                             capture_output=True, text=True, timeout=20).stdout.strip().splitlines()
+        return float(out[0])
+    except Exception:
+        return None
+
+
+# =====================================================================================================
+# CPU leg: the oracle as the timed CPU baseline and as the checker of the GPU results
+# =====================================================================================================
+def _cpu_modules():
     from oracle import meshes_oracle as O
     from oracle import port as P
+    return O, P
+
+
+def cpu_oracle_mesh(n, lens, shifts, p, s, crossing="mzi", strides=None):
+    O, _ = _cpu_modules()
+    return O.OracleMesh(N=n, L=len(strides) if strides is not None else len(lens), crossing=crossing,
+                        lens=None if strides is not None else list(lens),
+                        shifts=None if strides is not None else list(shifts),
+                        strides=None if strides is None else list(strides), p=np.asarray(p, np.float64),
+                        s=None if s is None else np.asarray(s, np.float64))
+
+
+def cpu_rel_err(a, b) -> float:
+    a = np.asarray(a)
+    b = np.asarray(b)
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))
+
+
+def cpu_pin_port():
+    """The port checked against the reference's own outputs (tests/golden/, made by running the reference's
+    StructuredMeshNetwork.dot / dot_vjp in complex128 and its complex64 meshdot_helper32) before it is timed."""
+    O, P = _cpu_modules()
+    fns = P.port_lib()
+    worst64, worst32, names = 0.0, 0.0, []
+    for name in ("clements_mzi_N64_split.npz", "clements_mzi_N16.npz", "reck_mzi_N10_split.npz"):
+        z = np.load(os.path.join(ROOT, "tests", "golden", name))
+        om = cpu_oracle_mesh(int(z["N"]), z["lens"].tolist(), z["shifts"].tolist(), z["p"],
+                             z["s"] if "s" in z.files else None, str(z["crossing"]))
+        y = P.forward(fns, om, z["x"], dtype=np.complex128)
+        G, gin = P.vjp(fns, om, z["y"], z["g"], dtype=np.complex128)
+        worst64 = max(worst64, cpu_rel_err(y, z["y"]), cpu_rel_err(O.contract_dp(om, G), z["dJdp"]),
+                      cpu_rel_err(gin, z["g_in"]))
+        worst32 = max(worst32, cpu_rel_err(P.forward(fns, om, z["x"], dtype=np.complex64), z["y_c64"]))
+        names.append(name)
+    return {"pinned": bool(worst64 < 1e-12 and worst32 < 1e-6), "max_rel_err_complex128": worst64,
+            "max_rel_err_complex64": worst32, "fixtures": names}
+
+
+def cpu_step_runner(problem, dtype=np.complex64):
+    """The headline step on the host through the port, with the mesh's packed T and the fields laid out once
+    (the reference's meshdot_helper_c contract, mesh.py:97-113): run(threads) does forward (mode 0), forms
+    dJ/dy* = 2 (y - y_t) and back-propagates (mode 2); returns (y, g_in, dJ/dT) in the port's layout."""
+    O, P = _cpu_modules()
     lens, shifts, p, s, x, yt, n_mzi = problem
-    om = O.OracleMesh(N=N, L=len(lens), crossing="mzi", lens=lens, shifts=shifts, p=p, s=s)
+    om = cpu_oracle_mesh(N, lens, shifts, p, s)
+    fns = P.port_lib()
+    T, inds = P.packed_T(om, dtype)
+    rdt = np.float32 if dtype == np.complex64 else np.float64
+    xv = np.ascontiguousarray(x.T.astype(dtype))
+    ytv = np.ascontiguousarray(yt.T.astype(dtype))
+    e = np.empty(0, dtype)
+    no_perm = np.empty((0, 0), np.int32)
+
+    def run(threads):
+        v = xv.copy()
+        P.call(fns, T, e.reshape(0, 0, 0), np.empty(0, rdt), np.empty(0, rdt), v, e.reshape(0, 0), inds, lens, shifts,
+               no_perm, -1, 0, threads)
+        dv = 2 * (v - ytv)
+        dT = np.zeros_like(T)
+        P.call(fns, T, dT, np.empty(0, rdt), np.empty(0, rdt), v, dv, inds, lens, shifts, no_perm, -1, 2, threads)
+        return v, dv, dT
+    return run
+
+
+def cpu_time_step(run, reps: int, threads: int) -> list:
+    """Seconds per step of a cpu_step_runner."""
+    out = []
+    for _ in range(reps):
+        a = time.perf_counter()
+        run(threads)
+        out.append(time.perf_counter() - a)
+    return out
+
+
+def cpu_baseline_step(problem, seconds=6.0):
+    """The headline step on the host cores: the port in complex64 (and complex128), full batch."""
+    threads = host_threads()
+    n_mzi = problem[6]
+    run = cpu_step_runner(problem)
+    cpu_time_step(run, 1, threads)                            # warm-up
+    times, t0 = [], time.perf_counter()
+    while time.perf_counter() - t0 < seconds or len(times) < 2:
+        times += cpu_time_step(run, 1, threads)
+    t128 = cpu_time_step(cpu_step_runner(problem, np.complex128), 2, threads)
+    t = statistics.median(times)
+    return {"value": n_mzi * B / t, "unit": "MZI-apps/s", "cores": threads, "kind": "port",
+            "sample": "the full batch (%d vectors) per step: fwd (mode 0) + 2(y - y_t) + bwd (mode 2), complex64, "
+                      "median of %d steps" % (B, len(times)),
+            "value_complex128": n_mzi * B / statistics.median(t128), **cpu_pin_port()}
+
+
+def cpu_check_step(problem, y, gin, dp, dp_sample, n_sample, seed=2002):
+    """Errors of one GPU step against the complex128 oracle on the same inputs: y, g_in and dJ/dp of the full
+    batch (exact adjoint), and dJ/dp of the first n_sample vectors against complex128 central differences
+    (h = 1e-6) on 64 random MZIs (theta and phi)."""
+    O, P = _cpu_modules()
+    lens, shifts, p, s, x, yt, n_mzi = problem
+    threads = host_threads()
+    om = cpu_oracle_mesh(N, lens, shifts, p, s)
+    fns = P.port_lib()
+    y128 = P.forward(fns, om, x, threads=threads, dtype=np.complex128)
+    G, gin128 = P.vjp(fns, om, y128, 2 * (y128 - yt), threads=threads, dtype=np.complex128)
+    dp128 = O.contract_dp(om, G)
+    # central differences: perturb one MZI's packed T at a time (complex128 port, one thread per evaluation)
+    T, inds = P.packed_T(om, np.complex128)
+    rng = np.random.default_rng(seed)
+    act = np.argwhere(om.active_mask())
+    pick = act[rng.choice(len(act), 64, replace=False)]
+    xs = np.ascontiguousarray(x[:n_sample].T.astype(np.complex128))
+    ts = yt[:n_sample].astype(np.complex128)
+    h = 1e-6
+    e0 = np.empty(0, np.complex128)
+
+    def loss(l, q, k, sgn):
+        pp = np.array(p[l, q], np.float64)
+        pp[k] += sgn * h
+        Tk = T.copy()
+        Tk[:, :, inds[l] + q - shifts[l] // 2] = O.T_mzi(pp[None, :], np.asarray(s[l, q], np.float64)[None, :])[:, :, 0]
+        v = xs.copy()
+        P.call(fns, Tk, e0.reshape(0, 0, 0), np.empty(0), np.empty(0), v, e0.reshape(0, 0), inds, lens, shifts,
+               np.empty((0, 0), np.int32), -1, 0, 1)
+        return float(np.sum(np.abs(v.T - ts) ** 2))
+
+    jobs = [(int(l), int(q), k, sg) for l, q in pick for k in (0, 1) for sg in (1, -1)]
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        vals = list(ex.map(lambda a: loss(*a), jobs))
+    fd = np.array([(vals[4 * i + 2 * k] - vals[4 * i + 2 * k + 1]) / (2 * h) for i in range(64) for k in (0, 1)])
+    got = np.array([dp_sample[l, q, k] for l, q in pick for k in (0, 1)])
+    errs = {"y": cpu_rel_err(y, y128), "g_in": cpu_rel_err(gin, gin128), "dJdp": cpu_rel_err(dp, dp128),
+            "dJdp_central_differences_64_mzis": cpu_rel_err(got, fd)}
+    errs["max"] = max(errs.values())
+    errs.update(tolerance=TOL, ok=bool(errs["max"] <= TOL),
+                against="complex128 oracle (C++ port of c/dot.cpp, modes 0 and 2) on the same inputs; central "
+                        "differences on the first %d vectors" % n_sample)
+    return errs
+
+
+def cpu_forward_check(n, lens, shifts, p, s, x, y_gpu, crossing="mzi", threads=None):
+    """rel err of y_gpu against the complex128 port forward of the same mesh and inputs."""
+    _, P = _cpu_modules()
+    om = cpu_oracle_mesh(n, lens, shifts, p, s, crossing)
+    y128 = P.forward(P.port_lib(), om, x, threads=threads or host_threads(), dtype=np.complex128)
+    return cpu_rel_err(y_gpu, y128.real if crossing == "orth" else y128)
+
+
+def cpu_baseline_forward(n, lens, shifts, p, s, x, seconds=2.0):
+    """Forward propagation (mode 0) of the whole batch through the port in complex64 on all host cores (packed
+    T and the field layout prepared once, as for the reference's meshdot_helper_c)."""
+    _, P = _cpu_modules()
+    threads = host_threads()
+    om = cpu_oracle_mesh(n, lens, shifts, p, s)
+    fns = P.port_lib()
+    T, inds = P.packed_T(om, np.complex64)
+    xv = np.ascontiguousarray(x.T.astype(np.complex64))
+    e = np.empty(0, np.complex64)
+    no_perm = np.empty((0, 0), np.int32)
+
+    def run():
+        v = xv.copy()
+        P.call(fns, T, e.reshape(0, 0, 0), np.empty(0, np.float32), np.empty(0, np.float32), v, e.reshape(0, 0), inds,
+               lens, shifts, no_perm, -1, 0, threads)
+
+    run()
+    times, t0 = [], time.perf_counter()
+    while time.perf_counter() - t0 < seconds or len(times) < 3:
+        a = time.perf_counter()
+        run()
+        times.append(time.perf_counter() - a)
+    n_mzi = int(active_mask(n, lens, shifts).sum())
+    return {"value": n_mzi * x.shape[0] / statistics.median(times), "unit": "MZI-apps/s", "cores": threads,
+            "kind": "port", "sample": "the full batch, forward (mode 0), complex64, median of %d" % len(times)}
+
+
+def cpu_check_batched(prob, outs):
+    """Per-mesh errors of the batched forward + backward against the complex128 port: y = U x, g_x = U^H g_y,
+    dJ/dp; the maximum over the meshes of each."""
+    O, P = _cpu_modules()
     fns = P.port_lib()
     threads = host_threads()
-    bs = max(8, min(B, 16 * threads))
-    xs, ts = x[:bs], yt[:bs]
-    t0 = time.perf_counter()
-    reps, work = 0, 0.0
-    while True:
-        a = time.perf_counter()
-        y = P.forward(fns, om, xs, threads=threads, dtype=np.complex64)
-        P.vjp(fns, om, y, 2 * (y - ts), threads=threads, dtype=np.complex64)
-        work += time.perf_counter() - a
-        reps += 1
-        if time.perf_counter() - t0 > seconds and reps >= 2:
-            break
-    rate = n_mzi * bs * reps / work
-    out = {"value": rate, "unit": "MZI-apps/s", "cores": threads, "kind": "port",
-           "sample": "%d of the %d vectors, fwd (mode 0) + bwd (mode 2), complex64, %d repeats, %.1f s"
-                     % (bs, B, reps, work)}
-    if not with_c128:
-        return out
-    # the same in complex128 (the reference's own precision for dot / dot_vjp), a shorter sample
-    a = time.perf_counter()
-    reps128 = 0
-    while True:
-        y = P.forward(fns, om, xs, threads=threads, dtype=np.complex128)
-        P.vjp(fns, om, y, 2 * (y - ts), threads=threads, dtype=np.complex128)
-        reps128 += 1
-        if time.perf_counter() - a > seconds / 4 and reps128 >= 2:
-            break
-    out["value_complex128"] = n_mzi * bs * reps128 / (time.perf_counter() - a)
-    return out
+    worst = {"y": 0.0, "g_x": 0.0, "dJdp": 0.0}
+    for d, (y, gy, gx, dp) in zip(prob, outs):
+        om = cpu_oracle_mesh(d["N"], d["lens"], d["shifts"], d["p"], d["s"], d["cr"])
+        y128 = P.forward(fns, om, d["x"], threads=threads, dtype=np.complex128)
+        G, gx128 = P.vjp(fns, om, y128, gy, threads=threads, dtype=np.complex128)
+        dp128 = O.contract_dp(om, G)
+        if d["cr"] == "orth":
+            y128, gx128 = y128.real, gx128.real
+        worst["y"] = max(worst["y"], cpu_rel_err(y, y128))
+        worst["g_x"] = max(worst["g_x"], cpu_rel_err(gx, gx128))
+        worst["dJdp"] = max(worst["dJdp"], cpu_rel_err(dp, dp128))
+    worst["max"] = max(worst.values())
+    worst.update(tolerance=TOL, ok=bool(worst["max"] <= TOL), meshes=len(prob),
+                 against="complex128 port of c/dot.cpp per mesh, every vector; maximum over the meshes")
+    return worst
+
+
+def cpu_unitary_fit_check(lens, shifts, p, s, U_gpu, Ut):
+    """Fidelity |tr(U^H U_t)|^2 / N^2 of the fitted phases re-evaluated in complex128, and the error of the
+    GPU's U against that evaluation."""
+    _, P = _cpu_modules()
+    n = len(lens)
+    om = cpu_oracle_mesh(n, lens, shifts, p, s)
+    U128 = P.forward(P.port_lib(), om, np.eye(n), threads=host_threads(), dtype=np.complex128).T
+    fid = float(np.abs(np.trace(U128.conj().T @ Ut.astype(np.complex128))) ** 2 / n ** 2)
+    return fid, cpu_rel_err(U_gpu, U128)
+
+
+def cpu_check_served(meshes_h, checked):
+    """Sampled served requests against the oracle in complex128 (the port for Clements meshes, the numpy
+    restatement for butterflies): y; for gradient requests also dJ/dp and g_x."""
+    O, P = _cpu_modules()
+    fns = P.port_lib()
+    threads = host_threads()
+    worst = {"y": 0.0, "dJdp": 0.0, "g_x": 0.0}
+    for i, x, gy, res in checked:
+        d = meshes_h[i]
+        om = cpu_oracle_mesh(d["N"], d["lens"], d["shifts"], d["p"], d["s"], "mzi", d["strides"])
+        if d["strides"] is None:
+            y128 = P.forward(fns, om, x, threads=threads, dtype=np.complex128)
+        else:
+            y128 = O.propagate(om, x)
+        if gy is None:
+            worst["y"] = max(worst["y"], cpu_rel_err(res, y128))
+            continue
+        y, dp, gx = res
+        worst["y"] = max(worst["y"], cpu_rel_err(y, y128))
+        if d["strides"] is None:
+            G, gx128 = P.vjp(fns, om, y128, gy, threads=threads, dtype=np.complex128)
+        else:
+            G, _, gx128 = O.vjp_unitary(om, y128, gy)
+        worst["dJdp"] = max(worst["dJdp"], cpu_rel_err(dp, O.contract_dp(om, G)))
+        worst["g_x"] = max(worst["g_x"], cpu_rel_err(gx, gx128))
+    worst["max"] = max(worst.values())
+    worst.update(tolerance=TOL, ok=bool(worst["max"] <= TOL), requests_checked=len(checked),
+                 against="complex128 oracle per sampled request (seeded sample of forward and gradient requests)")
+    return worst
+
+
+def cpu_lossy_check(lens, shifts, p, s14, x, y_gpu):
+    """Lossy forward: y of a sample of vectors against the oracle's lossy generic MZI mesh in complex128."""
+    O, _ = _cpu_modules()
+    om = cpu_oracle_mesh(N, lens, shifts, p, s14, "mzi_generic")
+    return cpu_rel_err(y_gpu, O.propagate(om, x))
+
+
+# =====================================================================================================
+# reference arm: the reference algorithm's CPU implementation on the host cores
+# =====================================================================================================
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    problem = make_problem()
+    n_mzi = problem[6]
+    threads = host_threads()
+    pin = cpu_pin_port()
+    run = cpu_step_runner(problem)
+    cpu_time_step(run, max(1, args.warmup), threads)
+    times = cpu_time_step(run, max(1, args.steps), threads)
+    t = statistics.median(times)
+    value = n_mzi * B / t
+    cb = {"value": value, "unit": "MZI-apps/s", "cores": threads, "kind": "port",
+          "sample": "the full batch (%d vectors) per step: fwd (mode 0) + 2(y - y_t) + bwd (mode 2), complex64, "
+                    "median of %d steps" % (B, len(times)), **pin}
+    line = {"metric": METRIC, "value": value, "unit": "MZI-apps/s", "n_gpus": args.gpus, "steps": len(times),
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded normal fields, uniform phases)",
+            "config": step_config(), "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": "MZI-apps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# =====================================================================================================
+# GPU arm
+# =====================================================================================================
+def fp32_peak(torch, lib, _lib, dev, stream, st, sel):
+    """FP32 FMA peak of this GPU: the library's scalar and packed FMA probes, each run for >= 50 ms, and the
+    architectural rate SMs x 128 lanes x 2 FLOP x maximum SM clock."""
+    props = torch.cuda.get_device_properties(dev)
+    sms = props.multi_processor_count
+    blocks, threads = sms * 4, 256
+    sink = torch.empty(blocks * threads, device=dev)
+
+    def run(fn, iters, per_iter):
+        _lib.check(fn(sink.data_ptr(), blocks, threads, iters, st), "fma probe")
+        torch.cuda.synchronize(dev)
+        best = None
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _lib.check(fn(sink.data_ptr(), blocks, threads, iters, st), "fma probe")
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            t = e0.elapsed_time(e1) * 1e-3
+            best = t if best is None else min(best, t)
+        return blocks * threads * iters * per_iter / best, best
+
+    # about 4 TFLOP per run: >= 50 ms at the expected rate
+    r1, t1 = run(lib.mg_fma_probe, 200000, 64 * 2)
+    r2, t2 = run(lib.mg_fma2_probe, 100000, 128 * 2)
+    mhz = max_sm_clock_mhz(sel) or 2070.0
+    spec = sms * FP32_LANES_PER_SM * 2 * mhz * 1e6
+    return {"spec": spec, "probe": max(r1, r2), "sms": sms, "sm_max_mhz": mhz,
+            "probe_ms": [t1 * 1e3, t2 * 1e3]}
+
+
+def roofline_fp32(flops_per_s, peak, kernel):
+    return {"kernel": kernel, "bound": "fp32", "achieved": flops_per_s / 1e12, "peak": peak["spec"] / 1e12,
+            "unit": "TFLOP/s", "frac": flops_per_s / peak["spec"], "frac_of_probe": flops_per_s / peak["probe"],
+            "peak_source": "SMs x 128 FP32 lanes x 2 x max SM clock (frac_of_probe: the measured FMA probe)"}
 
 
 def traffic_from_profiles(name: str):
@@ -181,31 +521,8 @@ def traffic_from_profiles(name: str):
     return None
 
 
-def run_reference(args, rank):
-    if rank != 0:
-        return
-    problem = make_problem()
-    n_mzi = problem[6]
-    # about a minute of CPU work in total, whatever K and W are (each step is a bounded sample)
-    per_step = max(0.05, 60.0 / max(args.steps + args.warmup, 1))
-    for _ in range(args.warmup):
-        cpu_baseline(problem, seconds=min(per_step, 0.5), with_c128=False)
-    vals = []
-    for _ in range(args.steps):
-        vals.append(cpu_baseline(problem, seconds=per_step, with_c128=False))
-    value = statistics.median(v["value"] for v in vals)
-    cb = dict(vals[0])
-    cb["value"] = value
-    line = {"metric": METRIC, "value": value, "unit": "MZI-apps/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * n_mzi * B / value, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "N": N, "L": N, "B": B, "n_mzi": n_mzi, "splitter_sigma": SIGMA},
-            "impl": "reference", "cpu_baseline": cb,
-            "e2e": {"value": value, "unit": "MZI-apps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
-
-
-def run_ours(args, rank, world, local_rank):
+def run_step(args, rank, world, local_rank):
+    """The headline step (every rank: one replica); returns the JSON line on rank 0."""
     import torch
     import torch.distributed as dist
 
@@ -215,8 +532,10 @@ def run_ours(args, rank, world, local_rank):
     dev = torch.device("cuda", local_rank)
     stream = torch.cuda.current_stream(dev)
     st = stream.cuda_stream
+    sel = gpu_id(torch, dev)
 
-    lens, shifts, p, s, x_h, yt_h, n_mzi = make_problem()
+    problem = make_problem()
+    lens, shifts, p, s, x_h, yt_h, n_mzi = problem
     L = len(lens)
     lens_d = torch.tensor(lens, dtype=torch.int32, device=dev)
     shifts_d = torch.tensor(shifts, dtype=torch.int32, device=dev)
@@ -238,17 +557,19 @@ def run_ours(args, rank, world, local_rank):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # > 129 MB L2
     launches_per_step = 4          # coefficient tiles, forward, back-propagation with fused L2, gradient reduce
 
-    def step(xx, yy_t, dp_out=None):
+    def step_on(xx, yy_t, dp_out, nb, ws, wsb, y_out, g_out):
         """One training step through the programmed-mesh C ABI: the back-propagation tiles are built once
         and serve the forward pass too; dJ/dy* = 2 (y - y_t) is formed inside the backward kernel."""
-        dp_out = dp if dp_out is None else dp_out
         _lib.check(lib.mg_build_tiles(2, N, L, 0, lens_d.data_ptr(), shifts_d.data_ptr(), None, 0, p_d.data_ptr(), ldp,
-                                      s_d.data_ptr(), lds, None, None, None, B, None, ws_b.data_ptr(), wsb_b, st),
+                                      s_d.data_ptr(), lds, None, None, None, nb, None, ws.data_ptr(), wsb, st),
                    "mg_build_tiles")
-        _lib.check(lib.mg_propagate(3, N, L, B, 0, 0, xx.data_ptr(), None, y.data_ptr(), None, N, None, 0, 0, None,
-                                    ws_b.data_ptr(), wsb_b, st), "mg_propagate")
-        _lib.check(lib.mg_propagate_l2(N, L, B, 0, 0, y.data_ptr(), yy_t.data_ptr(), None, gin.data_ptr(), N,
-                                       dp_out.data_ptr(), ldp, 0, None, ws_b.data_ptr(), wsb_b, st), "mg_propagate_l2")
+        _lib.check(lib.mg_propagate(3, N, L, nb, 0, 0, xx.data_ptr(), None, y_out.data_ptr(), None, N, None, 0, 0, None,
+                                    ws.data_ptr(), wsb, st), "mg_propagate")
+        _lib.check(lib.mg_propagate_l2(N, L, nb, 0, 0, y_out.data_ptr(), yy_t.data_ptr(), None, g_out.data_ptr(), N,
+                                       dp_out.data_ptr(), ldp, 0, None, ws.data_ptr(), wsb, st), "mg_propagate_l2")
+
+    def step(xx, yy_t, dp_out=None):
+        step_on(xx, yy_t, dp if dp_out is None else dp_out, B, ws_b, wsb_b, y, gin)
 
     def step_dropin(xx, yy_t):
         """The same step through the reference-shaped entry points (mg_fwdprop, mg_backdiff)."""
@@ -294,20 +615,22 @@ def run_ours(args, rank, world, local_rank):
                        "mg_propagate")
         torch.cuda.synchronize(dev)
         print(json.dumps({"profile_bwd_config": args.bwd_config, "status": lib.mg_read_status(ws_c.data_ptr(), 0, st)}))
-        return
+        return None
     if args.profile:
         # one warm-up step and one profiled step, no timing (for ncu captures: -s 2 -c 2 on prop_kernel)
         step(x, yt)
         step(x, yt)
         torch.cuda.synchronize(dev)
         print(json.dumps({"profile_steps": 2, "status": lib.mg_read_status(ws_b.data_ptr(), 0, st)}))
-        return
+        return None
+
+    peak = fp32_peak(torch, lib, _lib, dev, stream, st, sel)
 
     # ---- device-resident step (value)
     for _ in range(args.warmup):
         step(x, yt)
     barrier()
-    with ClockSampler(gpu_id(torch, dev)) as cs:
+    with ClockSampler(sel) as cs:
         times = timed(lambda: step(x, yt), args.steps)
         barrier()
     t_step = sum(times) / len(times)
@@ -318,7 +641,7 @@ def run_ours(args, rank, world, local_rank):
     if status != 0:
         raise RuntimeError("kernel status %d" % status)
 
-    # ---- end to end through the C ABI with host buffers: H2D x, y_t; D2H dJ/dp and the loss
+    # ---- end to end through the C ABI with host buffers: H2D x, y_t; D2H dJ/dp
     x_pin = torch.from_numpy(x_h).pin_memory()
     yt_pin = torch.from_numpy(yt_h).pin_memory()
     dp_pin = torch.empty(dp.numel(), dtype=torch.float32).pin_memory()
@@ -384,7 +707,7 @@ def run_ours(args, rank, world, local_rank):
     barrier()
     t_e2e = e0.elapsed_time(e1) * 1e-3 / args.steps
 
-    # ---- roofline of the dominant kernel: the back-propagation kernel alone (tiles built once)
+    # ---- kernels alone: the dominant back-propagation kernel (tiles built once), forward, fwddiff
     def bwd_kernel():
         _lib.check(lib.mg_propagate(2, N, L, B, 0, 0, y.data_ptr(), g.data_ptr(), None, gin.data_ptr(), N, None, 0, 0,
                                     None, ws_b.data_ptr(), wsb_b, st), "mg_propagate")
@@ -396,7 +719,6 @@ def run_ours(args, rank, world, local_rank):
     bwd_kernel()
     t_bwd = statistics.median(timed(bwd_kernel, max(5, args.steps)))
     t_fwd = statistics.median(timed(fwd_kernel, max(5, args.steps)))
-    # forward-mode derivative (the reference's fwddiff: y and dy along a direction of all phases)
     wsb_d = lib.mg_workspace_bytes(1, N, L, B, 0, 0, None)
     ws_d = torch.empty(wsb_d, dtype=torch.uint8, device=dev)
     _lib.check(lib.mg_workspace_init(ws_d.data_ptr(), wsb_d, st), "mg_workspace_init")
@@ -411,28 +733,31 @@ def run_ours(args, rank, world, local_rank):
                                     None, ws_d.data_ptr(), wsb_d, st), "mg_propagate")
 
     t_fwddiff = statistics.median(timed(fwddiff_kernel, max(5, args.steps // 4)))
-    # FP32 FMA peak of this device (the measured-peaks file has HBM and bf16 only)
-    props = torch.cuda.get_device_properties(dev)
-    sink = torch.empty(props.multi_processor_count * 4 * 256, device=dev)
-    iters = 4000
 
-    def probe():
-        _lib.check(lib.mg_fma_probe(sink.data_ptr(), props.multi_processor_count * 4, 256, iters, st), "fma_probe")
-
-    probe()
-    t_probe = min(timed(probe, 3))
-    peak = props.multi_processor_count * 4 * 256 * iters * 64 * 2 / t_probe
+    # ---- outputs of one more step for the error check, and the step on the first 64 vectors (for the
+    # central-difference check of dJ/dp)
+    step(x, yt)
+    y_h, gin_h = y.cpu().numpy(), gin.cpu().numpy()
+    dp_h = dp.cpu().numpy().reshape(L, N // 2, 2)
+    n_s = 64
+    wsb_s = lib.mg_workspace_bytes(2, N, L, n_s, 0, 0, None)
+    ws_s = torch.empty(wsb_s, dtype=torch.uint8, device=dev)
+    _lib.check(lib.mg_workspace_init(ws_s.data_ptr(), wsb_s, st), "mg_workspace_init")
+    y_s, g_s, dp_s = torch.empty_like(x[:n_s]), torch.empty_like(x[:n_s]), torch.empty_like(dp)
+    step_on(x[:n_s], yt[:n_s], dp_s, n_s, ws_s, wsb_s, y_s, g_s)
+    dp_s_h = dp_s.cpu().numpy().reshape(L, N // 2, 2)
+    status = max(status, lib.mg_read_status(ws_b.data_ptr(), 0, st), lib.mg_read_status(ws_s.data_ptr(), 0, st),
+                 lib.mg_read_status(ws_d.data_ptr(), 0, st))
 
     # ---- reduce over ranks (replicas: the job ends with its slowest rank)
     from meshes_gb300.replicas import max_over_ranks
     t_max = max_over_ranks(t_step, device=dev)
     t_e2e = max_over_ranks(t_e2e, device=dev)
     if rank != 0:
-        return
+        return None
     units = n_mzi * B * world
     value = units / t_max
     bwd_flops = n_mzi * B * FLOP_BWD
-    achieved = bwd_flops / t_bwd
     traffic = traffic_from_profiles("prop_bwd_clements_N256_L256_B4096.md")
     bwd_bytes = B * N * 3 * 8 + n_mzi * 4 * (2 + 2) + n_mzi * 4 * 2
     try:
@@ -440,24 +765,28 @@ def run_ours(args, rank, world, local_rank):
             hbm_peak, hbm_src = float(json.load(f)["hbm_gbs"]), "measured (copy bandwidth)"
     except (OSError, KeyError, ValueError):
         hbm_peak, hbm_src = 6800.0, "fallback"
+    roof = roofline_fp32(bwd_flops / t_bwd, peak, "prop_kernel<BWD> (back-propagation)")
+    roof.update(traffic=traffic, algorithmic_flops_per_launch=bwd_flops)
+    step_flops = value / world * (FLOP_FWD + FLOP_BWD)
     line = {
         "metric": METRIC, "value": value, "unit": "MZI-apps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded normal fields, uniform phases)",
-        "config": {"workload": WORKLOAD, "N": N, "L": L, "B": B, "n_mzi": n_mzi, "splitter_sigma": SIGMA,
-                   "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas" if world > 1 else "1 GPU"},
-        "pct_fp32_peak": 100 * value / world * (FLOP_FWD + FLOP_BWD) / peak,
-        "fp32_peak_tflops": peak / 1e12,
+        "config": step_config(),
+        "parallelism": "replicas" if world > 1 else "1 GPU",
+        "rel_err": cpu_check_step(problem, y_h, gin_h, dp_h, dp_s_h, n_s),
+        "pct_fp32_peak": 100 * step_flops / peak["spec"],
+        "pct_fp32_peak_probe": 100 * step_flops / peak["probe"],
+        "fp32_peak": {"spec_tflops": peak["spec"] / 1e12, "probe_tflops": peak["probe"] / 1e12, "sms": peak["sms"],
+                      "sm_max_mhz": peak["sm_max_mhz"], "probe_ms": peak["probe_ms"],
+                      "flop_per_mzi_app": FLOP_FWD + FLOP_BWD},
         "step": "programmed mesh: mg_build_tiles(bwd) + mg_propagate(fwd from bwd tiles) + mg_propagate_l2",
         "drop_in_step": {"ms": t_dropin * 1e3, "mzi_per_s": units / world / t_dropin,
                          "path": "mg_fwdprop + 2(y - y_t) + mg_backdiff (reference-shaped entry points)"},
         "kernels": {"fwd_prop_ms": t_fwd * 1e3, "bwd_prop_ms": t_bwd * 1e3, "fwddiff_prop_ms": t_fwddiff * 1e3,
                     "fwddiff_mzi_per_s": n_mzi * B / t_fwddiff,
                     "fwd_mzi_per_s": n_mzi * B / t_fwd, "bwd_mzi_per_s": n_mzi * B / t_bwd},
-        "roofline": {"kernel": "prop_kernel<BWD> (back-propagation)", "bound": "fp32", "achieved": achieved / 1e12,
-                     "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / peak,
-                     "peak_source": "measured: FP32 FMA probe on this GPU (no FP32 entry in the measured-peaks file)",
-                     "traffic": traffic, "algorithmic_flops_per_launch": bwd_flops},
+        "roofline": roof,
         # the same kernel against the HBM roofline (algorithmic bytes: read y and g, write g_in, the
         # parameters and dJ/dp), showing how far it is from being memory-bound
         "roofline_hbm": {"kernel": "prop_kernel<BWD> (back-propagation)", "bound": "hbm",
@@ -469,213 +798,100 @@ def run_ours(args, rank, world, local_rank):
                 "serialized_value": units / t_e2e_serial},
         "gpu_launches": launches_per_step * args.steps,
         "clocks": cs.summary(),
+        "status": status,
     }
-    line["cpu_baseline"] = cpu_baseline((lens, shifts, p, s, x_h, yt_h, n_mzi), seconds=10.0)
-    print(json.dumps(line))
+    line["cpu_baseline"] = cpu_baseline_step(problem)
+    line["_peak"] = peak
+    return line
 
 
+# ---- the other workloads (N = 1)
 def make_batched_problem(seed=1003, n_meshes=512):
     """512 meshes drawn 1:1:1 from Clements-mzi, Reck-mzi (native 2N-3 layers) and Clements-orth,
     N uniform in {8, ..., 256}, batch uniform in [1, 2048], phases U[0, 2pi), splitters N(0, 0.01)."""
-    from meshes_gb300 import geometry as gm
     rng = np.random.default_rng(seed)
     out = []
     for i in range(n_meshes):
         kind = ("clements-mzi", "reck-mzi", "clements-orth")[i % 3]
-        N = int(rng.choice([8, 16, 32, 64, 128, 256]))
-        B = int(rng.integers(1, 2049))
-        lens, shifts = gm.reck(N) if kind.startswith("reck") else gm.clements(N)
+        n = int(rng.choice([8, 16, 32, 64, 128, 256]))
+        nb = int(rng.integers(1, 2049))
+        lens, shifts = reck_layout(n) if kind.startswith("reck") else clements_layout(n)
         L = len(lens)
-        mask = gm.active_mask_nn(N, lens, shifts)
+        mask = active_mask(n, lens, shifts)
         cr = "orth" if kind.endswith("orth") else "mzi"
         n_p = 1 if cr == "orth" else 2
-        p = rng.uniform(0, 2 * np.pi, (L, N // 2, n_p)).astype(np.float32)
+        p = rng.uniform(0, 2 * np.pi, (L, n // 2, n_p)).astype(np.float32)
         p[~mask] = 0
         s = None
         if cr == "mzi":
-            s = rng.normal(0, 0.01, (L, N // 2, 2)).astype(np.float32)
+            s = rng.normal(0, 0.01, (L, n // 2, 2)).astype(np.float32)
             s[~mask] = 0
-        x = rng.standard_normal((B, N)) + (0 if cr == "orth" else 1j * rng.standard_normal((B, N)))
-        x = (x / np.linalg.norm(x, axis=1, keepdims=True)).astype(np.float32 if cr == "orth" else np.complex64)
-        out.append(dict(kind=kind, N=N, B=B, L=L, lens=lens, shifts=shifts, cr=cr, p=p, s=s, x=x,
+        x = unit_rows(rng, nb, n, real=cr == "orth")
+        out.append(dict(kind=kind, N=n, B=nb, L=L, lens=lens, shifts=shifts, cr=cr, p=p, s=s, x=x,
                         n_mzi=int(mask.sum())))
     return out
 
 
-def run_c1(args):
-    """Plain forward propagation, Clements mzi N=64 L=64 (2016 MZIs), ideal splitters, B=1024 unit-norm
-    complex64 columns, through the reference-shaped entry point mg_fwdprop; with the unitarity error
-    ||U U^H - I||_F of the programmed mesh."""
-    import torch
-    from meshes_gb300 import MeshNetworkGPU
-    from meshes_gb300 import geometry as gm
-    dev = torch.device("cuda", 0)
-    torch.cuda.set_device(dev)
-    rng = np.random.default_rng(1000)
-    Nc, Bc = 64, 1024
-    lens, shifts = gm.clements(Nc)
-    mask = gm.active_mask_nn(Nc, lens, shifts)
-    p = rng.uniform(0, 2 * np.pi, (len(lens), Nc // 2, 2)).astype(np.float32)
-    p[~mask] = 0
-    m = MeshNetworkGPU(Nc, len(lens), lens, shifts, p.reshape(-1), None, "mzi", is_phase=False, device=dev)
-    x = rng.standard_normal((Bc, Nc)) + 1j * rng.standard_normal((Bc, Nc))
-    x = torch.from_numpy((x / np.linalg.norm(x, axis=1, keepdims=True)).astype(np.complex64)).to(dev).t()
-    out = torch.empty_like(x)
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    for _ in range(max(3, args.warmup)):
-        m.dot(x, out=out)
+def event_ms(torch, fn, k, warm=3, flush=None):
+    """Median CUDA-event time of fn over k calls (after warm-up), the L2 flushed before each when given."""
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
     ts = []
-    for _ in range(max(5, min(args.steps, 200))):
-        flush.zero_()
+    for _ in range(k):
+        if flush is not None:
+            flush.zero_()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        m.dot(x, out=out)
+        fn()
         e1.record()
         torch.cuda.synchronize()
         ts.append(e0.elapsed_time(e1) * 1e-3)
-    t = statistics.median(ts)
-    U = m.matrix().t().to(torch.complex128)
-    unit_err = float(torch.linalg.norm(U @ U.conj().t() - torch.eye(Nc, dtype=torch.complex128, device=dev)))
-    n_mzi = int(mask.sum())
-    print(json.dumps({"metric": "MZI-apps/s (fwd)", "value": n_mzi * Bc / t, "unit": "MZI-apps/s", "n_gpus": 1,
-                      "steps": len(ts), "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
-                      "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded)",
-                      "config": {"workload": "clements_mzi_N64_L64_B1024_fwd", "n_mzi": n_mzi,
-                                 "l2": "flushed between timed calls"},
-                      "unitarity_error": unit_err, "status": m.status()}))
+    return statistics.median(ts)
 
 
-def run_c4(args):
-    """Unitary fitting: Clements mzi N=128 L=128 with splitting errors N(0, 0.02), target a Haar-random
-    unitary (QR of a complex Gaussian with the R-diagonal phase fix), x = I, J = ||U - U_t||_F^2,
-    2000 Adam steps (lr 1e-2) on theta, phi through the autograd function; steps/s and the fidelity
-    |tr(U^H U_t)|^2 / N^2 reached.  The headline runs the step as a CUDA graph (GraphedStep: captured
-    once, replayed); the same 2000 steps run eagerly beside it, from the same start, with the same
-    device-side Adam, and must end at the same loss."""
+def run_plain_forward(args, peak):
+    """Plain forward propagation, Clements mzi N=64 L=64 (2016 MZIs), ideal splitters, B=1024 unit-norm
+    complex64 vectors, one reference-shaped call (MeshNetworkGPU.dot -> mg_fwdprop); error against the
+    complex128 port and the unitarity error ||U U^H - I||_F of the programmed mesh."""
     import torch
     from meshes_gb300 import MeshNetworkGPU
-    from meshes_gb300 import geometry as gm
-    from meshes_gb300.autograd import GraphedStep, mesh_apply
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
-    rng = np.random.default_rng(1004)
-    Nc = 128
-    lens, shifts = gm.clements(Nc)
-    mask = gm.active_mask_nn(Nc, lens, shifts)
-    p0 = rng.uniform(0, 2 * np.pi, (len(lens), Nc // 2, 2)).astype(np.float32)
-    s0 = rng.normal(0, 0.02, (len(lens), Nc // 2, 2)).astype(np.float32)
-    p0[~mask] = 0
-    s0[~mask] = 0
-    m = MeshNetworkGPU(Nc, len(lens), lens, shifts, p0.reshape(-1), s0, "mzi", is_phase=False, device=dev)
-    Z = (rng.standard_normal((Nc, Nc)) + 1j * rng.standard_normal((Nc, Nc))) / np.sqrt(2)
-    Q, R = np.linalg.qr(Z)
-    Ut = (Q * (np.diag(R) / np.abs(np.diag(R)))[None, :]).astype(np.complex64)
-    x = torch.eye(Nc, dtype=torch.complex64, device=dev)
-    target = torch.tensor(Ut.T, device=dev)
-    n_steps = 2000
-
-    def trainer():
-        p = torch.tensor(p0, device=dev, requires_grad=True)
-        opt = torch.optim.Adam([p], lr=1e-2, capturable=True)
-
-        def step():
-            opt.zero_grad(set_to_none=True)
-            loss = ((mesh_apply(m, x, p) - target).abs() ** 2).sum()
-            loss.backward()
-            opt.step()
-            return loss
-        return p, step
-
-    # eager: every step from Python
-    p_e, step_e = trainer()
-    first = float(step_e().detach())
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(n_steps - 1):
-        loss_e = step_e()
-    torch.cuda.synchronize()
-    t_eager = (time.perf_counter() - t0) / (n_steps - 1)
-    # graphed: 3 warm-up steps and the capture, then replays
-    p, step = trainer()
-    warm = 3
-    graphed = GraphedStep(step, warmup=warm)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(n_steps - warm):
-        loss = graphed()
-    torch.cuda.synchronize()
-    t = (time.perf_counter() - t0) / (n_steps - warm)
-    with torch.no_grad():
-        U = mesh_apply(m, x, p).t().to(torch.complex128)
-        fid = float(torch.abs(torch.trace(U.conj().t() @ torch.tensor(Ut, dtype=torch.complex128, device=dev))) ** 2
-                    / Nc ** 2)
-    print(json.dumps({"metric": "Adam steps/s (unitary fitting)", "value": 1.0 / t, "unit": "steps/s", "n_gpus": 1,
-                      "steps": n_steps, "warmup": warm, "ms_per_step": t * 1e3, "higher_is_better": True,
-                      "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded)",
-                      "config": {"workload": "clements_mzi_N128_L128_haar_fit_2000_adam", "lr": 1e-2},
-                      "loss_first": first, "loss_last": float(loss.detach()), "fidelity": fid,
-                      "eager": {"steps_per_s": 1.0 / t_eager, "ms_per_step": t_eager * 1e3,
-                                "loss_last": float(loss_e.detach()),
-                                "same_phases": bool(torch.equal(p.detach(), p_e.detach()))},
-                      "timing": "host wall clock per optimisation step (fwd + bwd + Adam), device synchronised; "
-                                "headline: CUDA-graph replay of the whole step"}))
+    rng = np.random.default_rng(1000)
+    nc, bc = 64, 1024
+    lens, shifts = clements_layout(nc)
+    mask = active_mask(nc, lens, shifts)
+    p = rng.uniform(0, 2 * np.pi, (len(lens), nc // 2, 2)).astype(np.float32)
+    p[~mask] = 0
+    m = MeshNetworkGPU(nc, len(lens), lens, shifts, p.reshape(-1), None, "mzi", is_phase=False, device=dev)
+    x_h = unit_rows(rng, bc, nc)
+    x = torch.from_numpy(x_h).to(dev).t()                 # (N, B) columns, the reference's layout
+    out = torch.empty_like(x)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    with ClockSampler(gpu_id(torch, dev)) as cs:
+        t = event_ms(torch, lambda: m.dot(x, out=out), max(20, min(args.steps * 10, 200)), warm=max(3, args.warmup),
+                     flush=flush)
+    y_h = out.t().cpu().numpy()
+    U = m.matrix().t().to(torch.complex128)
+    unit_err = float(torch.linalg.norm(U @ U.conj().t() - torch.eye(nc, dtype=torch.complex128, device=dev)))
+    n_mzi = int(mask.sum())
+    err = cpu_forward_check(nc, lens, shifts, p, None, x_h, y_h)
+    return {"metric": "MZI-apps/s (fwd)", "value": n_mzi * bc / t, "unit": "MZI-apps/s", "ms": t * 1e3,
+            "config": {"workload": "clements_mzi_N64_L64_B1024_fwd", "n_mzi": n_mzi, "B": bc,
+                       "call": "MeshNetworkGPU.dot -> mg_fwdprop (coefficient pass + propagation)",
+                       "l2": "flushed between timed calls"},
+            "rel_err": {"y": err, "tolerance": TOL, "ok": bool(err <= TOL),
+                        "against": "complex128 port of c/dot.cpp, every vector"},
+            "unitarity_error": unit_err,
+            "roofline": roofline_fp32(n_mzi * bc * FLOP_FWD / t, peak, "mg_fwdprop (coef_kernel + prop_kernel<FWD>)"),
+            "cpu_baseline": cpu_baseline_forward(nc, lens, shifts, p, None, x_h),
+            "clocks": cs.summary(), "status": m.status()}
 
 
-def run_lossy(args):
-    """Lossy generic MZIs (phase errors and gains g_ij; reference crossing.py:444-488) on the Clements
-    N=256 L=256 mesh, B=4096: forward + adjoint through LossyMesh (inputs checkpointed per segment,
-    each segment recomputed and back-propagated from stored layer inputs), J = sum |y - y_t|^2."""
-    import torch
-    from meshes_gb300 import geometry as gm
-    from meshes_gb300.lossy import LossyMesh
-    dev = torch.device("cuda", 0)
-    torch.cuda.set_device(dev)
-    lens, shifts, p, s, x_h, yt_h, n_mzi = make_problem()
-    rng = np.random.default_rng(1006)
-    L = len(lens)
-    mask = gm.active_mask_nn(N, lens, shifts)
-    s14 = np.zeros((L, N // 2, 14))
-    s14[..., :2] = s
-    s14[..., 2:10] = rng.normal(0, 0.02, (L, N // 2, 8))
-    s14[..., 10:] = -np.abs(rng.normal(0.004, 0.002, (L, N // 2, 4)))
-    s14[~mask] = 0
-    mesh = LossyMesh(N, lens, shifts, device=dev)
-    pt = torch.tensor(p, dtype=torch.float64, device=dev, requires_grad=True)
-    st = torch.tensor(s14, dtype=torch.float64, device=dev)
-    x = torch.from_numpy(x_h).to(dev)
-    yt = torch.from_numpy(yt_h).to(dev)
-
-    def step():
-        pt.grad = None
-        y = mesh(x, mesh.T(pt, st))
-        loss = torch.sum(torch.abs(y - yt) ** 2)
-        loss.backward()
-        return loss
-
-    for _ in range(max(3, args.warmup)):
-        step()
-    torch.cuda.synchronize()
-    k = max(5, min(args.steps, 50))
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(k):
-        step()
-    e1.record()
-    torch.cuda.synchronize()
-    t = e0.elapsed_time(e1) * 1e-3 / k
-    print(json.dumps({"metric": "MZI-apps/s (fwd+bwd, lossy, checkpointed)", "value": n_mzi * B / t,
-                      "unit": "MZI-apps/s", "n_gpus": 1, "steps": k, "warmup": args.warmup, "ms_per_step": t * 1e3,
-                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
-                      "data": "synthetic (seeded)",
-                      "config": {"workload": "clements_lossy_mzi_N256_L256_B4096_fwd+bwd", "segment": mesh.segment_for(B),
-                                 "includes": "T(p) and its phase VJP (library kernels); per segment a forward "
-                                             "launch, then a recompute, a stored back-propagation and a reduce"},
-                      "status": mesh.status()}))
-
-
-def run_batched(args):
-    """Batched uneven meshes: the one-mesh-per-call drop-in (mg_fwdprop / mg_backdiff per mesh) against
-    the persistent multi-mesh launch replayed from a CUDA graph; forward and forward + backward."""
+def run_batched(args, peak):
+    """512 uneven meshes: the one-mesh-per-call drop-in (mg_fwdprop / mg_backdiff per mesh) against the
+    persistent multi-mesh launch replayed from a CUDA graph; forward and forward + backward."""
     import torch
     from meshes_gb300 import MeshNetworkGPU, _lib
     from meshes_gb300.batched import BatchedMeshes
@@ -684,22 +900,26 @@ def run_batched(args):
     torch.cuda.set_device(dev)
     st = torch.cuda.current_stream().cuda_stream
     prob = make_batched_problem(n_meshes=args.meshes)
+    grng = np.random.default_rng(1013)
     meshes, bufs = [], []
     for d in prob:
         m = MeshNetworkGPU(d["N"], d["L"], d["lens"], d["shifts"], d["p"].reshape(-1), d["s"], d["cr"],
                            is_phase=False, device=dev)
         meshes.append(m)
         x = torch.from_numpy(d["x"]).to(dev)
+        gy = unit_rows(grng, d["B"], d["N"], real=d["cr"] == "orth")
+        d["gy"] = gy
         nbf = lib.mg_workspace_bytes(0, d["N"], d["L"], d["B"], m.crossing, 0, None)
         nbb = lib.mg_workspace_bytes(2, d["N"], d["L"], d["B"], m.crossing, 0, None)
         wf = torch.empty(nbf, dtype=torch.uint8, device=dev)
         wb = torch.empty(nbb, dtype=torch.uint8, device=dev)
         lib.mg_workspace_init(wf.data_ptr(), nbf, st)
         lib.mg_workspace_init(wb.data_ptr(), nbb, st)
-        bufs.append(dict(x=x, y=torch.empty_like(x), g=torch.randn_like(x) if x.is_complex() else torch.randn_like(x),
-                         gi=torch.empty_like(x), dp=torch.empty(m.p_phase.numel(), device=dev),
-                         wf=(wf, nbf), wb=(wb, nbb)))
+        bufs.append(dict(x=x, y=torch.empty_like(x), g=torch.from_numpy(gy).to(dev), gi=torch.empty_like(x),
+                         dp=torch.empty(m.p_phase.numel(), device=dev), wf=(wf, nbf), wb=(wb, nbb)))
     units = sum(d["n_mzi"] * d["B"] for d in prob)
+    flops_f = sum(d["n_mzi"] * d["B"] * FLOPS[d["cr"]][0] for d in prob)
+    flops_b = sum(d["n_mzi"] * d["B"] * FLOPS[d["cr"]][1] for d in prob)
 
     def plain(backward):
         for d, m, b in zip(prob, meshes, bufs):
@@ -724,14 +944,13 @@ def run_batched(args):
         bm.step(True)
         bm.step(True)
         print(json.dumps({"profile_steps": 2, "meshes": len(prob), "items": bm.n_items, "status": bm.check_status()}))
-        return
+        return None
     g_f = BatchedMeshes.capture(bm, backward=False)
-    bm2 = bm
     g_fb = torch.cuda.CUDAGraph()
-    bm2.step(True)
+    bm.step(True)
     torch.cuda.synchronize()
     with torch.cuda.graph(g_fb):
-        bm2.step(True)
+        bm.step(True)
 
     def t_of(fn, k):
         for _ in range(max(2, args.warmup)):
@@ -746,123 +965,310 @@ def run_batched(args):
         return e0.elapsed_time(e1) * 1e-3 / k
 
     k = max(3, min(args.steps, 20))
-    t_plain_f = t_of(lambda: plain(False), k)
-    t_plain_fb = t_of(lambda: plain(True), k)
-    t_bat_f = t_of(g_f.replay, k)
-    t_bat_fb = t_of(g_fb.replay, k)
+    with ClockSampler(gpu_id(torch, dev)) as cs:
+        t_plain_f = t_of(lambda: plain(False), k)
+        t_plain_fb = t_of(lambda: plain(True), k)
+        t_bat_f = t_of(g_f.replay, k)
+        t_bat_fb = t_of(g_fb.replay, k)
+    # one more forward + backward replay; its outputs are checked per mesh
+    g_fb.replay()
     status = bm.check_status()
-    line = {"metric": "MZI-apps/s (batched uneven meshes, fwd+bwd)", "value": units / t_bat_fb, "unit": "MZI-apps/s",
-            "n_gpus": 1, "steps": k, "warmup": args.warmup, "ms_per_step": t_bat_fb * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "c64/f32", "data": "synthetic (seeded)",
-            "config": {"workload": "batched_%d_meshes_clements_reck_orth_N8-256_B1-2048" % len(prob), "meshes": len(prob),
-                       "mzi_apps_per_pass": units, "items": bm.n_items, "graph": True},
+    outs = [(stt.y.cpu().numpy(), d["gy"], stt.gx.cpu().numpy(), stt.dp.cpu().numpy()) for stt, d in zip(bm.states, prob)]
+    err = cpu_check_batched(prob, outs)
+    return {"metric": "MZI-apps/s (batched uneven meshes, fwd+bwd)", "value": units / t_bat_fb, "unit": "MZI-apps/s",
+            "ms": t_bat_fb * 1e3,
+            "config": {"workload": "batched_%d_meshes_clements_reck_orth_N8-256_B1-2048" % len(prob),
+                       "meshes": len(prob), "mzi_apps_per_pass": units, "items": bm.n_items, "graph": True},
             "batched": {"fwd_mzi_per_s": units / t_bat_f, "fwdbwd_mzi_per_s": units / t_bat_fb,
                         "fwd_ms": t_bat_f * 1e3, "fwdbwd_ms": t_bat_fb * 1e3},
             "plain_one_mesh_per_call": {"fwd_mzi_per_s": units / t_plain_f, "fwdbwd_mzi_per_s": units / t_plain_fb,
                                         "fwd_ms": t_plain_f * 1e3, "fwdbwd_ms": t_plain_fb * 1e3},
             "speedup_batched_vs_plain": {"fwd": t_plain_f / t_bat_f, "fwdbwd": t_plain_fb / t_bat_fb},
-            "status": status}
-    print(json.dumps(line))
+            "rel_err": err,
+            "roofline": roofline_fp32((flops_f + flops_b) / t_bat_fb, peak,
+                                      "batched_kernel (forward + back-propagation launches and reduce)"),
+            "roofline_fwd": roofline_fp32(flops_f / t_bat_f, peak, "batched_kernel (forward launch)"),
+            "clocks": cs.summary(), "status": status}
 
 
-def run_serve(args):
-    """Served mixed traffic: 64 resident meshes (Clements / log-depth butterfly, N in {16..512}, splitters
-    N(0, 0.02)), Poisson arrivals at 20k req/s, uniform mesh choice, batch log-uniform in [1, 512],
-    80% forward / 20% gradient requests; p50/p99 latency from arrival to result and MZI-apps/s."""
+def run_unitary_fit(args, peak):
+    """Unitary fitting: Clements mzi N=128 L=128 with splitting errors N(0, 0.02), target a Haar-random
+    unitary (QR of a complex Gaussian with the R-diagonal phase fix), x = I, J = ||U - U_t||_F^2,
+    2000 Adam steps (lr 1e-2) on theta, phi through the autograd function; steps/s and the fidelity
+    |tr(U^H U_t)|^2 / N^2 of the fitted phases re-evaluated in complex128.  The headline runs the step as a
+    CUDA graph (GraphedStep: captured once, replayed); the same 2000 steps run eagerly beside it, from the same
+    start, with the same device-side Adam, and must end at the same phases."""
     import torch
     from meshes_gb300 import MeshNetworkGPU
-    from meshes_gb300 import geometry as gm
+    from meshes_gb300.autograd import GraphedStep, mesh_apply
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(1004)
+    nc = 128
+    lens, shifts = clements_layout(nc)
+    mask = active_mask(nc, lens, shifts)
+    p0 = rng.uniform(0, 2 * np.pi, (len(lens), nc // 2, 2)).astype(np.float32)
+    s0 = rng.normal(0, 0.02, (len(lens), nc // 2, 2)).astype(np.float32)
+    p0[~mask] = 0
+    s0[~mask] = 0
+    m = MeshNetworkGPU(nc, len(lens), lens, shifts, p0.reshape(-1), s0, "mzi", is_phase=False, device=dev)
+    Z = (rng.standard_normal((nc, nc)) + 1j * rng.standard_normal((nc, nc))) / np.sqrt(2)
+    Q, R = np.linalg.qr(Z)
+    Ut = (Q * (np.diag(R) / np.abs(np.diag(R)))[None, :]).astype(np.complex64)
+    x = torch.eye(nc, dtype=torch.complex64, device=dev)
+    target = torch.tensor(Ut.T, device=dev)
+    n_steps = 2000
+    n_mzi = int(mask.sum())
+
+    def trainer():
+        p = torch.tensor(p0, device=dev, requires_grad=True)
+        opt = torch.optim.Adam([p], lr=1e-2, capturable=True)
+
+        def step():
+            opt.zero_grad(set_to_none=True)
+            loss = ((mesh_apply(m, x, p) - target).abs() ** 2).sum()
+            loss.backward()
+            opt.step()
+            return loss
+        return p, step
+
+    with ClockSampler(gpu_id(torch, dev)) as cs:
+        # eager: every step from Python
+        p_e, step_e = trainer()
+        first = float(step_e().detach())
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(n_steps - 1):
+            loss_e = step_e()
+        torch.cuda.synchronize()
+        t_eager = (time.perf_counter() - t0) / (n_steps - 1)
+        # graphed: 3 warm-up steps and the capture, then replays
+        p, step = trainer()
+        warm = 3
+        graphed = GraphedStep(step, warmup=warm)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(n_steps - warm):
+            loss = graphed()
+        torch.cuda.synchronize()
+        t = (time.perf_counter() - t0) / (n_steps - warm)
+    with torch.no_grad():
+        U = mesh_apply(m, x, p).t().to(torch.complex128)
+        fid = float(torch.abs(torch.trace(U.conj().t() @ torch.tensor(Ut, dtype=torch.complex128, device=dev))) ** 2
+                    / nc ** 2)
+    fid128, err_U = cpu_unitary_fit_check(lens, shifts, p.detach().cpu().numpy(), s0, U.cpu().numpy(), Ut)
+    return {"metric": "Adam steps/s (unitary fitting)", "value": 1.0 / t, "unit": "steps/s", "ms": t * 1e3,
+            "config": {"workload": "clements_mzi_N128_L128_haar_fit_2000_adam", "lr": 1e-2, "steps": n_steps},
+            "loss_first": first, "loss_last": float(loss.detach()), "fidelity": fid,
+            "fidelity_complex128": fid128,
+            "rel_err": {"U": err_U, "fidelity_abs_diff": abs(fid - fid128), "tolerance": TOL, "ok": bool(err_U <= TOL),
+                        "against": "the fitted phases re-evaluated by the complex128 port of c/dot.cpp"},
+            "eager": {"steps_per_s": 1.0 / t_eager, "ms_per_step": t_eager * 1e3,
+                      "loss_last": float(loss_e.detach()), "same_phases": bool(torch.equal(p.detach(), p_e.detach()))},
+            "roofline": roofline_fp32(n_mzi * nc * (FLOP_FWD + FLOP_BWD) / t, peak,
+                                      "whole Adam step (forward, back-propagation, optimizer) as one CUDA graph"),
+            "timing": "host wall clock per optimisation step (fwd + bwd + Adam), device synchronised; "
+                      "headline: CUDA-graph replay of the whole step",
+            "clocks": cs.summary()}
+
+
+def run_lossy(args, peak):
+    """Lossy generic MZIs (phase errors and gains g_ij; reference crossing.py:444-488) on the Clements
+    N=256 L=256 mesh, B=4096: forward + adjoint through LossyMesh (inputs checkpointed per segment,
+    each segment recomputed and back-propagated from stored layer inputs), J = sum |y - y_t|^2."""
+    import torch
+    from meshes_gb300.lossy import LossyMesh
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    lens, shifts, p, s, x_h, yt_h, n_mzi = make_problem()
+    rng = np.random.default_rng(1006)
+    L = len(lens)
+    mask = active_mask(N, lens, shifts)
+    s14 = np.zeros((L, N // 2, 14))
+    s14[..., :2] = s
+    s14[..., 2:10] = rng.normal(0, 0.02, (L, N // 2, 8))
+    s14[..., 10:] = -np.abs(rng.normal(0.004, 0.002, (L, N // 2, 4)))
+    s14[~mask] = 0
+    mesh = LossyMesh(N, lens, shifts, device=dev)
+    pt = torch.tensor(p, dtype=torch.float64, device=dev, requires_grad=True)
+    stt = torch.tensor(s14, dtype=torch.float64, device=dev)
+    x = torch.from_numpy(x_h).to(dev)
+    yt = torch.from_numpy(yt_h).to(dev)
+    out = {}
+
+    def step():
+        pt.grad = None
+        y = mesh(x, mesh.T(pt, stt))
+        loss = torch.sum(torch.abs(y - yt) ** 2)
+        loss.backward()
+        out["y"] = y
+        return loss
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    k = max(5, min(args.steps, 50))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(gpu_id(torch, dev)) as cs:
+        e0.record()
+        for _ in range(k):
+            step()
+        e1.record()
+        torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) * 1e-3 / k
+    n_chk = 64
+    err = cpu_lossy_check(lens, shifts, p, s14, x_h[:n_chk], out["y"][:n_chk].cpu().numpy())
+    return {"metric": "MZI-apps/s (fwd+bwd, lossy, checkpointed)", "value": n_mzi * B / t, "unit": "MZI-apps/s",
+            "ms": t * 1e3,
+            "config": {"workload": "clements_lossy_mzi_N256_L256_B4096_fwd+bwd", "segment": mesh.segment_for(B),
+                       "includes": "T(p) and its phase VJP (library kernels); per segment a forward launch, then a "
+                                   "recompute, a stored back-propagation and a reduce"},
+            "rel_err": {"y": err, "tolerance": TOL, "ok": bool(err <= TOL),
+                        "against": "the oracle's lossy generic MZI mesh in complex128, first %d vectors (the "
+                                   "gradient is checked against central differences by the GPU tests)" % n_chk},
+            "roofline": roofline_fp32(n_mzi * B * (FLOP_FWD + FLOP_BWD) / t, peak,
+                                      "lossy step (the reference's 32 + 96 FLOP per MZI-application)"),
+            "clocks": cs.summary(), "status": mesh.status()}
+
+
+def run_serve(args, peak):
+    """Served mixed traffic: 64 resident meshes (Clements / log-depth butterfly, N in {16..512}, splitters
+    N(0, 0.02)), Poisson arrivals at 20k req/s for 60 s, uniform mesh choice, batch log-uniform in [1, 512],
+    80% forward / 20% gradient requests; p50/p99 latency from scheduled arrival to result on the host,
+    MZI-apps/s, and a seeded sample of the results checked in complex128."""
+    import gc
+
+    import torch
+    from meshes_gb300 import MeshNetworkGPU
     from meshes_gb300.serve import MeshServer
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     rng = np.random.default_rng(1005)
-    meshes, pools = [], []
+    meshes, pools, meshes_h = [], [], []
     for i in range(64):
-        N = int(rng.choice([16, 32, 64, 128, 256, 512]))
+        n = int(rng.choice([16, 32, 64, 128, 256, 512]))
         if i % 2 == 0:
-            lens, shifts = gm.clements(N)
+            lens, shifts = clements_layout(n)
             L, strides = len(lens), None
-            mask = gm.active_mask_nn(N, lens, shifts)
+            mask = active_mask(n, lens, shifts)
         else:
-            strides = gm.fft(N)
+            strides = fft_layout(n)
             lens = shifts = None
             L = len(strides)
-            mask = np.ones((L, N // 2), bool)
-        p = rng.uniform(0, 2 * np.pi, (L, N // 2, 2)).astype(np.float32)
-        s = rng.normal(0, 0.02, (L, N // 2, 2)).astype(np.float32)
+            mask = np.ones((L, n // 2), bool)
+        p = rng.uniform(0, 2 * np.pi, (L, n // 2, 2)).astype(np.float32)
+        s = rng.normal(0, 0.02, (L, n // 2, 2)).astype(np.float32)
         p[~mask] = 0
         s[~mask] = 0
-        meshes.append(MeshNetworkGPU(N, L, lens, shifts, p.reshape(-1), s, "mzi", is_phase=False, strides=strides,
+        meshes.append(MeshNetworkGPU(n, L, lens, shifts, p.reshape(-1), s, "mzi", is_phase=False, strides=strides,
                                      device=dev))
-        x = rng.standard_normal((512, N)) + 1j * rng.standard_normal((512, N))
-        pools.append((x / np.linalg.norm(x, axis=1, keepdims=True)).astype(np.complex64))
+        meshes_h.append(dict(N=n, lens=lens, shifts=shifts, strides=strides, p=p, s=s, n_mzi=int(mask.sum())))
+        pools.append(unit_rows(rng, 512, n))
     srv = MeshServer(meshes, mem_budget=512 << 20)
     # the client loop and the server's scheduler thread share the interpreter: hand the GIL over every
     # 0.2 ms instead of every 5 ms, so neither side waits a whole default interval for the other
     sys.setswitchinterval(2e-4)
-    n_mzi = [(sum(m.lens_h) if m.strides is None else m.L * (m.N // 2)) for m in meshes]
     rate, duration = float(args.rate), float(args.duration)
     n_req = int(rate * duration)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
     mesh_ids = rng.integers(0, 64, n_req)
     bsz = np.clip(np.round(np.exp(rng.uniform(0, np.log(512), n_req))), 1, 512).astype(int)
     grad = rng.random(n_req) < 0.2
+    # seeded sample of requests whose results are kept and checked (the others are dropped on completion)
+    crng = np.random.default_rng(1015)
+    fwd_ids, grad_ids = np.flatnonzero(~grad), np.flatnonzero(grad)
+    keep = set(crng.choice(fwd_ids, min(48, len(fwd_ids)), replace=False).tolist() +
+               crng.choice(grad_ids, min(48, len(grad_ids)), replace=False).tolist())
+    done_t = np.full(n_req, np.nan)
+    kept = {}
+
+    def on_done(k):
+        def cb(f):
+            done_t[k] = f.t_done
+            if k in keep and not f.cancelled() and f.exception() is None:
+                kept[k] = f.result()
+        return cb
+
     srv.start()
-    # warm-up: one request per mesh
-    for i in range(64):
+    for i in range(64):                                   # warm-up: one request per mesh
         srv.submit(i, pools[i][:4]).result(60)
+    # the harness keeps every future alive until it completes; without this the interpreter's full
+    # collections walk them and stall the client and completion threads for ~0.1-0.2 s
+    gc.disable()
     futs = []
     t_submit = 0.0
-    # the harness keeps every future and result alive; without this the interpreter's full collections
-    # walk hundreds of thousands of them and stall the client and completion threads for ~0.1-0.2 s
-    import gc
-    gc.disable()
-    t0 = time.perf_counter()
-    k = 0
-    while k < n_req:
-        now = time.perf_counter() - t0
-        while k < n_req and arrivals[k] <= now:
-            i, b = int(mesh_ids[k]), int(bsz[k])
-            x = pools[i][:b]
-            ts0 = time.perf_counter()
-            f = srv.submit(i, x, gy=x if grad[k] else None)
-            t_submit += time.perf_counter() - ts0
-            futs.append((k, f))
-            k += 1
-        time.sleep(20e-6)
-    for _, f in futs:
-        f.result(120)
-    t_end = max(f.t_done for _, f in futs)
+    with ClockSampler(gpu_id(torch, dev)) as cs:
+        t0 = time.perf_counter()
+        k = 0
+        while k < n_req:
+            now = time.perf_counter() - t0
+            while k < n_req and arrivals[k] <= now:
+                i, b = int(mesh_ids[k]), int(bsz[k])
+                x = pools[i][:b]
+                ts0 = time.perf_counter()
+                f = srv.submit(i, x, gy=x if grad[k] else None)
+                f.add_done_callback(on_done(k))
+                t_submit += time.perf_counter() - ts0
+                futs.append(f)
+                k += 1
+            if len(futs) > 4096:                          # drop references to finished requests
+                futs = [f for f in futs if not f.done()]
+            time.sleep(20e-6)
+        for f in futs:
+            f.result(120)
+        t_end = float(np.nanmax(done_t))
     gc.enable()
     srv.stop()
+    status = srv.kernel_status()
     # latency of each request: result available on the host minus its scheduled arrival time
-    lat = np.array([f.t_done - (t0 + arrivals[kk]) for kk, f in futs])
-    apps = sum(n_mzi[int(mesh_ids[kk])] * int(bsz[kk]) * (2 if grad[kk] else 1) for kk, _ in futs)
+    lat = done_t - (t0 + arrivals)
+    nm = np.array([d["n_mzi"] for d in meshes_h], np.float64)[mesh_ids] * bsz
+    apps = float(np.sum(nm * (1 + grad)))
+    flops = float(np.sum(nm * (FLOP_FWD + FLOP_BWD * grad)))
     span = t_end - t0
-    line = {"metric": "serve p50/p99 latency (ms) and MZI-apps/s", "value": float(np.percentile(lat, 50) * 1e3),
-            "unit": "ms (p50 latency)", "n_gpus": 1, "steps": len(futs), "warmup": 64, "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded Poisson stream)",
-            "config": {"workload": "serve_64_meshes_clements_butterfly_N16-512_%dk_req_s" % round(rate / 1000), "rate_req_s": rate,
-                       "duration_s": duration, "requests": len(futs), "grad_fraction": float(grad.mean())},
+    checked = [(int(mesh_ids[k]), pools[int(mesh_ids[k])][:int(bsz[k])],
+                pools[int(mesh_ids[k])][:int(bsz[k])] if grad[k] else None, kept[k]) for k in sorted(kept)]
+    err = cpu_check_served(meshes_h, checked)
+    return {"metric": "serve p50/p99 latency (ms) and MZI-apps/s", "value": float(np.percentile(lat, 50) * 1e3),
+            "unit": "ms (p50 latency)", "higher_is_better": False,
+            "config": {"workload": "serve_64_meshes_clements_butterfly_N16-512_%dk_req_s_%ds" % (round(rate / 1000),
+                                                                                                  round(duration)),
+                       "rate_req_s": rate, "duration_s": duration, "requests": n_req,
+                       "grad_fraction": float(grad.mean())},
             "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
-            "throughput_mzi_apps_per_s": apps / span, "served_req_per_s": len(futs) / span, "ticks": srv.ticks,
-            "client_us_per_submit": 1e6 * t_submit / max(len(futs), 1), "scheduler": "native (mg_server)",
-            "status": srv.kernel_status()}
-    print(json.dumps(line))
+            "incomplete_requests": int(np.isnan(done_t).sum()),
+            "throughput_mzi_apps_per_s": apps / span, "served_req_per_s": n_req / span, "ticks": srv.ticks,
+            "client_us_per_submit": 1e6 * t_submit / max(n_req, 1), "scheduler": "native (mg_server)",
+            "rel_err": err,
+            "roofline": roofline_fp32(flops / span, peak, "served traffic (persistent forward and back-propagation "
+                                                          "launches per tick)"),
+            "clocks": cs.summary(), "status": status}
+
+
+CONFIG_RUNNERS = {"plain_forward": run_plain_forward, "batched": run_batched, "unitary_fit": run_unitary_fit,
+                  "serve": run_serve, "lossy": run_lossy}
+
+
+def standalone_peak():
+    import torch
+    from meshes_gb300 import _lib
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+    return fp32_peak(torch, _lib.load(), _lib, dev, stream, stream.cuda_stream, gpu_id(torch, dev))
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
-    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--profile", action="store_true", help="two untimed steps only (for ncu captures)")
-    ap.add_argument("--workload", default="clements256", choices=["clements256", "batched", "serve", "c1", "c4", "lossy"],
-                    help="clements256: the headline fwd+bwd step; batched: 512 uneven meshes, plain vs "
-                         "persistent; serve: Poisson request stream on 64 resident meshes; c1: N=64 forward; "
-                         "c4: N=128 unitary fitting with Adam; lossy: checkpointed adjoint of lossy MZIs")
-    ap.add_argument("--duration", type=float, default=10.0, help="serve workload: seconds of traffic")
+    ap.add_argument("--workload", default="all", choices=["all", "step"] + sorted(CONFIG_RUNNERS),
+                    help="all: the headline step and every other workload in one line; step: the headline only; "
+                         "otherwise one workload alone")
+    ap.add_argument("--duration", type=float, default=60.0, help="serve workload: seconds of traffic")
     ap.add_argument("--meshes", type=int, default=512, help="batched workload: number of meshes")
     ap.add_argument("--bwd-config", default="", help="with --profile: back-propagation launches with tile "
                                                     "configuration M,V,W,CL,S,split only")
@@ -874,10 +1280,11 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank)
         return
-    if args.workload != "clements256":
+    if args.workload in CONFIG_RUNNERS:
         if rank == 0:
-            {"batched": run_batched, "serve": run_serve, "c1": run_c1, "c4": run_c4,
-             "lossy": run_lossy}[args.workload](args)
+            res = CONFIG_RUNNERS[args.workload](args, standalone_peak())
+            if res is not None:
+                print(json.dumps(res), flush=True)
         return
     if world > 1:
         import torch
@@ -885,11 +1292,20 @@ def main():
         torch.cuda.set_device(local_rank)
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     try:
-        run_ours(args, rank, world, local_rank)
+        line = run_step(args, rank, world, local_rank)
     finally:
         if world > 1:
             import torch.distributed as dist
             dist.destroy_process_group()
+    if line is None:
+        return
+    peak = line.pop("_peak")
+    if args.workload == "all" and world == 1 and not args.profile:
+        line["configs"] = {}
+        for name, fn in CONFIG_RUNNERS.items():
+            res = fn(args, peak)
+            line["configs"][res["config"]["workload"]] = res
+    print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

@@ -14,8 +14,9 @@
  * for ideal splitters.  Geometry arrays are device int32 arrays of length L: lens/shifts for
  * nearest-neighbour meshes (Clements, Reck, ...), strides (log2 of the stride) for butterfly meshes.
  *
- * Limits: N even, 2 <= N <= 512; ldu >= N and even; u pointers 16-byte aligned (complex) or 8-byte
- * aligned (real).
+ * Limits: N even, 2 <= N <= 640 for nearest-neighbour meshes (the reference's own limit,
+ * gpu/mesh.py:83) and N a power of two <= 512 for butterfly meshes; ldu >= N and even; u pointers
+ * 16-byte aligned (complex) or 8-byte aligned (real).
  */
 #ifndef MESHES_GB300_H
 #define MESHES_GB300_H

@@ -2,12 +2,12 @@
 
 Run from the repository root, in a container where the reference tree is mounted:
 
-    make -C oracle ref                      # compiles the reference's c/dot.cpp into oracle/_ref/dot.so
-    python tests/golden/make_golden.py [/path/to/reference]
+    MESHES_REF=/path/to/reference make -C oracle ref
+    python tests/golden/make_golden.py [/path/to/reference]     # default: $MESHES_REF
 
 The reference package (``mesh.py`` + ``crossing.py`` + geometry classes) is imported from its own tree
-with two stand-ins that the survey found necessary: ``numba.njit`` as the identity and an empty
-``matplotlib.pyplot`` (neither library is on the path).  Its C backend (``mesh.py:82-95``) is pointed at
+with two stand-ins, because neither library is installed here: ``numba.njit`` as the identity and an empty
+``matplotlib.pyplot``.  Its C backend (``mesh.py:82-95``) is pointed at
 ``oracle/_ref/dot.so``, so every number stored here comes from the reference's own
 ``StructuredMeshNetwork.dot`` / ``dot_vjp`` (complex128, ``mesh.py:351-392``) and its complex64
 ``meshdot_helper32`` (``mesh.py:97-113``).  Back-propagation runs with one OpenMP thread
@@ -339,4 +339,9 @@ def main(ref_path):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) > 1:
+        main(sys.argv[1])
+    elif os.environ.get("MESHES_REF"):
+        main(os.environ["MESHES_REF"])
+    else:
+        sys.exit("usage: make_golden.py /path/to/reference (or set MESHES_REF)")
