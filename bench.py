@@ -1117,7 +1117,7 @@ def run_lossy(args, peak):
         torch.cuda.synchronize()
     t = e0.elapsed_time(e1) * 1e-3 / k
     n_chk = 64
-    err = cpu_lossy_check(lens, shifts, p, s14, x_h[:n_chk], out["y"][:n_chk].cpu().numpy())
+    err = cpu_lossy_check(lens, shifts, p, s14, x_h[:n_chk], out["y"][:n_chk].detach().cpu().numpy())
     return {"metric": "MZI-apps/s (fwd+bwd, lossy, checkpointed)", "value": n_mzi * B / t, "unit": "MZI-apps/s",
             "ms": t * 1e3,
             "config": {"workload": "clements_lossy_mzi_N256_L256_B4096_fwd+bwd", "segment": mesh.segment_for(B),
@@ -1303,8 +1303,15 @@ def main():
     if args.workload == "all" and world == 1 and not args.profile:
         line["configs"] = {}
         for name, fn in CONFIG_RUNNERS.items():
-            res = fn(args, peak)
-            line["configs"][res["config"]["workload"]] = res
+            t0 = time.perf_counter()
+            try:
+                res = fn(args, peak)
+                line["configs"][res["config"]["workload"]] = res
+            except Exception as e:      # a failed workload is reported in the line, not hidden
+                import traceback
+                traceback.print_exc()
+                line["configs"][name] = {"error": "%s: %s" % (type(e).__name__, e)}
+            print("bench: %s done in %.1f s" % (name, time.perf_counter() - t0), file=sys.stderr, flush=True)
     print(json.dumps(line), flush=True)
 
 

@@ -172,6 +172,17 @@ int mg_propagate(int op, int N, int L, int B, int crossing, int geometry, const 
                  void* out1, int ldu, float* dp, int ldp, int accumulate, const mg_config* cfg, void* workspace,
                  size_t workspace_bytes, void* stream);
 
+/* Test entry point for the bounded-wait failure path: mg_propagate (op MG_OP_FWD or MG_OP_BWD, nearest-neighbour
+ * geometry, tiles built by mg_build_tiles for the same shape, no dp) with every pipeline wait limited to wait_ns
+ * and the coefficient copy of pipeline chunk `unarmed_chunk` never issued.  Every CTA gives up at that chunk:
+ * it records MG_ST_TIMEOUT in the workspace status word, waits (within the same limit) for the copies it did
+ * issue, releases its barriers and returns, leaving the outputs incomplete.  Nothing stays in flight and the
+ * context stays usable; the next call on the workspace (after mg_read_status clears the status) runs normally.
+ * No counterpart in the reference (its kernels have no time limit). */
+int mg_propagate_wait_test(int op, int N, int L, int B, int crossing, const void* in0, const void* in1, void* out0,
+                           void* out1, int ldu, unsigned long long wait_ns, int unarmed_chunk, void* workspace,
+                           size_t workspace_bytes, void* stream);
+
 /* ---- permutations between layers (the reference's StructuredMeshNetwork.perm, mesh.py:238-277, applied
  * as c/dot.cpp:29-40,150-153,289-292 does; its GPU API forbids them, mesh.py:573) ---------------------
  * With geometry | MG_GEO_PERM, mg_build_perms writes the gather tables of `perms` into a workspace planned

@@ -340,9 +340,11 @@ void set_perm_args(const Plan& P, unsigned char* ws, int l0, int l1, PropArgs& a
 
 int run_prop(const Plan& P, const void* in0, const void* in1, void* out0, void* out1, int ldu, float* dp, int ldp,
              int accumulate, unsigned char* ws, cudaStream_t st, const void* target = nullptr, void* ckpt = nullptr,
-             int ckpt_every = 0) {
+             int ckpt_every = 0, unsigned long long wait_ns = 0, int unarmed = 0) {
   if (P.B == 0) return MG_OK;
   PropArgs a{};
+  a.wait_ns = wait_ns;
+  a.unarmed = unarmed;
   a.target = target;
   a.act = nullptr;
   a.act_plane = 0;
@@ -720,6 +722,27 @@ int mg_propagate(int op, int N, int L, int B, int crossing, int geometry, const 
   if (op == OP_BWD && dp && ldp < N / 2 * crossing_np(crossing)) return fail(MG_E_ARG, "ldp too small");
   return run_prop(P, in0, in1, out0, out1, ldu, dp, ldp, accumulate, static_cast<unsigned char*>(ws),
                   static_cast<cudaStream_t>(stream));
+}
+
+int mg_propagate_wait_test(int op, int N, int L, int B, int crossing, const void* in0, const void* in1, void* out0,
+                           void* out1, int ldu, unsigned long long wait_ns, int unarmed_chunk, void* ws, size_t wsb,
+                           void* stream) {
+  g_err.clear();
+  if (op != OP_FWD && op != OP_BWD) return fail(MG_E_ARG, "op must be MG_OP_FWD or MG_OP_BWD");
+  if (wait_ns == 0) return fail(MG_E_ARG, "wait_ns must be positive");
+  Plan P;
+  TRY(make_plan(op, N, L, B, crossing, GEO_NN, nullptr, &P));
+  TRY(check_ws(P, ws, wsb));
+  TRY(check_ldu(P, ldu));
+  TRY(check_field(in0, "in0", P.real, B > 0));
+  TRY(check_field(in1, "in1", P.real, op == OP_BWD && B > 0));
+  TRY(check_field(out0, "out0", P.real, op != OP_BWD && B > 0));
+  TRY(check_field(out1, "out1", P.real, op != OP_FWD && B > 0));
+  const int nch = (L + P.CL - 1) / P.CL;
+  if (unarmed_chunk < 0 || unarmed_chunk >= nch)
+    return fail(MG_E_ARG, "unarmed_chunk=%d outside the launch's %d pipeline chunks", unarmed_chunk, nch);
+  return run_prop(P, in0, in1, out0, out1, ldu, nullptr, 0, 0, static_cast<unsigned char*>(ws),
+                  static_cast<cudaStream_t>(stream), nullptr, nullptr, 0, wait_ns, unarmed_chunk + 1);
 }
 
 int mg_build_perms(int op, int N, int L, int B, int crossing, int geometry, const int* perms, const mg_config* cfg,

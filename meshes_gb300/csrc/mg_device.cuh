@@ -148,13 +148,13 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
 // limit only has to separate "slow" from "never" (profilers replaying kernels are slow, not stuck).
 constexpr uint64_t kWaitLimitNs = 4000000000ull;   // 4 s
 
-// Wait for phase `parity` of `bar`; false after the time limit (the caller then records ST_TIMEOUT).
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+// Wait for phase `parity` of `bar`; false after `limit_ns` (the caller then records ST_TIMEOUT).
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, uint64_t limit_ns = kWaitLimitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer_ns();
   for (uint32_t it = 1;; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
-    if ((it & 63u) == 0 && globaltimer_ns() - t0 > kWaitLimitNs) return false;
+    if ((it & 63u) == 0 && globaltimer_ns() - t0 > limit_ns) return false;
   }
 }
 

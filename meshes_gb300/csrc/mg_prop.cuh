@@ -75,6 +75,11 @@ struct PropArgs {
   int ckpt_every;
   // layers per CTA block of the partial buffer (0: L); lets layer ranges keep every range's partials
   int pstride;
+  // time limit of each pipeline wait (0: kWaitLimitNs)
+  unsigned long long wait_ns;
+  // failure-path test only (mg_propagate_wait_test): chunk + 1 whose coefficient copy is never issued, so
+  // that its wait runs out (0: none)
+  int unarmed;
 };
 
 template <bool REAL> struct Fld { using T = float2; using C = C2x2; };
@@ -896,7 +901,9 @@ __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem
 
   auto chunk_lo = [&](int c) { return (OP == OP_BWD) ? max(0, a.L - (c + 1) * a.CL) : c * a.CL; };
   auto chunk_hi = [&](int c) { return (OP == OP_BWD) ? a.L - c * a.CL : min(a.L, (c + 1) * a.CL); };
+  const uint64_t wlim = a.wait_ns ? a.wait_ns : kWaitLimitNs;
   auto issue = [&](int c) {
+    if (c + 1 == a.unarmed) return;
     const int lo = chunk_lo(c), hi = chunk_hi(c);
     const unsigned bytes = (unsigned)(hi - lo) * a.layer_bytes;
     const uint32_t bar = smem_u32(bars + (c % a.S));
@@ -919,12 +926,13 @@ __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem
 
   for (int c = 0; c < nch; ++c) {
     const int lo = chunk_lo(c), hi = chunk_hi(c);
-    const bool ok = mbar_wait_bounded(smem_u32(bars + (c % a.S)), (uint32_t)((c / a.S) & 1));
+    const bool ok = mbar_wait_bounded(smem_u32(bars + (c % a.S)), (uint32_t)((c / a.S) & 1), wlim);
     if (__syncthreads_or(!ok)) {
       // give up: record, wait (bounded) for the copies still in flight, release the barriers, leave
       if (tid == 0) {
         set_status(a.status, ST_TIMEOUT);
-        for (int cc = c + 1; cc < issued; ++cc) mbar_wait_bounded(smem_u32(bars + (cc % a.S)), (uint32_t)((cc / a.S) & 1));
+        for (int cc = c + 1; cc < issued; ++cc)
+          if (cc + 1 != a.unarmed) mbar_wait_bounded(smem_u32(bars + (cc % a.S)), (uint32_t)((cc / a.S) & 1), wlim);
         for (int s = 0; s <= a.S; ++s) mbar_inval(smem_u32(bars + s));
       }
       return;
@@ -944,11 +952,12 @@ __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem
     if constexpr (OP == OP_BWD && kDirect) chunk_reduce_direct<M, GR>(a, kinds, lo, hi - lo, gst, np2, G);
     if constexpr (OP == OP_BWD && GR == 4) chunk_reduce_raw<M>(a, kinds, lo, hi - lo, gst, np2, G);
     if constexpr (kDT) {
-      const bool okd = mbar_wait_bounded(smem_u32(bars + a.S), (uint32_t)(c & 1));
+      const bool okd = mbar_wait_bounded(smem_u32(bars + a.S), (uint32_t)(c & 1), wlim);
       if (__syncthreads_or(!okd)) {
         if (tid == 0) {
           set_status(a.status, ST_TIMEOUT);
-          for (int cc = c + 1; cc < issued; ++cc) mbar_wait_bounded(smem_u32(bars + (cc % a.S)), (uint32_t)((cc / a.S) & 1));
+          for (int cc = c + 1; cc < issued; ++cc)
+          if (cc + 1 != a.unarmed) mbar_wait_bounded(smem_u32(bars + (cc % a.S)), (uint32_t)((cc / a.S) & 1), wlim);
           for (int s = 0; s <= a.S; ++s) mbar_inval(smem_u32(bars + s));
         }
         return;

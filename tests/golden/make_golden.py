@@ -335,7 +335,87 @@ def main(ref_path):
              shifts=np.array(shifts), p=flat_to_grid(pp, lens, shifts, N, 2), s=flat_to_grid(ss, lens, shifts, N, n_s),
              x=x, y=y, **extra)
 
+    converter_cases(save)
     print("wrote", *written, sep="\n  ")
+
+
+def converter_cases(save):
+    """Networks as the reference's StructuredMeshNetwork.gpu() converter sees them (mesh.py:568-579): for each
+    reference network the attributes that converter reads (N, L, lens, shifts, grid_phase, grid_splitter, the
+    crossing class, perm, is_phase, phi_out, phi_pos; a ClippedNetwork's full mesh and ports) and its own dot /
+    dot_vjp outputs.  Own seeded stream, so the fixtures above do not change."""
+    from meshes.clements import ClementsNetwork
+    from meshes.reck import ReckNetwork
+    from meshes.butterfly import ButterflyNetwork
+    from meshes.mesh import StructuredMeshNetwork
+    from meshes.square import SquareNetwork
+    from meshes.crossing import MZICrossingOutPhase
+
+    rng = np.random.default_rng(20261204)
+
+    def f32(a):
+        return np.asarray(a, np.float64).astype(np.float32).astype(np.float64)
+
+    def randomise(net):
+        net.p_phase[:] = f32(rng.uniform(0, 2 * np.pi, net.p_phase.shape))
+        if net.p_splitter.ndim:
+            net.p_splitter = f32(rng.normal(0, 0.02, net.p_splitter.shape))
+
+    def attrs(net, prefix=""):
+        perm_rows = np.array([np.arange(net.N) if r is None else np.asarray(r) for r in net.perm])
+        perm_none = np.array([r is None for r in net.perm])
+        return {prefix + "N": net.N, prefix + "L": net.L, prefix + "lens": np.array(net.lens),
+                prefix + "shifts": np.array(net.shifts), prefix + "grid_phase": net.grid_phase,
+                prefix + "grid_splitter": net.grid_splitter, prefix + "X": type(net.X).__name__,
+                prefix + "net_class": type(net).__name__, prefix + "perm_rows": perm_rows,
+                prefix + "perm_none": perm_none, prefix + "is_phase": bool(net.is_phase),
+                prefix + "phi_out": np.asarray(net.phi_out if net.is_phase else np.zeros(0)),
+                prefix + "phi_pos": net.phi_pos}
+
+    def case(name, net, B, vjp=True):
+        randomise(net)
+        N = net.N
+        x = rng.standard_normal((N, B)) + 1j * rng.standard_normal((N, B))
+        x /= np.linalg.norm(x, axis=0, keepdims=True)
+        y = net.dot(x)
+        out = dict(attrs(net), x=x, y=y, p_phase=net.p_phase)
+        if vjp:
+            t = rng.standard_normal((N, B)) + 1j * rng.standard_normal((N, B))
+            g = 2 * (y - t)
+            dJdp, dJdv = net.dot_vjp(y, g)
+            out.update(g=g, dJdp=dJdp, g_in=dJdv)
+        save("converter_" + name, **out)
+
+    n = 8
+    case("clements_mzi_N8_screen", ClementsNetwork(N=n, p_splitter=np.zeros((n * (n - 1) // 2, 2))), 5)
+    n = 6
+    case("reck_mzi_N6_screen", ReckNetwork(N=n, p_splitter=np.zeros((n * (n - 1) // 2, 2))), 4)
+    n = 8
+    case("butterfly_mzi_N8", ButterflyNetwork(N=n, p_splitter=np.zeros((n // 2 * (n - 1), 2))), 4)
+    n = 8
+    lens, shifts = [int(v) for v in ClementsNetwork(N=n).lens], [int(v) for v in ClementsNetwork(N=n).shifts]
+    perm = [None] * (len(lens) + 1)
+    for k in (1, 4, len(lens)):
+        perm[k] = rng.permutation(n)
+    case("perm_mzi_N8", StructuredMeshNetwork(n, lens, shifts, p_splitter=np.zeros((sum(lens), 2)), perm=perm,
+                                              is_phase=False), 3)
+    n = 6
+    case("outphase_N6", StructuredMeshNetwork(n, [int(v) for v in ClementsNetwork(N=n).lens],
+                                              [int(v) for v in ClementsNetwork(N=n).shifts],
+                                              p_splitter=np.zeros((n * (n - 1) // 2, 2)), X=MZICrossingOutPhase(),
+                                              is_phase=False), 3)
+    # a clipped network: SquareNetwork (square.py) over its full diamond mesh, ClippedNetwork.dot and grad_L2
+    net = SquareNetwork(N=3)
+    full = net.full
+    randomise(full)
+    net.p_phase, net.p_splitter = full.p_phase, full.p_splitter
+    x = rng.standard_normal((net.N, 2)) + 1j * rng.standard_normal((net.N, 2))
+    y = net.dot(x)
+    Z = rng.standard_normal((net.M, net.N)) + 1j * rng.standard_normal((net.M, net.N))
+    J, dJdp = net.grad_L2(Z)
+    save("converter_squarenet_N3", **attrs(full, "full_"), net_class="SquareNetwork",
+         idx_in=np.arange(full.N)[net.idx_in], idx_out=np.arange(full.N)[net.idx_out], x=x, y=y, U_target=Z, J=J,
+         dJdp=dJdp, p_phase=full.p_phase)
 
 
 if __name__ == "__main__":
