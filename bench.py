@@ -868,6 +868,13 @@ def run_plain_forward(args, peak):
     x_h = unit_rows(rng, bc, nc)
     x = torch.from_numpy(x_h).to(dev).t()                 # (N, B) columns, the reference's layout
     out = torch.empty_like(x)
+    if args.profile:
+        # three untimed calls (for ncu launch lists of one call: coefficient pass, propagation, gaps)
+        for _ in range(3):
+            m.dot(x, out=out)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_calls": 3, "status": m.status()}))
+        return None
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     with ClockSampler(gpu_id(torch, dev)) as cs:
         t = event_ms(torch, lambda: m.dot(x, out=out), max(20, min(args.steps * 10, 200)), warm=max(3, args.warmup),

@@ -76,7 +76,7 @@ class MeshFunction(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x: torch.Tensor, p: torch.Tensor, mesh: MeshNetworkGPU):
         lib = load()
-        x = x.contiguous()
+        x = x.resolve_conj().resolve_neg().contiguous()
         p = p.detach().to(torch.float32).contiguous()
         B, N = x.shape
         assert N == mesh.N, "x must be (B, N) with N=%d" % mesh.N
@@ -101,7 +101,7 @@ class MeshFunction(torch.autograd.Function):
         y, p = ctx.saved_tensors
         mesh = ctx.mesh
         B, N = y.shape
-        gy = gy.contiguous()
+        gy = gy.resolve_conj().resolve_neg().contiguous()
         plan_ = _plans(mesh)[OP_BWD]
         if ctx.tiles_version is not None and getattr(plan_, "version", None) == ctx.tiles_version:
             ws, nb = plan_.workspace(B)               # tiles of this forward are still in place

@@ -107,6 +107,7 @@ struct Plan {
   int M, V, W, CL, S, G, logG, R, np2, grid;
   bool split;   // two CTA kinds per SM (V and V-1 vectors per lane group), CTAs [0, nA) the first kind
   int nA;
+  bool pair;    // warp-pair launch: a vector over two warps (4 modes per lane), V vectors per pair
   unsigned lb, dlb;
   size_t smem;
   size_t off_kinds, off_tiles, off_dtiles, off_partial, total;
@@ -182,7 +183,15 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
     V = wide ? ((op == OP_BWD && p.real) ? 2 : vw[op]) : stored ? stored_default_v(OP_BWD, M) : vd[op][ilog2(M) - 1];
   }
   if (perm && stored) return fail(MG_E_ARG, "stored-activation back-propagation takes no permutations");
-  if (wide ? (perm || stored || !wide_instantiated(op, crossing == CR_ORTH, V, p.gr))
+  // warp-pair launch (split 3): back-propagation of a nearest-neighbour complex mesh with a full-warp M = 8 plan
+  const int split_mode = cfg ? cfg->split : 0;
+  p.pair = split_mode == 3;
+  if (p.pair) {
+    if (!(cfg && cfg->V)) V = 7;
+    if (stored || perm || geometry != GEO_NN || G != 32 || !pair_instantiated(op, crossing == CR_ORTH, M, V, p.gr, true))
+      return fail(MG_E_CONFIG, "no warp-pair kernel for op=%d crossing=%d geometry=%d M=%d G=%d V=%d", op, crossing,
+                  geometry, M, G, V);
+  } else if (wide ? (perm || stored || !wide_instantiated(op, crossing == CR_ORTH, V, p.gr))
            : perm ? !perm_instantiated(op, crossing == CR_ORTH, M, V, p.gr)
                   : (stored ? !instantiated_stored(OP_BWD, M, V) : !instantiated(op, M, V)))
     return fail(MG_E_CONFIG, "no %skernel instantiated for op=%d M=%d V=%d",
@@ -194,10 +203,9 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   // N=256, B=4096 it saves 5% there, while back-propagation gets 28% slower: its two bodies (V and
   // V-1, ~25 KB of code each) overflow the instruction cache together (ncu: instruction-fetch stalls
   // 17x those of the uniform launch).
-  const int split_mode = cfg ? cfg->split : 0;
   p.split = false;
   p.nA = 0;
-  if (split_mode != 2 && (op == OP_FWD || op == OP_BWD) && V >= 2 && !stored && !perm &&
+  if (split_mode != 2 && !p.pair && (op == OP_FWD || op == OP_BWD) && V >= 2 && !stored && !perm &&
       split_instantiated(op, crossing == CR_ORTH, M, V, G == 32, p.gr)) {
     const long ws = (cfg && cfg->W) ? cfg->W : 4;
     const long capA = ws * p.R * V, capB = ws * p.R * (V - 1);
@@ -211,7 +219,8 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   const int gslot = (op != OP_BWD) ? 0 : ((p.gr == 1 || p.gr == 2) ? 8 : (p.real ? 16 : 32));
   const size_t gstl = (size_t)p.np2 * gslot;
   const int maxw = prop_max_threads(op, M, V) / 32;
-  int W = (cfg && cfg->W) ? cfg->W : (p.split ? 4 : 0);
+  int W = (cfg && cfg->W) ? cfg->W : (p.split ? 4 : p.pair ? 8 : 0);
+  if (p.pair && (W & 1)) return fail(MG_E_CONFIG, "a warp-pair launch needs an even W, got %d", W);
   if (!W) {
     // enough warps to cover the batch in one wave, rounded up to a multiple of 4 so the four
     // schedulers of an SM carry equal work (measured: 8 warps on 128 SMs beat 7 warps on 147)
@@ -245,7 +254,7 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   if (p.lb % 16 || p.dlb % 16) return fail(MG_E_CONFIG, "tile sizes %u/%u not multiples of 16 bytes", p.lb, p.dlb);
   if ((size_t)CL * p.lb >= (1u << 20) || (size_t)CL * p.dlb >= (1u << 20))
     return fail(MG_E_CONFIG, "one pipeline stage exceeds the 1 MB bulk-copy limit");
-  const long per_cta = (long)W * p.R * V;
+  const long per_cta = p.pair ? (long)(W / 2) * V : (long)W * p.R * V;
   p.grid = (int)((B + per_cta - 1) / per_cta);
   if (p.split) {
     const long capB = (long)W * p.R * (V - 1);
@@ -367,7 +376,9 @@ int run_prop(const Plan& P, const void* in0, const void* in1, void* out0, void* 
   lc.stream = st;
   cudaError_t e;
   a.nA = P.nA;
-  if (P.M == kWideM)
+  if (P.pair)
+    e = launch_prop_pair(P.V, lc, a);
+  else if (P.M == kWideM)
     e = launch_prop_wide(P.op, P.real, P.V, P.gr, lc, a);
   else if (!P.perm && P.geometry == GEO_NN && nn_instantiated(P.op, P.real, P.M, P.V, P.gr, P.G == 32, P.split))
     e = launch_prop_nn(P.op, P.real, P.M, P.V, P.gr, P.G == 32, P.split, lc, a);
@@ -688,7 +699,7 @@ int mg_propagate(int op, int N, int L, int B, int crossing, int geometry, const 
     Plan Pb, Pf;
     TRY(make_plan(OP_BWD, N, L, B, crossing, geometry, cfg, &Pb));
     TRY(check_ws(Pb, ws, wsb));
-    mg_config cf = {Pb.M, 0, 0, 0, 0, cfg ? cfg->split : 0};
+    mg_config cf = {Pb.M, 0, 0, 0, 0, (cfg && cfg->split != 3) ? cfg->split : 0};
     mg_config tf;   // a measured forward configuration of this shape applies if its M matches the tiles'
     if (!cfg && !Pb.perm && lookup_tuned(OP_FWD, crossing, Pb.geometry, N, B, &tf) && tf.M == Pb.M) cf = tf;
     TRY(make_plan(OP_FWD, N, L, B, crossing, geometry, &cf, &Pf));

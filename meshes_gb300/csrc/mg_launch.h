@@ -82,6 +82,10 @@ cudaError_t launch_prop_nn(int op, bool real, int M, int V, int gr, bool full, b
 constexpr int kWideM = 20;
 bool wide_instantiated(int op, bool real, int V, int gr);
 cudaError_t launch_prop_wide(int op, bool real, int V, int gr, const LaunchCfg& lc, const PropArgs& a);
+// warp-pair back-propagation (mg_prop_pair.cu): a vector over the 64 lanes of two warps, 4 modes per lane, on
+// the tiles of an M = 8, G = 32 plan; V counts vectors per pair
+bool pair_instantiated(int op, bool real, int M, int V, int gr, bool full);
+cudaError_t launch_prop_pair(int V, const LaunchCfg& lc, const PropArgs& a);
 // split launches (two CTA kinds per SM); instantiated only for the full-warp configurations in
 // split_instantiated()
 bool split_instantiated(int op, bool real, int M, int V, bool full, int gr);

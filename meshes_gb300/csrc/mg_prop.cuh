@@ -312,7 +312,7 @@ struct Lanes {
 // forward up to 16% faster.
 template <int OP, int M, int V, bool REAL, int GR, bool PK, typename UA, typename UB, typename WA, typename WB>
 __device__ __forceinline__ void crossing(const float4* tl, int doff, int e, int G, int j, int r, UA ua, UB ub, WA wa,
-                                         WB wb, float4* gl) {
+                                         WB wb, float4* gl, bool store = true) {
   using CT = typename Fld<REAL>::C;
   CT t, d, acc;
   ld_coef(tl, e, G, j, t);
@@ -336,7 +336,7 @@ __device__ __forceinline__ void crossing(const float4* tl, int doff, int e, int 
 #pragma unroll
       for (int v = 0; v < V; ++v) x_bwd_direct(t, cs, ua(v), ub(v), wa(v), wb(v), ath, aph);
     }
-    acc2_stage(reinterpret_cast<float2*>(gl), e * G + j, G, r, ath, aph, true);
+    acc2_stage(reinterpret_cast<float2*>(gl), e * G + j, G, r, ath, aph, store);
   } else if constexpr (PK && MG_PACKED_CROSSINGS && OP == OP_FWD && !REAL && V >= 2 && M >= 4 && M * V >= 16) {
     // (smaller forward tiles keep the one-vector form: the coefficient pairs made them spill; measured on
     // GB300 at N = 32 and 64: 7% slower)

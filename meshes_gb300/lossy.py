@@ -78,7 +78,7 @@ class GenericMZIT(torch.autograd.Function):
     @staticmethod
     def backward(ctx, gT: torch.Tensor):
         p64, s64 = ctx.saved_tensors
-        g = gT.detach().to(torch.complex64).contiguous()
+        g = gT.detach().to(torch.complex64).resolve_conj().resolve_neg().contiguous()
         dp = torch.empty_like(p64)
         check(load().mg_generic_mzi_T_vjp(p64.numel() // 2, p64.data_ptr(), s64.data_ptr() if s64.numel() else None,
                                           g.data_ptr(), dp.data_ptr(), _stream(p64.device)), "mg_generic_mzi_T_vjp")
@@ -197,8 +197,8 @@ class LossyMeshFunction(torch.autograd.Function):
     def forward(ctx, x: torch.Tensor, T: torch.Tensor, mesh: LossyMesh):
         assert x.dim() == 2 and x.shape[1] == mesh.N, "x must be (B, N) with N=%d" % mesh.N
         assert tuple(T.shape) == (mesh.L, mesh.N // 2, 2, 2), "T must be (L, N/2, 2, 2)"
-        x = x.detach().to(device=mesh.device, dtype=torch.complex64).contiguous()
-        Tc = T.detach().to(device=mesh.device, dtype=torch.complex64).contiguous()
+        x = x.detach().to(device=mesh.device, dtype=torch.complex64).resolve_conj().resolve_neg().contiguous()
+        Tc = T.detach().to(device=mesh.device, dtype=torch.complex64).resolve_conj().resolve_neg().contiguous()
         B, L = x.shape[0], mesh.L
         seg = mesh.segment_for(B)
         K = -(-L // seg)
@@ -220,7 +220,7 @@ class LossyMeshFunction(torch.autograd.Function):
         mesh = ctx.mesh
         Tc, x, ckpt = ctx.saved_tensors
         B, N, L, seg = x.shape[0], mesh.N, mesh.L, ctx.seg
-        gy = gy.detach().to(torch.complex64).contiguous()
+        gy = gy.detach().to(torch.complex64).resolve_conj().resolve_neg().contiguous()
         dT = torch.zeros((L, N // 2, 2, 2), dtype=torch.complex64, device=mesh.device)
         g = torch.empty_like(gy)
         if B > 0:
@@ -304,7 +304,7 @@ class GenericMeshGPU:
         v = v if isinstance(v, torch.Tensor) else torch.as_tensor(np.asarray(v))
         v = v.to(device=self.device)
         assert v.dim() == 2 and v.shape[0] == self.N, "v must be (N, B) with N=%d" % self.N
-        return v.t().to(torch.complex64).contiguous()
+        return v.t().to(torch.complex64).resolve_conj().resolve_neg().contiguous()
 
     def _args(self, p_phase, p_splitter):
         p = self.p_phase if p_phase is None else self._param(p_phase).reshape(-1)

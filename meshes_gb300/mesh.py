@@ -152,7 +152,9 @@ class MeshNetworkGPU:
         """(N, B) input -> (tensor whose column b starts at data_ptr + b*ldu elements, ldu)."""
         if not isinstance(v, torch.Tensor):
             v = torch.as_tensor(np.asarray(v))
-        v = v.to(device=self.device, dtype=self.dtype)
+        # a lazily conjugated or negated view (torch's conj/neg bits, e.g. U.t().conj()) is materialised: the
+        # kernels read the memory behind data_ptr, which holds the unconjugated values
+        v = v.to(device=self.device, dtype=self.dtype).resolve_conj().resolve_neg()
         assert v.dim() == 2 and v.shape[0] == self.N, "v must be (N, B) with N=%d" % self.N
         align = 8 if self.X == "orth" else 16
         if (v.stride(0) == 1 and (v.shape[1] == 1 or (v.stride(1) >= self.N and v.stride(1) % 2 == 0))

@@ -505,3 +505,22 @@ def test_golden_clipped_mesh(name):
     dp = dp.cpu().numpy()
     assert O.rel_err(dp[:ncp].reshape(L, N // 2, 2), z["dJdp"]) < TOL
     assert O.rel_err(dp[ncp:], z["dJdph"]) < TOL
+
+
+def test_conjugated_and_negated_views():
+    """Inputs that are lazily conjugated or negated views (torch's conj/neg bits) give the results of their
+    materialised values: the library reads raw memory, so such views are resolved before a call."""
+    rng = np.random.default_rng(77)
+    om = O.random_mesh(rng, 16, "clements", "mzi", 0.02)
+    m = gpu_mesh(om)
+    U = torch.tensor(O.haar_unitary(rng, 16).astype(np.complex64), device="cuda")
+    v = U.t().conj()
+    assert v.is_conj()
+    ref = m.dot(v.resolve_conj())
+    assert torch.equal(m.dot(v), ref)
+    y = O.propagate(om, U.t().conj().t().cpu().numpy())
+    assert O.rel_err(to_np(m.dot(v)), y) < TOL
+    g = torch.tensor(O.unit_columns(rng, 16, 16).astype(np.complex64), device="cuda").t()
+    dp1, g1 = m.grad_phi(v, g.conj())
+    dp2, g2 = m.grad_phi(v.resolve_conj(), g.conj().resolve_conj())
+    assert torch.equal(dp1, dp2) and torch.equal(g1, g2)
