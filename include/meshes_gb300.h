@@ -343,6 +343,20 @@ int mg_lossy_backward(int N, int L, int B, int geometry, int seg, const void* x,
 int mg_generic_mzi_T(int n, const double* p, const double* s, void* T, void* stream);
 int mg_generic_mzi_T_vjp(int n, const double* p, const double* s, const void* gT, double* dp, void* stream);
 
+/* ---- self-configuration ----------------------------------------------------------------------
+ * The nulling pass of the matrix-diagonalisation method (reference configure.py:187-330, diag and its
+ * diagHelper_fn), host code in double precision.  U (target), Z (product of the meshes' matrices at their
+ * starting phases), VdV and WWd (identity on entry) are N x N complex128 row-major, updated in place and returned
+ * in the transposed-or-not form the reference's pass leaves them in.  ijzp: K steps (i, j, ind, p) - zero
+ * element (i, j) with MZI ind of the left (p = 0, n1 MZIs) or right (p = 1, n2 MZIs) mesh; s1/s2 (n x 2)
+ * splitting errors, c1/c2 (n x 2) (theta, phi) updated in place; type 0 = MZI crossing, 1 = its flipped form
+ * (phase shifter at the output); init (K x 2) line-search starting points; noise (K x 2) added to each
+ * programmed MZI, or NULL; improved selects the reference's improved updates.  Returns MG_E_ARG (nothing
+ * changed) when a step points outside the matrices or meshes.  Does not touch the GPU. */
+int mg_diag_configure(int N, int K, void* U, void* Z, void* VdV, void* WWd, int n1, const double* s1, double* c1,
+                      int type1, int n2, const double* s2, double* c2, int type2, const int* ijzp, const double* init,
+                      const double* noise, int improved);
+
 /* ---- measurement helpers -------------------------------------------------------------------- */
 
 /* FP32 FMA throughput probe: `blocks` x `threads` threads each run `iters` iterations of 64

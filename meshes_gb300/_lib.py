@@ -115,6 +115,8 @@ _SIGS = {
     "mg_generic_mzi_T_vjp": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "mg_propagate_wait_test": (c_int, [c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                        c_int, c_ulonglong, c_int, c_void_p, c_size_t, c_void_p]),
+    "mg_diag_configure": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_int,
+                                  c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_int]),
     "mg_fma_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
     "mg_fma2_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
     "mg_trig_check": (c_int, [c_void_p, c_void_p, c_int, c_void_p]),

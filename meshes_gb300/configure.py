@@ -1,0 +1,251 @@
+"""Self-configuration of MZI meshes by matrix diagonalisation (reference configure.py:187-330, ``diag``).
+
+``diag(m1, m2, phi_diag, U, nm, nn, ijxyp, improved)`` programs a left mesh m1 and a right mesh m2 (either may
+be None) and a diagonal phase screen so that they realise the target U, with the reference's arguments:
+``nm`` groups of ``nn(m)`` nulling steps, ``ijxyp(m, n)`` giving the matrix element (i, j) that step n of
+group m zeroes, the MZI at layer x and top mode y that does it and the mesh p (0: m1, 1: m2), and
+``improved`` selecting the reference's improved update (``diag*``).  The meshes are ``MeshNetworkGPU``
+objects with MZI crossings (nearest-neighbour layers); their phases are written in place.
+
+Work split:
+  * the meshes' matrices at their random starting phases are evaluated on the GPU by the propagation
+    kernels (the columns of the running product Z propagated through each mesh: ``Z = m.dot(Z)``);
+  * the nulling pass itself - one MZI at a time, each step a 10-iteration line search on a 2x2 problem and an
+    update of two rows of N x N matrices - is sequential and O(N) per step, and runs natively on the host in
+    double precision (``mg_diag_configure`` in libmeshes_gb300, the counterpart of the reference's
+    JIT-compiled helper).
+
+Random draws follow the reference's order on NumPy's global generator (``np.random.rand`` for each mesh's
+starting phi, ``np.random.randint`` for the line-search starting points, ``np.random.randn`` for the
+programming noise ``sigp``), so a seeded call reproduces the reference's programmed phases.
+
+``reck(U, ...)`` and ``diag_reck(mesh, U, improved)`` are the Reck entry points (reference reck.py:68-72,
+146-164, ``ReckNetwork(M=U, method='diag' | 'diag*')``); ``square(M, ...)`` programs a SquareNet
+(square.py:77-101, ``SquareNetwork(M=M, method='diag')``) into a clipped mesh.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Callable, Optional
+
+import numpy as np
+import torch
+
+from . import geometry as geom
+from ._lib import check, load
+from .mesh import MeshNetworkGPU
+
+# line-search starting points of the MZI crossings (configure.py:176-182): (pi/2, 0) or (-pi/2, 0)
+INIT_P, INIT_M = np.array([np.pi / 2, 0.0]), np.array([-np.pi / 2, 0.0])
+_c_double_p = ctypes.POINTER(ctypes.c_double)
+
+
+def _flat_layout(lens, shifts):
+    """(layer, slot) of every MZI in the reference's flat order (layer by layer, top to bottom)."""
+    lay = np.concatenate([np.full(ln, l) for l, ln in enumerate(lens)]).astype(np.int64) if sum(lens) else np.zeros(0, np.int64)
+    slot = np.concatenate([sh // 2 + np.arange(ln) for ln, sh in zip(lens, shifts)]).astype(np.int64) if sum(lens) else lay
+    return lay, slot
+
+
+def diag_steps(geo1, geo2, nm: int, nn: Callable, ijxyp: Callable):
+    """The steps (i, j, ind, p) of the nulling pass (configure.py:221-225); geo = (lens, shifts) of m1 and m2
+    (empty for a missing mesh).  Returns ijzp (K, 4) int32 and the layer/mode arrays x, y."""
+    i, j, x, y, r = np.concatenate([np.array(ijxyp(np.repeat(m, nn(m)), np.arange(nn(m)))) for m in range(nm)], 1)
+    i1, s1 = np.cumsum([0] + list(geo1[0])), np.array(geo1[1], dtype=np.int64)
+    i2, s2 = np.cumsum([0] + list(geo2[0])), np.array(geo2[1], dtype=np.int64)
+    L2 = len(geo2[0])
+    w1, w2 = np.where(1 - r)[0], np.where(r)[0]
+    x1, y1, x2, y2 = x[w1], y[w1], x[w2] + L2 - 1, y[w2]
+    ind = x * 0
+    ind[w1] = i1[x1] + (y1 - s1[x1]) // 2
+    ind[w2] = i2[x2] + (y2 - s2[x2]) // 2
+    return np.ascontiguousarray(np.array([i, j, ind, r]).T, dtype=np.int32), x, y
+
+
+def diag_init(init, x, y, K: int) -> np.ndarray:
+    """Line-search starting points per step (configure.py:227-232): init is 'rand', 'uniform' or a callable
+    of (x, y) giving 1 (start at +pi/2) or 0 (start at -pi/2) per step."""
+    if callable(init):
+        init = init(x, y)
+    elif isinstance(init, str) and init == "rand":
+        init = np.random.randint(0, 2, K)
+    elif isinstance(init, str) and init == "uniform":
+        init = np.ones(K, dtype=int)
+    else:
+        raise ValueError(init)
+    init = np.asarray(init)
+    if init.ndim == 1:
+        init = np.outer(init, INIT_P) + np.outer(1 - init, INIT_M)
+    return np.ascontiguousarray(init, dtype=np.float64)
+
+
+def diag_core(U, Z, s1, c1, s2, c2, ijzp, init, noise, improved: bool, type1: int = 0, type2: int = 1):
+    """The nulling pass on the host (mg_diag_configure) from the starting product Z of the meshes' matrices.
+    c1, c2 ((n, 2) float64 (theta, phi) in the reference's flat order) are updated in place; returns
+    (U, VdV, WWd) as the pass leaves them and the diagonal phases phi_diag (configure.py:246)."""
+    N = U.shape[0]
+    Ub = np.array(U, dtype=np.complex128, order="C")
+    Zb = np.array(Z, dtype=np.complex128, order="C")
+    VdV = np.eye(N, dtype=np.complex128)
+    WWd = np.eye(N, dtype=np.complex128)
+    s1 = np.ascontiguousarray(s1, dtype=np.float64).reshape(-1, 2)
+    s2 = np.ascontiguousarray(s2, dtype=np.float64).reshape(-1, 2)
+    assert c1.dtype == np.float64 and c1.flags.c_contiguous and c2.dtype == np.float64 and c2.flags.c_contiguous
+    assert len(s1) == len(c1) and len(s2) == len(c2)
+    ijzp = np.ascontiguousarray(ijzp, dtype=np.int32)
+    init = np.ascontiguousarray(init, dtype=np.float64)
+    noise_p = None if noise is None else np.ascontiguousarray(noise, dtype=np.float64)
+    lib = load()
+    ptr = lambda a: None if a is None else a.ctypes.data
+    check(lib.mg_diag_configure(N, len(ijzp), ptr(Ub), ptr(Zb), ptr(VdV), ptr(WWd), len(c1), ptr(s1), ptr(c1), type1,
+                                len(c2), ptr(s2), ptr(c2), type2, ptr(ijzp), ptr(init), ptr(noise_p), int(improved)),
+          "mg_diag_configure")
+    phi_diag = np.angle(np.diag(Ub)) - np.angle(np.sum(VdV * WWd.T, axis=1))
+    return Ub, VdV, WWd, phi_diag
+
+
+def _mesh_state(m: Optional[MeshNetworkGPU]):
+    """(lens, shifts), flat layout and flat splitters (n, 2) float64 of a mesh (empty for None)."""
+    if m is None:
+        return ([], []), (np.zeros(0, np.int64), np.zeros(0, np.int64)), np.zeros((0, 2))
+    if m.X != "mzi" or m.geometry != geom_nn():
+        raise ValueError("self-configuration programs nearest-neighbour meshes of MZI crossings")
+    if m.perm_table is not None:
+        raise ValueError("self-configuration takes meshes without permutations")
+    lay, slot = _flat_layout(m.lens_h, m.shifts_h)
+    sp = m.p_splitter
+    s = (sp.detach().double().cpu().numpy()[lay, slot] if sp.numel() else np.zeros((len(lay), 2)))
+    return (m.lens_h, m.shifts_h), (lay, slot), s
+
+
+def geom_nn():
+    from ._lib import GEO_NN
+    return GEO_NN
+
+
+def _set_phases(m: MeshNetworkGPU, layout, c: np.ndarray):
+    """Write flat (theta, phi) into the mesh's grid (zeros in inactive slots); a phase screen is set to 0."""
+    lay, slot = layout
+    grid = np.zeros((m.L, m.N // 2, 2))
+    grid[lay, slot] = c
+    new = np.concatenate([grid.reshape(-1), np.zeros(m.N if m.is_phase else 0)])
+    m.p_phase.copy_(torch.as_tensor(new, dtype=torch.float32))
+
+
+def _set_screen(m: MeshNetworkGPU, phi):
+    m.p_phase[m.L * (m.N // 2) * 2:].copy_(torch.as_tensor(np.asarray(phi), dtype=torch.float32))
+
+
+def diag(m1: Optional[MeshNetworkGPU], m2: Optional[MeshNetworkGPU], phi_diag, U, nm: int, nn: Callable,
+         ijxyp: Callable, improved: bool, sigp: float = 0.0, init="rand"):
+    """Program m1 (left), m2 (right) and the diagonal phases phi_diag (written in place) to realise U; the
+    reference's diag (configure.py:187-246), see the module docstring."""
+    assert m1 is not None or m2 is not None
+    U = np.asarray(U, dtype=np.complex128)
+    N = (m1 or m2).N
+    assert U.shape == (N, N)
+    geo1, lay1, s1 = _mesh_state(m1)
+    geo2, lay2, s2 = _mesh_state(m2)
+    dev = (m1 or m2).device
+    # starting point: theta = 0, phi uniform random, no screen; Z = M2 M1 evaluated on the GPU
+    c = []
+    Zd = torch.eye(N, dtype=torch.complex64, device=dev)
+    for m, lay in ((m1, lay1), (m2, lay2)):
+        n = len(lay[0])
+        cm = np.zeros((n, 2))
+        cm[:, 1] = 2 * np.pi * np.random.rand(n)
+        c.append(cm)
+        if m is not None:
+            _set_phases(m, lay, cm)
+            Zd = m.dot(Zd)
+    Z = Zd.cpu().numpy().astype(np.complex128)
+    ijzp, x, y = diag_steps(geo1, geo2, nm, nn, ijxyp)
+    init_arr = diag_init(init, x, y, len(ijzp))
+    noise = np.random.randn(len(ijzp), 2) * sigp          # drawn as the reference draws it, one pair per step
+    _, _, _, ph = diag_core(U, Z, s1, c[0], s2, c[1], ijzp, init_arr, noise if sigp else None, improved)
+    for m, lay, cm in ((m1, lay1, c[0]), (m2, lay2, c[1])):
+        if m is not None:
+            _set_phases(m, lay, cm)
+    if isinstance(phi_diag, torch.Tensor):
+        phi_diag.copy_(torch.as_tensor(ph, dtype=phi_diag.dtype))
+    else:
+        phi_diag[:] = ph
+    return ph
+
+
+def reck_steps(N: int):
+    """nn and ijxyp of the Reck mesh with its screen at the output (reference reck.py:155-160)."""
+    def nn(m):
+        return N - 1 - m
+
+    def ijxyp(m, n):
+        return [m, N - 1 - n, m * 2 + n, N - 2 - n, m * 0]
+    return nn, ijxyp
+
+
+def diag_reck(mesh: MeshNetworkGPU, U, improved: bool = True, sigp: float = 0.0, init="rand"):
+    """Program a Reck MeshNetworkGPU (screen at the output) to realise U (reference diagReck, reck.py:146-160):
+    its crossing phases and its phase screen are written in place."""
+    N = mesh.N
+    if not (mesh.is_phase and mesh.phi_pos == "out"):
+        raise ValueError("the Reck diagonalisation programs a mesh with its phase screen at the output")
+    nn, ijxyp = reck_steps(N)
+    phi = np.zeros(N)
+    diag(mesh, None, phi, U, N - 1, nn, ijxyp, improved, sigp, init)
+    _set_screen(mesh, phi)
+    return mesh
+
+
+def reck(U, p_splitter=0.0, improved: bool = True, sigp: float = 0.0, init="rand", device=None) -> MeshNetworkGPU:
+    """A Reck MeshNetworkGPU realising U (reference ReckNetwork(M=U, p_splitter=..., method='diag*' (improved)
+    or 'diag'), reck.py:68-72): p_splitter is a scalar or (N(N-1)/2, 2) splitting errors in the reference's
+    flat order."""
+    U = np.asarray(U, dtype=np.complex128)
+    N = U.shape[0]
+    lens, shifts = geom.reck(N)
+    lay = _flat_layout(lens, shifts)
+    s = np.zeros((len(lay[0]), 2)) + np.asarray(p_splitter, dtype=np.float64)
+    grid = np.zeros((len(lens), N // 2, 2))
+    grid[lay[0], lay[1]] = s
+    m = MeshNetworkGPU(N, len(lens), lens, shifts, np.zeros(len(lens) * (N // 2) * 2 + N), grid.astype(np.float32),
+                       "mzi", phi_pos="out", is_phase=True, device=device)
+    return diag_reck(m, U, improved, sigp, init)
+
+
+def square(M, p_splitter=0.0, eig: Optional[float] = None, improved: bool = False, init="rand", device=None):
+    """A SquareNet (square.py:22-101, SquareNetwork(M=M, method='diag'), screen at the output) realising the
+    (m, n) matrix M, returned as a ClippedMeshGPU over its (m + n)-mode diamond mesh, and the scale factor the
+    reference applies to M first (1, or sqrt(eig / max eigenvalue of M M^H) when eig is given)."""
+    from scipy.linalg import eigvalsh
+
+    from .clipped import ClippedMeshGPU
+    M11 = np.array(M, dtype=np.complex128)
+    m_out, n_in = M11.shape
+    Nf = m_out + n_in
+    shifts = np.abs(np.arange(-n_in + 1, m_out))
+    lens = (Nf - shifts - shifts[::-1]) // 2
+    MMt = M11 @ M11.conj().T
+    fact = np.sqrt(eig / eigvalsh(MMt, subset_by_index=[m_out - 1, m_out - 1])[0]) if eig else 1.0
+    MMt = MMt * fact ** 2
+    M11 = M11 * fact
+    M12 = np.linalg.cholesky(np.eye(m_out) - MMt)
+    U = np.zeros((Nf, Nf), dtype=np.complex128)
+    U[:m_out, :n_in] = M11
+    U[:m_out, n_in:] = M12
+    lay = _flat_layout(lens.tolist(), shifts.tolist())
+    s = np.zeros((len(lay[0]), 2)) + np.asarray(p_splitter, dtype=np.float64)
+    grid = np.zeros((len(lens), Nf // 2, 2))
+    grid[lay[0], lay[1]] = s
+    full = MeshNetworkGPU(Nf, len(lens), lens, shifts, np.zeros(len(lens) * (Nf // 2) * 2 + Nf),
+                          grid.astype(np.float32), "mzi", phi_pos="out", is_phase=True, device=device)
+
+    def nn(m):
+        return n_in
+
+    def ijxyp(m, n):
+        return [m, n_in + m - n, m + n, n_in - 1 + m - n, m * 0]
+
+    phi = np.zeros(Nf)
+    diag(full, None, phi, U, m_out, nn, ijxyp, improved, 0.0, init)
+    _set_screen(full, phi)
+    return ClippedMeshGPU(full, slice(n_in), slice(m_out)), fact

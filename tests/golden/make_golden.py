@@ -336,7 +336,42 @@ def main(ref_path):
              x=x, y=y, **extra)
 
     converter_cases(save)
+    configure_cases(save)
     print("wrote", *written, sep="\n  ")
+
+
+def configure_cases(save):
+    """The reference's own self-configuration by matrix diagonalisation (configure.py:187-330): a Reck mesh
+    programmed with ReckNetwork(M=U, method='diag*') and (method='diag'), and a SquareNet with
+    SquareNetwork(M=M, method='diag'), each from a recorded NumPy seed (diag draws its random start from
+    np.random).  Stored: the target, splitting errors (reference flat order), the seed, the programmed
+    crossing phases and output screen, and the programmed mesh's matrix.  Own seeded stream."""
+    from meshes.reck import ReckNetwork
+    from meshes.square import SquareNetwork
+
+    rng = np.random.default_rng(20261205)
+
+    def haar(n):
+        Z = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+        Q, R = np.linalg.qr(Z)
+        return Q * (np.diag(R) / np.abs(np.diag(R)))[None, :]
+
+    for name, n, method, seed in (("reck_diagstar_N8", 8, "diag*", 11), ("reck_diag_N8", 8, "diag", 12)):
+        U = haar(n)
+        sp = rng.normal(0, 0.02, (n * (n - 1) // 2, 2)).astype(np.float32).astype(np.float64)
+        np.random.seed(seed)
+        net = ReckNetwork(M=U, p_splitter=sp, method=method)
+        save("configure_" + name, N=n, method=method, seed=seed, U=U, p_splitter=sp, lens=np.array(net.lens),
+             shifts=np.array(net.shifts), p_crossing=np.array(net.p_crossing), phi_out=np.array(net.phi_out),
+             matrix=net.dot(np.eye(n, dtype=complex)))
+    n = 3
+    M = 0.8 * haar(n)
+    seed = 13
+    np.random.seed(seed)
+    net = SquareNetwork(M=M, method="diag")
+    save("configure_square_diag_N3", N=n, method="diag", seed=seed, M=M, lens=np.array(net.full.lens),
+         shifts=np.array(net.full.shifts), p_crossing=np.array(net.full.p_crossing),
+         phi_out=np.array(net.full.phi_out), matrix=net.dot(np.eye(n, dtype=complex)))
 
 
 def converter_cases(save):

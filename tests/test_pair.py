@@ -77,9 +77,10 @@ def test_pair_launch_matches_oracle_and_one_warp_launch(geo, N, B, V):
     xb, gb, db = _run(om, y, None, one, target=t)
     assert np.array_equal(xa, xb) and np.array_equal(ga, gb)
     assert O.rel_err(da, db) < 1e-6
-    # explicit upstream gradient instead of the fused L2 target
-    xc, gc, dc = _run(om, y, 2 * (y - t), pair)
-    assert np.array_equal(gc, ga) and O.rel_err(dc, dp_ref) < TOL
+    # explicit upstream gradient instead of the fused L2 target, formed in complex64 as the kernel forms it
+    g32 = 2 * (y.astype(np.complex64) - t.astype(np.complex64))
+    xc, gc, dc = _run(om, y, g32, pair)
+    assert np.array_equal(gc, ga) and np.array_equal(dc, da)
 
 
 def test_pair_launch_rejects_other_shapes():
