@@ -152,7 +152,8 @@ int mg_backdiff_ft(int N, int L, int B, const int* strides, const float* p, floa
  * it until exit); problems needing more return MG_E_WORKSPACE without launching.  The first call on
  * each device looks up the array's device address and should come before any stream capture.  All
  * calls share the array, so calls that overlap on the GPU race: serialise them.  Kernel status codes
- * are not reported by this entry point. */
+ * are not reported by this entry point.  The array's address is cached per device for the life of the
+ * process: do not call it again after cudaDeviceReset re-creates the device's context. */
 int mg_fwdprop_noalloc(int N, int L, int B, const int* lens, const int* shifts, const float* p, int ldp,
                        const float* s, int lds, const void* u_in, void* u_out, int ldu, int crossing, void* stream);
 
@@ -363,9 +364,10 @@ int mg_diag_configure(int N, int K, void* U, void* Z, void* VdV, void* WWd, int 
  * independent FMAs; writes one float per thread to `sink`.  Used by bench.py to measure the FP32
  * CUDA-core peak of the device it runs on. */
 int mg_fma_probe(float* sink, int blocks, int threads, int iters, void* stream);
-/* Self-check of the coefficient precompute's double-precision sin/cos: out[4i..4i+3] = the differences
- * (sin, cos)(x[i]) own - library for the full-precision version and for the tile-precision version (results
- * rounded to float32), for n device doubles x (used by the tests). */
+/* Self-check of the coefficient precompute's double-precision sin/cos: out[6i..6i+5] = the differences
+ * (sin, cos)(x[i]) own - library for the full-precision version, the tile-precision version (results rounded
+ * to float32) and the small-angle version used for splitting errors, for n device doubles x (used by the
+ * tests). */
 int mg_trig_check(const double* x, double* out, int n, void* stream);
 /* The same probe with packed FP32 pairs (fma.rn.f32x2, sm_100+): 128 FMAs per thread-iteration. */
 int mg_fma2_probe(float* sink, int blocks, int threads, int iters, void* stream);

@@ -540,19 +540,22 @@ __global__ void fma_probe_kernel(float* sink, int iters, float m) {
   sink[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
-// sincos_d and sincos_c (the coefficient precompute's own double sin/cos, full and tile precision)
-// against the library sincos
+// sincos_d, sincos_c and sincos_small (the coefficient precompute's own double sin/cos: full precision,
+// tile precision, small splitter angles) against the library sincos
 __global__ void trig_check_kernel(const double* x, double* out, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double s, c, s2, c2, s3, c3;
+  double s, c, s2, c2, s3, c3, s4, c4;
   sincos_d(x[i], &s, &c);
   sincos(x[i], &s2, &c2);
   sincos_c(x[i], &s3, &c3);
-  out[4 * i] = s - s2;
-  out[4 * i + 1] = c - c2;
-  out[4 * i + 2] = s3 - s2;
-  out[4 * i + 3] = c3 - c2;
+  sincos_small(x[i], &s4, &c4);
+  out[6 * i] = s - s2;
+  out[6 * i + 1] = c - c2;
+  out[6 * i + 2] = s3 - s2;
+  out[6 * i + 3] = c3 - c2;
+  out[6 * i + 4] = s4 - s2;
+  out[6 * i + 5] = c4 - c2;
 }
 
 // The same chains with packed FP32 pairs (one fma.rn.f32x2 = two FMAs per lane): whether the FMA pipe

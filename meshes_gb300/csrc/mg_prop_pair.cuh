@@ -2,14 +2,19 @@
 //
 // A plan with M = 8 modes per lane and a full warp per vector (G = 32, N in (128, 256]) stores its coefficient
 // tiles and gradient partials for 32 lanes of 8 modes.  The warp-pair launch reads the same tiles and writes the
-// same partials, but gives each lane 4 modes: lane jv = 32*h + lane of warp h of a pair owns modes
+// same partials, but gives each lane 4 modes: virtual lane jv in [0, 64) of a pair (32 per warp) owns modes
 // [4*jv, 4*jv + 4), and the pair holds V vectors.  With V = 7 a pair carries 3.5 vectors per warp, so every SM
 // scheduler (two warps) carries 7 vectors: at N = 256, B = 4096 the 147 CTAs of 4 pairs leave one scheduler
 // in 27 idle, where warps of 4 whole vectors (8 per scheduler) fill only 128 of the 152 SMs.
 //
 // Index map onto the M = 8 plan: slot q = 2*jv + e4 (e4 in {0, 1}) is the plan's entry e8 = 2*(jv & 1) + e4
 // of plan lane j32 = jv >> 1, so crossing() is called with (e8, G = 32, j32) and finds the tile rows, the
-// splitter coefficients and the staging position of the plan.
+// splitter coefficients and the staging position of the plan.  Lane L of warp h holds virtual lane
+// jv = 32*h + 2*(L & 15) + (L >> 4): lanes 0-15 the even, lanes 16-31 the odd virtual lanes, so that each
+// half-warp reads (and stages) one contiguous run of the plan's rows - with consecutive lanes on
+// consecutive virtual lanes, lanes 2k and 2k+1 would hit the same banks 2 KB apart on every load.  The
+// neighbouring virtual lanes are then lanes L + 16 / L - 15 (next) and L - 16 / L + 15 (previous), reached
+// with indexed shuffles.
 //
 // Odd-shift layers couple mode 3 of lane jv with mode 0 of lane jv + 1.  Inside a warp this is the shuffle
 // pair of layer_mis.  Across the pair boundary (lane 31 of warp 0, lane 0 of warp 1) both lanes compute that
@@ -25,6 +30,14 @@
 #include "mg_prop.cuh"
 
 namespace mg {
+
+// virtual lane of lane L in warp h of a pair, and the lanes holding the next / previous virtual lane
+__device__ __forceinline__ int pair_jv(int h, int lane) { return 32 * h + 2 * (lane & 15) + (lane >> 4); }
+__device__ __forceinline__ int pair_next_lane(int lane) { return lane < 16 ? lane + 16 : lane - 15; }
+__device__ __forceinline__ int pair_prev_lane(int lane) { return lane >= 16 ? lane - 16 : lane + 15; }
+__device__ __forceinline__ float2 shfl_idx(float2 v, int src) {
+  return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
 
 // named barrier over the two warps of pair `pair` (barrier 0 is __syncthreads)
 __device__ __forceinline__ void pair_sync(int pair) {
@@ -47,7 +60,8 @@ __device__ __forceinline__ void pair_local(const float4* tl, int jv, F (&u)[V][4
 template <int OP, int V, typename F>
 __device__ __forceinline__ void pair_mis(const float4* tl, int h, int lane, F (&u)[V][4], F (&w)[V][4], float4* gl,
                                          F* mine, const F* theirs, int pair) {
-  const int jv = 32 * h + lane;
+  const int jv = pair_jv(h, lane);
+  const int nxt = pair_next_lane(lane), prv = pair_prev_lane(lane);
   const int j32 = jv >> 1, eb = 2 * (jv & 1);
   // publish the boundary modes for the other warp of the pair
   if (h == 0 && lane == 31) {
@@ -69,8 +83,8 @@ __device__ __forceinline__ void pair_mis(const float4* tl, int h, int lane, F (&
   if (h == 0) {
 #pragma unroll
     for (int v = 0; v < V; ++v) {
-      nb[v] = shfl_down(u[v][0], 1, 32);
-      nbw[v] = shfl_down(w[v][0], 1, 32);
+      nb[v] = shfl_idx(u[v][0], nxt);
+      nbw[v] = shfl_idx(w[v][0], nxt);
     }
     if (lane == 31) {
 #pragma unroll
@@ -82,8 +96,8 @@ __device__ __forceinline__ void pair_mis(const float4* tl, int h, int lane, F (&
   } else {
 #pragma unroll
     for (int v = 0; v < V; ++v) {
-      nb[v] = shfl_up(u[v][3], 1, 32);
-      nbw[v] = shfl_up(w[v][3], 1, 32);
+      nb[v] = shfl_idx(u[v][3], prv);
+      nbw[v] = shfl_idx(w[v][3], prv);
     }
     if (lane == 0) {
 #pragma unroll
@@ -104,7 +118,7 @@ __device__ __forceinline__ void pair_mis(const float4* tl, int h, int lane, F (&
         [&](int v) -> F& { return w[v][3]; }, [&](int v) -> F& { return nbw[v]; }, gl);
 #pragma unroll
     for (int v = 0; v < V; ++v) {
-      const F bu = shfl_up(nb[v], 1, 32), bw = shfl_up(nbw[v], 1, 32);
+      const F bu = shfl_idx(nb[v], prv), bw = shfl_idx(nbw[v], prv);
       if (lane != 0) {
         u[v][0] = bu;
         w[v][0] = bw;
@@ -120,7 +134,7 @@ __device__ __forceinline__ void pair_mis(const float4* tl, int h, int lane, F (&
         gl, lane != 0);
 #pragma unroll
     for (int v = 0; v < V; ++v) {
-      const F bu = shfl_down(nb[v], 1, 32), bw = shfl_down(nbw[v], 1, 32);
+      const F bu = shfl_idx(nb[v], nxt), bw = shfl_idx(nbw[v], nxt);
       if (lane != 31) {
         u[v][3] = bu;
         w[v][3] = bw;
@@ -139,7 +153,7 @@ __device__ __forceinline__ void prop_pair_body(const PropArgs& a, unsigned char*
   constexpr int OP = OP_BWD;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int h = warp & 1, pair = warp >> 1, npair = a.W >> 1;
-  const int jv = 32 * h + lane;
+  const int jv = pair_jv(h, lane);
   const int np2 = 128;                       // plan slots per layer (G = 32, M = 8)
   const int vb0 = a.v0 + pair * V;
 

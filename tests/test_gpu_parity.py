@@ -43,7 +43,7 @@ def to_np(t):
 def fixtures():
     """Fixtures of the plain meshes (the phase-screen and lossy fixtures have their own tests)."""
     return sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz") and "_screen_" not in f and "lossy" not in f
-                  and not f.startswith(("clipped_", "perm_", "piloss_", "xmesh_", "crossings_", "converter_")))
+                  and not f.startswith(("clipped_", "perm_", "piloss_", "xmesh_", "crossings_", "converter_", "configure_")))
 
 
 def load_fixture(name):
@@ -471,19 +471,26 @@ def test_packed_crossing_tiles(N, M, V):
 def test_coefficient_trigonometry_matches_library():
     """The coefficient precompute's own double sin/cos (Cody-Waite reduction + Taylor series) agrees with
     the CUDA library's to a few units in the last place, over phase-like, small and large arguments; its
-    tile-precision version (values rounded to float32 afterwards) to 1e-13."""
+    tile-precision version (values rounded to float32 afterwards) and its small-angle version for splitting
+    errors (|x| < 1/8 by series, other arguments through the tile version, NaN passed through) to 1e-13."""
     from meshes_gb300 import _lib
     lib = _lib.load()
     rng = np.random.default_rng(77)
     x = np.concatenate([rng.uniform(0, 2 * np.pi, 20000), rng.uniform(-20, 20, 20000),
                         rng.normal(0, 0.02, 20000), rng.uniform(-1e5, 1e5, 5000),
+                        rng.uniform(-0.125, 0.125, 20000), np.nextafter(0.125, 0) * np.array([1.0, -1.0]),
                         np.arange(-64, 65) * np.pi / 4, [0.0, 1e-30, -1e-30, 0.125, -0.125, 2.0 ** 20, 3e7]])
     xd = torch.tensor(x, dtype=torch.float64, device="cuda")
-    out = torch.empty(4 * x.size, dtype=torch.float64, device="cuda")
+    out = torch.empty(6 * x.size, dtype=torch.float64, device="cuda")
     assert lib.mg_trig_check(xd.data_ptr(), out.data_ptr(), x.size, torch.cuda.current_stream().cuda_stream) == 0
-    out = out.view(-1, 4).abs()
+    out = out.view(-1, 6).abs()
     assert out[:, :2].max().item() < 1e-15
     assert out[:, 2:].max().item() < 1e-13
+    # NaN takes the library path of every version and comes back as NaN
+    xn = torch.tensor([float("nan")], dtype=torch.float64, device="cuda")
+    on = torch.empty(6, dtype=torch.float64, device="cuda")
+    assert lib.mg_trig_check(xn.data_ptr(), on.data_ptr(), 1, torch.cuda.current_stream().cuda_stream) == 0
+    assert torch.isnan(on).all().item()
 
 
 @pytest.mark.parametrize("name", ["clipped_squarenet_N4.npz", "clipped_qrnet_N4.npz"])
