@@ -876,15 +876,40 @@ def run_plain_forward(args, peak):
         print(json.dumps({"profile_calls": 3, "status": m.status()}))
         return None
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    reps = max(20, min(args.steps * 10, 200))
+    # the reference-shaped C call with its arguments prepared once (what a C or CuPy caller pays)
+    from meshes_gb300 import _lib
+    lib = _lib.load()
+    st = torch.cuda.current_stream(dev).cuda_stream
+    wsb = lib.mg_workspace_bytes(0, nc, len(lens), bc, 0, 0, None)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    _lib.check(lib.mg_workspace_init(ws.data_ptr(), wsb, st), "mg_workspace_init")
+    capi_args = (nc, len(lens), bc, m.lens.data_ptr(), m.shifts.data_ptr(), m.p_phase.data_ptr(), nc // 2 * 2, None, 0,
+                 x.data_ptr(), out.data_ptr(), nc, 0, ws.data_ptr(), wsb, st)
+
+    def capi_call():
+        lib.mg_fwdprop(*capi_args)
+
     with ClockSampler(gpu_id(torch, dev)) as cs:
-        t = event_ms(torch, lambda: m.dot(x, out=out), max(20, min(args.steps * 10, 200)), warm=max(3, args.warmup),
-                     flush=flush)
+        t = event_ms(torch, lambda: m.dot(x, out=out), reps, warm=max(3, args.warmup), flush=flush)
+        t_capi = event_ms(torch, capi_call, reps, warm=3, flush=flush)
+        # the device time of one call: the same C call recorded in a CUDA graph and replayed (no host work
+        # between the events)
+        g = torch.cuda.CUDAGraph()
+        capi_call()
+        torch.cuda.synchronize()
+        with torch.cuda.graph(g):
+            capi_call()
+        t_dev = event_ms(torch, g.replay, reps, warm=3, flush=flush)
     y_h = out.t().cpu().numpy()
     U = m.matrix().t().to(torch.complex128)
     unit_err = float(torch.linalg.norm(U @ U.conj().t() - torch.eye(nc, dtype=torch.complex128, device=dev)))
     n_mzi = int(mask.sum())
     err = cpu_forward_check(nc, lens, shifts, p, None, x_h, y_h)
     return {"metric": "MZI-apps/s (fwd)", "value": n_mzi * bc / t, "unit": "MZI-apps/s", "ms": t * 1e3,
+            "ms_c_call": t_capi * 1e3, "ms_device": t_dev * 1e3,
+            "timing": "ms: one MeshNetworkGPU.dot call between CUDA events (host work included); ms_c_call: one "
+                      "mg_fwdprop call with prepared arguments; ms_device: that call replayed from a CUDA graph",
             "config": {"workload": "clements_mzi_N64_L64_B1024_fwd", "n_mzi": n_mzi, "B": bc,
                        "call": "MeshNetworkGPU.dot -> mg_fwdprop (coefficient pass + propagation)",
                        "l2": "flushed between timed calls"},

@@ -108,6 +108,7 @@ struct Plan {
   bool split;   // two CTA kinds per SM (V and V-1 vectors per lane group), CTAs [0, nA) the first kind
   int nA;
   bool pair;    // warp-pair launch: a vector over two warps (4 modes per lane), V vectors per pair
+  bool occ2;    // kernel compiled for two resident CTAs per SM; shared memory sized for two
   unsigned lb, dlb;
   size_t smem;
   size_t off_kinds, off_tiles, off_dtiles, off_partial, total;
@@ -186,11 +187,16 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   // warp-pair launch (split 3): back-propagation of a nearest-neighbour complex mesh with a full-warp M = 8 plan
   const int split_mode = cfg ? cfg->split : 0;
   p.pair = split_mode == 3;
+  p.occ2 = split_mode == 4;
+  if (p.occ2 && (stored || perm || geometry != GEO_NN || G != 32 || !nn2_instantiated(op, crossing == CR_ORTH, M, V, p.gr)))
+    return fail(MG_E_CONFIG, "no two-CTA-per-SM kernel for op=%d crossing=%d geometry=%d M=%d G=%d V=%d", op, crossing,
+                geometry, M, G, V);
   if (p.pair) {
     if (!(cfg && cfg->V)) V = 7;
     if (stored || perm || geometry != GEO_NN || G != 32 || !pair_instantiated(op, crossing == CR_ORTH, M, V, p.gr, true))
       return fail(MG_E_CONFIG, "no warp-pair kernel for op=%d crossing=%d geometry=%d M=%d G=%d V=%d", op, crossing,
                   geometry, M, G, V);
+  } else if (p.occ2) {
   } else if (wide ? (perm || stored || !wide_instantiated(op, crossing == CR_ORTH, V, p.gr))
            : perm ? !perm_instantiated(op, crossing == CR_ORTH, M, V, p.gr)
                   : (stored ? !instantiated_stored(OP_BWD, M, V) : !instantiated(op, M, V)))
@@ -205,7 +211,7 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   // 17x those of the uniform launch).
   p.split = false;
   p.nA = 0;
-  if (split_mode != 2 && !p.pair && (op == OP_FWD || op == OP_BWD) && V >= 2 && !stored && !perm &&
+  if (split_mode != 2 && !p.pair && !p.occ2 && (op == OP_FWD || op == OP_BWD) && V >= 2 && !stored && !perm &&
       split_instantiated(op, crossing == CR_ORTH, M, V, G == 32, p.gr)) {
     const long ws = (cfg && cfg->W) ? cfg->W : 4;
     const long capA = ws * p.R * V, capB = ws * p.R * (V - 1);
@@ -218,8 +224,8 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   p.dlb = (op == OP_BWD && p.gr == 0) ? (unsigned)(p.np2 * (p.real ? 16 : 64)) : 0;
   const int gslot = (op != OP_BWD) ? 0 : ((p.gr == 1 || p.gr == 2) ? 8 : (p.real ? 16 : 32));
   const size_t gstl = (size_t)p.np2 * gslot;
-  const int maxw = prop_max_threads(op, M, V) / 32;
-  int W = (cfg && cfg->W) ? cfg->W : (p.split ? 4 : p.pair ? 8 : 0);
+  const int maxw = p.occ2 ? 8 : prop_max_threads(op, M, V) / 32;
+  int W = (cfg && cfg->W) ? cfg->W : (p.split ? 4 : (p.pair || p.occ2) ? 8 : 0);
   if (p.pair && (W & 1)) return fail(MG_E_CONFIG, "a warp-pair launch needs an even W, got %d", W);
   if (!W) {
     // enough warps to cover the batch in one wave, rounded up to a multiple of 4 so the four
@@ -234,7 +240,7 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   int S = (cfg && cfg->S) ? cfg->S : ((op == OP_FWD || p.split) ? 2 : 3);
   if (S < 1 || S > 8) return fail(MG_E_CONFIG, "S=%d stages outside [1, 8]", S);
   // a split launch keeps two CTAs resident per SM (each also pays the 1 KB the SM reserves per CTA)
-  const size_t budget = p.split ? (size_t)di.smem_per_sm / 2 - 1024 : (size_t)di.smem_optin - 1024;
+  const size_t budget = (p.split || p.occ2) ? (size_t)di.smem_per_sm / 2 - 1024 : (size_t)di.smem_optin - 1024;
   int CL = (cfg && cfg->CL) ? cfg->CL : 0;
   const size_t per_layer = (size_t)S * p.lb + p.dlb + W * gstl;
   const size_t fixed = 8 * (size_t)(S + 1) + (L <= kMaxSmemKinds ? 4 * (size_t)L : 0) +
@@ -378,6 +384,8 @@ int run_prop(const Plan& P, const void* in0, const void* in1, void* out0, void* 
   a.nA = P.nA;
   if (P.pair)
     e = launch_prop_pair(P.V, lc, a);
+  else if (P.occ2)
+    e = launch_prop_nn2(P.op, P.real, P.M, P.V, P.gr, lc, a);
   else if (P.M == kWideM)
     e = launch_prop_wide(P.op, P.real, P.V, P.gr, lc, a);
   else if (!P.perm && P.geometry == GEO_NN && nn_instantiated(P.op, P.real, P.M, P.V, P.gr, P.G == 32, P.split))
@@ -702,7 +710,7 @@ int mg_propagate(int op, int N, int L, int B, int crossing, int geometry, const 
     Plan Pb, Pf;
     TRY(make_plan(OP_BWD, N, L, B, crossing, geometry, cfg, &Pb));
     TRY(check_ws(Pb, ws, wsb));
-    mg_config cf = {Pb.M, 0, 0, 0, 0, (cfg && cfg->split != 3) ? cfg->split : 0};
+    mg_config cf = {Pb.M, 0, 0, 0, 0, (cfg && cfg->split != 3 && cfg->split != 4) ? cfg->split : 0};
     mg_config tf;   // a measured forward configuration of this shape applies if its M matches the tiles'
     if (!cfg && !Pb.perm && lookup_tuned(OP_FWD, crossing, Pb.geometry, N, B, &tf) && tf.M == Pb.M) cf = tf;
     TRY(make_plan(OP_FWD, N, L, B, crossing, geometry, &cf, &Pf));

@@ -37,10 +37,10 @@ inline cudaError_t ensure_smem_attr(K kernel, std::atomic<unsigned long long>& d
   return cudaSuccess;
 }
 
-template <int OP, int M, int V, bool REAL, int GT, int GR, bool PERM = false, bool NN = false>
+template <int OP, int M, int V, bool REAL, int GT, int GR, bool PERM = false, bool NN = false, int MINB = 1>
 inline cudaError_t launch_one(const LaunchCfg& lc, const PropArgs& a) {
   static std::atomic<unsigned long long> done{0};
-  auto k = prop_kernel<OP, M, V, REAL, GT, GR, PERM, NN>;
+  auto k = prop_kernel<OP, M, V, REAL, GT, GR, PERM, NN, MINB>;
   cudaError_t e = ensure_smem_attr(k, done);
   if (e != cudaSuccess) return e;
   k<<<lc.grid, lc.block, lc.smem, lc.stream>>>(a);
@@ -82,6 +82,10 @@ cudaError_t launch_prop_nn(int op, bool real, int M, int V, int gr, bool full, b
 constexpr int kWideM = 20;
 bool wide_instantiated(int op, bool real, int V, int gr);
 cudaError_t launch_prop_wide(int op, bool real, int V, int gr, const LaunchCfg& lc, const PropArgs& a);
+// nearest-neighbour full-warp kernels compiled for two resident 256-thread CTAs per SM (at most 128 registers
+// per thread): (op, M, V) in nn2_instantiated (mg_prop_nn.cu)
+bool nn2_instantiated(int op, bool real, int M, int V, int gr);
+cudaError_t launch_prop_nn2(int op, bool real, int M, int V, int gr, const LaunchCfg& lc, const PropArgs& a);
 // warp-pair back-propagation (mg_prop_pair.cu): a vector over the 64 lanes of two warps, 4 modes per lane, on
 // the tiles of an M = 8, G = 32 plan; V counts vectors per pair
 bool pair_instantiated(int op, bool real, int M, int V, int gr, bool full);

@@ -978,8 +978,10 @@ __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem
   if constexpr (OP != OP_FWD) store_fields<M, V, REAL>(w, a.out1, vb0, a.vend, a.N, a.ldu, j);
 }
 
-template <int OP, int M, int V, bool REAL, int GT, int GR, bool PERM = false, bool NN = false>
-__global__ void __launch_bounds__(PropTraits<OP, M, V, REAL>::kMaxThreads)
+// MINB > 1: compiled for MINB resident CTAs of 256 threads per SM (at most 65536 / (256 * MINB) registers per
+// thread), for batch tiles small enough that several CTAs share an SM
+template <int OP, int M, int V, bool REAL, int GT, int GR, bool PERM = false, bool NN = false, int MINB = 1>
+__global__ void __launch_bounds__(MINB > 1 ? 256 : PropTraits<OP, M, V, REAL>::kMaxThreads, MINB)
 prop_kernel(const PropArgs a0) {
   extern __shared__ __align__(128) unsigned char smem[];
   PropArgs a = a0;

@@ -55,4 +55,14 @@ cudaError_t launch_prop_nn(int op, bool real, int M, int V, int gr, bool full, b
   }
 }
 
+bool nn2_instantiated(int op, bool real, int M, int V, int gr) {
+  return !real && M == 8 && V == 2 && ((op == OP_FWD && gr == 0) || (op == OP_BWD && gr == 1));
+}
+
+cudaError_t launch_prop_nn2(int op, bool real, int M, int V, int gr, const LaunchCfg& lc, const PropArgs& a) {
+  if (!nn2_instantiated(op, real, M, V, gr)) return cudaErrorInvalidConfiguration;
+  return op == OP_FWD ? launch_one<OP_FWD, 8, 2, false, 32, 0, false, true, 2>(lc, a)
+                      : launch_one<OP_BWD, 8, 2, false, 32, 1, false, true, 2>(lc, a);
+}
+
 }  // namespace mg
