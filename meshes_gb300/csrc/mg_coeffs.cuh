@@ -10,6 +10,7 @@
 // shift/2 <= q < shift/2 + len (gpu/gmem.cu:236-238); a butterfly layer with stride 2^e couples
 // modes (2*2^e*(q/2^e) + q%2^e, +2^e) (gpu/fwdprop.cu:52-93).
 #pragma once
+#include "mg_ffcoef.cuh"
 #include "mg_prop.cuh"
 
 namespace mg {
@@ -72,7 +73,11 @@ __device__ __forceinline__ void slot_T(const CoefArgs& a, int l, int q, bool act
     D1 = c2x2_zero();
   }
   if (a.crossing == CR_MZI) {
-    mzi_T(pp[0], pp[1], ss ? ss[0] : 0.f, ss ? ss[1] : 0.f, &T, need_d ? &D0 : nullptr, need_d ? &D1 : nullptr, csb);
+    // T alone (and the splitter pair of the direct gradient) in float-float on the FP32 pipe; with derivative
+    // tiles, or angles beyond the float-float range, the double-precision form
+    const float al = ss ? ss[0] : 0.f, be = ss ? ss[1] : 0.f;
+    if (need_d || !mzi_T_ff(pp[0], pp[1], al, be, &T, csb))
+      mzi_T(pp[0], pp[1], al, be, &T, need_d ? &D0 : nullptr, need_d ? &D1 : nullptr, csb);
   } else {   // CR_SYM
     sym_T(pp[0], pp[1], ss ? ss[0] : 0.f, &T, need_d ? &D0 : nullptr, need_d ? &D1 : nullptr);
   }

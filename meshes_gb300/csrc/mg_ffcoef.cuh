@@ -1,0 +1,130 @@
+// MZI transfer matrices for the coefficient tiles in float-float arithmetic on the FP32 pipe.
+//
+// The tiles hold float32 values, and a deep mesh accumulates any systematic rounding error linearly, so each
+// entry must be the float32 nearest to the exact value (then the rounding errors are unbiased and grow only
+// as sqrt(L)).  The double-precision path (mzi_T in mg_device.cuh) delivers that, but GB300's FP64 pipe is
+// narrow: it bounds the coefficient pass of a training step.  Here the same closed form is evaluated in
+// float-float ("double-single") arithmetic - Dekker's exact two-product and Knuth's exact two-sum, a value is
+// the unevaluated sum hi + lo of two floats, about 48 significant bits - so the result is correct to ~1e-13
+// before its single rounding to float32, far below the float32 half-unit (3e-8), and the FP32 pipe does the
+// work at many times the FP64 rate.
+//
+// sin and cos: Cody-Waite reduction by pi/2 (pi/2 split into three floats, the first two of 16 significant
+// bits so that k * P1 and k * P2 are exact for |k| < 256), then the Taylor series on |r| <= pi/4, its first
+// terms in float-float and the small tail in float (truncation below 1e-14).  Arguments of 400 or more in
+// magnitude take the double-precision path.
+#pragma once
+#include "mg_device.cuh"
+
+namespace mg {
+
+struct ff {
+  float h, l;
+};
+
+// exact a*b as hi + lo (FMA)
+__device__ __forceinline__ ff ff_two_prod(float a, float b) {
+  const float p = a * b;
+  return {p, __fmaf_rn(a, b, -p)};
+}
+// exact a+b as hi + lo (Knuth)
+__device__ __forceinline__ ff ff_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+// renormalise hi + lo with |hi| >= |lo|
+__device__ __forceinline__ ff ff_quick(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  const ff s = ff_two_sum(a.h, b.h);
+  return ff_quick(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff{-b.h, -b.l}); }
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  const float p = a.h * b.h;
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return ff_quick(p, e);
+}
+__device__ __forceinline__ ff ff_mulf(ff a, float b) {
+  const float p = a.h * b;
+  float e = __fmaf_rn(a.h, b, -p);
+  e = __fmaf_rn(a.l, b, e);
+  return ff_quick(p, e);
+}
+__device__ __forceinline__ ff ff_neg(ff a) { return {-a.h, -a.l}; }
+// the float nearest to hi + lo
+__device__ __forceinline__ float ff_round(ff a) { return __fadd_rn(a.h, a.l); }
+
+struct ffz {
+  ff x, y;
+};
+__device__ __forceinline__ ffz ffz_mul(ffz a, ffz b) {
+  return {ff_sub(ff_mul(a.x, b.x), ff_mul(a.y, b.y)), ff_add(ff_mul(a.x, b.y), ff_mul(a.y, b.x))};
+}
+__device__ __forceinline__ float2 ffz_round(ffz a) { return make_float2(ff_round(a.x), ff_round(a.y)); }
+
+// sin and cos of a float x with |x| < 400 in float-float; returns false (nothing written) beyond
+__device__ __forceinline__ bool ff_sincos(float x, ff* s, ff* c) {
+  if (!(fabsf(x) < 400.f)) return false;
+  // Cody-Waite: pi/2 = P1 + P2 + P3 (residual 1.2e-18); k * P1, k * P2 exact for |k| < 256
+  constexpr float P1 = 1.57080078125f, P2 = -4.4543994590640068e-06f, P3 = -5.5644315544167711e-11f;
+  const float k = rintf(x * 0.636619747f);
+  ff r = ff_two_sum(x, -k * P1);
+  r = ff_add(r, ff{-k * P2, 0.f});
+  r = ff_add(r, ff_neg(ff_two_prod(k, P3)));
+  const ff r2 = ff_mul(r, r);
+  const float t = r2.h;
+  // sin r = r + r^3 (-1/3! + r^2 (1/5! + r^2 (-1/7! + r^2 q))), q in float (|r^9 q| < 3e-7)
+  const float qs = __fmaf_rn(t, __fmaf_rn(t, __fmaf_rn(t, 1.60590444e-10f, -2.50521079e-08f), 2.75573188e-06f), 0.f);
+  ff ps = ff_add(ff{-0.000198412701f, 2.72559687e-12f}, ff{qs, 0.f});                 // -1/7! + r^2 q
+  ps = ff_add(ff{0.00833333377f, -4.34617203e-10f}, ff_mul(r2, ps));                   // 1/5!
+  ps = ff_add(ff{-0.166666672f, 4.96705388e-09f}, ff_mul(r2, ps));                     // -1/3!
+  const ff sr = ff_add(r, ff_mul(ff_mul(r, r2), ps));
+  // cos r = 1 + r^2 (-1/2 + r^2 (1/4! + r^2 (-1/6! + r^2 q)))
+  const float qc = __fmaf_rn(t, __fmaf_rn(t, __fmaf_rn(t, -1.14707454e-11f, 2.08767559e-09f), -2.755732e-07f),
+                             2.48015876e-05f);
+  ff pc = ff_add(ff{-0.00138888892f, 3.36310944e-11f}, ff_mulf(r2, qc));                // -1/6! + r^2 q
+  pc = ff_add(ff{0.0416666679f, -1.24176347e-09f}, ff_mul(r2, pc));                    // 1/4!
+  pc = ff_add(ff{-0.5f, 0.f}, ff_mul(r2, pc));                                         // -1/2!
+  const ff cr = ff_add(ff{1.f, 0.f}, ff_mul(r2, pc));
+  switch (static_cast<int>(k) & 3) {
+    case 0: *s = sr; *c = cr; break;
+    case 1: *s = cr; *c = ff_neg(sr); break;
+    case 2: *s = ff_neg(sr); *c = ff_neg(cr); break;
+    default: *s = ff_neg(cr); *c = sr; break;
+  }
+  return true;
+}
+
+// The standard MZI T (mzi_T in mg_device.cuh, reference crossing.py:216-221) and, when given, the
+// (cos, sin)(pi/4 + beta) pair of the direct gradient, in float-float; false (nothing written) when an angle
+// is outside the float-float range, and the caller takes the double path.
+__device__ __forceinline__ bool mzi_T_ff(float th, float ph, float al, float be, C2x2* T, float2* csb) {
+  ff S, C, Sph, Cph, sa, ca, sb, cb;
+  if (!ff_sincos(0.5f * th, &S, &C) || !ff_sincos(ph, &Sph, &Cph) || !ff_sincos(al, &sa, &ca) ||
+      !ff_sincos(be, &sb, &cb))
+    return false;
+  const ff Cp = ff_sub(ff_mul(ca, cb), ff_mul(sa, sb)), Sp = ff_add(ff_mul(sa, cb), ff_mul(ca, sb));
+  const ff Cm = ff_add(ff_mul(ca, cb), ff_mul(sa, sb)), Sm = ff_sub(ff_mul(sa, cb), ff_mul(ca, sb));
+  if (csb) {
+    const ff r2 = {0.707106769f, 1.21016175e-08f};                                    // 1/sqrt 2
+    *csb = make_float2(ff_round(ff_mul(r2, ff_sub(cb, sb))), ff_round(ff_mul(r2, ff_add(cb, sb))));
+  }
+  const ffz E0 = {C, S};                                    // e^{i th/2}
+  const ffz E1 = ffz_mul(E0, ffz{Cph, Sph});                // e^{i(th/2 + ph)}
+  const ff CSp = ff_mul(C, Sp), SCm = ff_mul(S, Cm), SSm = ff_mul(S, Sm), CCp = ff_mul(C, Cp);
+  const ffz A00 = {ff_neg(CSp), SCm}, A01 = {ff_neg(SSm), CCp};
+  const ffz A10 = {SSm, CCp}, A11 = {ff_neg(CSp), ff_neg(SCm)};
+  T->t00 = ffz_round(ffz_mul(E1, A00));
+  T->t01 = ffz_round(ffz_mul(E0, A01));
+  T->t10 = ffz_round(ffz_mul(E1, A10));
+  T->t11 = ffz_round(ffz_mul(E0, A11));
+  return true;
+}
+
+}  // namespace mg

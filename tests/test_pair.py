@@ -93,3 +93,47 @@ def test_pair_launch_rejects_other_shapes():
     assert lib.mg_workspace_bytes(2, 64, 64, 4096, 0, 0, c) == 0            # G = 8 < 32
     assert lib.mg_workspace_bytes(2, 256, 256, 4096, 0, 0, _lib.cfg_ptr(_lib.config(8, 7, 7, 0, 0, 3))) == 0   # odd W
     assert lib.mg_workspace_bytes(2, 256, 256, 4096, 0, 0, c) > 0
+
+
+@pytest.mark.parametrize("op", [0, 2])
+def test_two_cta_per_sm_launch_matches_oracle(op):
+    """Launch option split = 4: the nearest-neighbour kernels compiled for two resident CTAs per SM (M = 8, V = 2),
+    shared memory sized for two; the same fields as the default launch, bitwise."""
+    from meshes_gb300 import _lib
+    rng = np.random.default_rng(91 + op)
+    N, B = 256, 1000
+    om = O.random_mesh(rng, N, "clements", "mzi", 0.02)
+    x = O.unit_columns(rng, N, B)
+    t = O.unit_columns(rng, N, B)
+    y = O.propagate(om, x)
+    occ2 = _lib.config(8, 2, 8, 0, 0, 4)
+    if op == 2:
+        G, xr, gin = O.vjp_unitary(om, y, 2 * (y - t))
+        xa, ga, da = _run(om, y, None, occ2, target=t)
+        assert O.rel_err(ga, gin) < TOL and O.rel_err(xa, x) < TOL
+        assert O.rel_err(da, O.contract_dp(om, G)) < TOL
+        xb, gb, db = _run(om, y, None, _lib.config(8, 2, 8, 0, 0, 2), target=t)
+        assert np.array_equal(ga, gb) and np.array_equal(xa, xb)
+        return
+    from meshes_gb300 import _lib as L_
+    lib = L_.load()
+    st = torch.cuda.current_stream().cuda_stream
+    lens = torch.tensor(om.lens, dtype=torch.int32, device="cuda")
+    shifts = torch.tensor(om.shifts, dtype=torch.int32, device="cuda")
+    p = torch.tensor(np.asarray(om.p, np.float32).reshape(-1), device="cuda")
+    s = torch.tensor(np.asarray(om.s, np.float32).reshape(-1), device="cuda")
+    outs = []
+    for cfg in (occ2, _lib.config(8, 2, 8, 0, 0, 2)):
+        c = _lib.cfg_ptr(cfg)
+        wsb = lib.mg_workspace_bytes(0, N, om.L, B, 0, 0, c)
+        ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
+        _lib.check(lib.mg_workspace_init(ws.data_ptr(), wsb, st), "init")
+        _lib.check(lib.mg_build_tiles(0, N, om.L, 0, lens.data_ptr(), shifts.data_ptr(), None, 0, p.data_ptr(), N,
+                                      s.data_ptr(), N, None, None, None, B, c, ws.data_ptr(), wsb, st), "tiles")
+        xd = torch.tensor(x.astype(np.complex64), device="cuda")
+        yd = torch.empty_like(xd)
+        _lib.check(lib.mg_propagate(0, N, om.L, B, 0, 0, xd.data_ptr(), None, yd.data_ptr(), None, N, None, 0, 0, c,
+                                    ws.data_ptr(), wsb, st), "fwd")
+        assert lib.mg_read_status(ws.data_ptr(), 0, st) == 0
+        outs.append(yd.cpu().numpy())
+    assert O.rel_err(outs[0], y) < TOL and np.array_equal(outs[0], outs[1])
