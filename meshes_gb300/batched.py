@@ -20,6 +20,12 @@ from ._lib import BATCH_NN, GEO_NN, OP_BWD, OP_FWD, check, load, mg_batch_item, 
 from .mesh import MeshNetworkGPU, _stream
 
 BCLS_C8, BCLS_C16, BCLS_R8 = 0, 1, 2
+MG_BATCH_FULL_WARP = 32
+
+
+def MG_BATCH_ONLY(cls: int) -> int:
+    """Flag of mg_batched_propagate: every item of the launch is of kernel class cls."""
+    return (cls + 1) << 8
 _CLS_MV = {BCLS_C8: (8, 4), BCLS_C16: (16, 2), BCLS_R8: (8, 4)}
 WARPS = 8
 
@@ -122,17 +128,26 @@ class BatchedMeshes:
         self.states: List[_MeshState] = [_MeshState(m, b) for m, b in zip(meshes, batch_sizes)]
         sms = torch.cuda.get_device_properties(self.device).multi_processor_count
         self.grid = grid or sms
-        items = []
+        # launch groups: with every mesh nearest-neighbour (MG_BATCH_NN), complex M = 8 meshes whose vector fills
+        # the warp (G = 32) run in their own launch on the one-mesh kernel's body (packed crossings, compile-time
+        # lane group), everything else in one launch of the three-class kernel; each group is sorted
+        # longest-first and drained from its own counter
+        self.nn = BATCH_NN if all(st.mesh.geometry == GEO_NN for st in self.states) else 0
+        groups = {}
         for i, st in enumerate(self.states):
+            full = bool(self.nn) and st.cls == BCLS_C8 and st.G == 32
+            flags = (MG_BATCH_ONLY(BCLS_C8) | MG_BATCH_FULL_WARP) if full else 0
             for k in range(st.n_items):
                 v0 = k * st.cap
-                items.append((st.cost(), i, v0, min(v0 + st.cap, st.B), k))
-        items.sort(key=lambda t: -t[0])                   # longest processing time first
-        arr = (mg_batch_item * max(len(items), 1))()
-        for n, (_, i, v0, v1, k) in enumerate(items):
-            arr[n].mesh, arr[n].v0, arr[n].vend, arr[n].part = i, v0, v1, k
-        self.n_items = len(items)
-        self.items = _to_device(arr, self.device)
+                groups.setdefault(flags, []).append((st.cost(), i, v0, min(v0 + st.cap, st.B), k))
+        self.groups = []
+        for flags, items in sorted(groups.items(), reverse=True):
+            items.sort(key=lambda t: -t[0])               # longest processing time first
+            arr = (mg_batch_item * max(len(items), 1))()
+            for n, (_, i, v0, v1, k) in enumerate(items):
+                arr[n].mesh, arr[n].v0, arr[n].vend, arr[n].part = i, v0, v1, k
+            self.groups.append((flags, len(items), _to_device(arr, self.device)))
+        self.n_items = sum(g[1] for g in self.groups)
         self.desc = {}
         self.smem = {}
         for op in (OP_FWD, OP_BWD):
@@ -141,7 +156,7 @@ class BatchedMeshes:
                 ds[i] = st.descriptor(op)
             self.desc[op] = _to_device(ds, self.device)
             self.smem[op] = max(st.info[op].smem for st in self.states)
-        self.head = torch.zeros(2, dtype=torch.int32, device=self.device)
+        self.head = torch.zeros(max(len(self.groups), 1), dtype=torch.int32, device=self.device)
         self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.graph = None
 
@@ -176,10 +191,10 @@ class BatchedMeshes:
         stream = _stream(self.device)
         self.head.zero_()
         # all meshes nearest-neighbour: the kernel bodies without strided layers (MG_BATCH_NN)
-        nn = BATCH_NN if all(st.mesh.geometry == GEO_NN for st in self.states) else 0
-        check(lib.mg_batched_propagate(op | nn, self.desc[op].data_ptr(), len(self.states), self.items.data_ptr(),
-                                       self.n_items, self.head.data_ptr(), self.grid, self.smem[op],
-                                       self.status.data_ptr(), stream), "mg_batched_propagate")
+        for g, (flags, n, items) in enumerate(self.groups):
+            check(lib.mg_batched_propagate(op | self.nn | flags, self.desc[op].data_ptr(), len(self.states),
+                                           items.data_ptr(), n, self.head[g:].data_ptr(), self.grid, self.smem[op],
+                                           self.status.data_ptr(), stream), "mg_batched_propagate")
         if op == OP_BWD:
             check(lib.mg_batched_reduce(self.desc[op].data_ptr(), len(self.states), stream), "mg_batched_reduce")
 

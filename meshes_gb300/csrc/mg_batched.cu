@@ -20,8 +20,13 @@ constexpr int kBatchWarps = 8;
 __device__ __forceinline__ int cls_M(int cls) { return cls == MG_BCLS_C16 ? 16 : 8; }
 
 // NN: every mesh of the launch is nearest-neighbour (layer kinds 0 and odd-shift), so the bodies without
-// the strided and butterfly layers run (fewer registers; a mesh with another kind is refused per item)
-template <int OP, bool NN>
+// the strided and butterfly layers run (fewer registers; a mesh with another kind is refused per item).
+// CLS >= 0: every item's mesh is of kernel class CLS (others are refused per item) and only that class's body
+// is compiled.  GT = 32 (class MG_BCLS_C8 with MG_BATCH_FULL_WARP): every item's mesh has a vector filling
+// the warp (G = 32, N in (128, 256]) and the body is the one-mesh kernel's, compile-time lane group and
+// packed f32x2 crossings, without spills; with a run-time lane group the packed forms spill and the
+// bodies keep the one-vector crossings (measured on GB300 in the three-class kernel: 13% slower packed).
+template <int OP, bool NN, int CLS = -1, int GT = 0>
 __global__ void __launch_bounds__(kBatchWarps * 32, 1)
 batched_kernel(const mg_batch_mesh* __restrict__ meshes, int n_meshes, const mg_batch_item* __restrict__ items,
                int n_items, int* head, int* status) {
@@ -39,6 +44,10 @@ batched_kernel(const mg_batch_mesh* __restrict__ meshes, int n_meshes, const mg_
       continue;
     }
     const mg_batch_mesh md = meshes[it.mesh];
+    if ((CLS >= 0 && md.cls != CLS) || (GT > 0 && md.G != GT)) {
+      if (threadIdx.x == 0) set_status(status, ST_BAD_WORK);
+      continue;
+    }
     const int M = cls_M(md.cls);
     if (md.G < 1 || md.G > 32 || (md.G & (md.G - 1)) || md.G * M < md.N || it.v0 < 0 || it.vend > md.B) {
       if (threadIdx.x == 0) set_status(status, ST_BAD_WORK);
@@ -69,15 +78,23 @@ batched_kernel(const mg_batch_mesh* __restrict__ meshes, int n_meshes, const mg_
         continue;
       }
     }
-    switch (md.cls) {
-      // one-vector crossings here: with three class bodies in one kernel the packed forms made
-      // back-propagation spill and gained nothing going forward (measured on GB300: the batched engine
-      // 13% and 3.5% slower)
-      case MG_BCLS_C8: prop_body<OP, 8, 4, false, 0, (OP == OP_BWD ? 1 : 0), false, NN, false>(a, smem); break;
-      case MG_BCLS_C16: prop_body<OP, 16, 2, false, 0, (OP == OP_BWD ? 1 : 0), false, NN, false>(a, smem); break;
-      case MG_BCLS_R8: prop_body<OP, 8, 4, true, 0, (OP == OP_BWD ? 2 : 0), false, NN>(a, smem); break;
-      default:
-        if (threadIdx.x == 0) set_status(status, ST_BAD_WORK);
+    if constexpr (CLS == MG_BCLS_C8) {
+      prop_body<OP, 8, 4, false, GT, (OP == OP_BWD ? 1 : 0), false, NN, GT == 32>(a, smem);
+    } else if constexpr (CLS == MG_BCLS_C16) {
+      prop_body<OP, 16, 2, false, 0, (OP == OP_BWD ? 1 : 0), false, NN, false>(a, smem);
+    } else if constexpr (CLS == MG_BCLS_R8) {
+      prop_body<OP, 8, 4, true, 0, (OP == OP_BWD ? 2 : 0), false, NN>(a, smem);
+    } else {
+      switch (md.cls) {
+        // one-vector crossings here: with three class bodies in one kernel the packed forms made
+        // back-propagation spill and gained nothing going forward (measured on GB300: the batched engine
+        // 13% and 3.5% slower)
+        case MG_BCLS_C8: prop_body<OP, 8, 4, false, 0, (OP == OP_BWD ? 1 : 0), false, NN, false>(a, smem); break;
+        case MG_BCLS_C16: prop_body<OP, 16, 2, false, 0, (OP == OP_BWD ? 1 : 0), false, NN, false>(a, smem); break;
+        case MG_BCLS_R8: prop_body<OP, 8, 4, true, 0, (OP == OP_BWD ? 2 : 0), false, NN>(a, smem); break;
+        default:
+          if (threadIdx.x == 0) set_status(status, ST_BAD_WORK);
+      }
     }
   }
 }
@@ -116,21 +133,44 @@ __global__ void batched_reduce_kernel(const mg_batch_mesh* __restrict__ meshes) 
 using namespace mg;
 
 namespace {
-template <int OP, bool NN>
+template <int OP, bool NN, int CLS, int GT>
 cudaError_t launch_batched(const mg_batch_mesh* meshes, int n_meshes, const mg_batch_item* items, int n_items, int* head,
                            int grid, size_t smem, int* status, cudaStream_t st) {
   static std::atomic<unsigned long long> done{0};
-  cudaError_t e = ensure_smem_attr(batched_kernel<OP, NN>, done);
+  cudaError_t e = ensure_smem_attr(batched_kernel<OP, NN, CLS, GT>, done);
   if (e == cudaSuccess)
-    batched_kernel<OP, NN><<<grid, kBatchWarps * 32, smem, st>>>(meshes, n_meshes, items, n_items, head, status);
+    batched_kernel<OP, NN, CLS, GT><<<grid, kBatchWarps * 32, smem, st>>>(meshes, n_meshes, items, n_items, head, status);
   return e;
+}
+template <int OP, int CLS, int GT = 0>
+cudaError_t launch_batched_nn(bool nn, const mg_batch_mesh* meshes, int n_meshes, const mg_batch_item* items,
+                              int n_items, int* head, int grid, size_t smem, int* status, cudaStream_t st) {
+  return nn ? launch_batched<OP, true, CLS, GT>(meshes, n_meshes, items, n_items, head, grid, smem, status, st)
+            : launch_batched<OP, false, CLS, GT>(meshes, n_meshes, items, n_items, head, grid, smem, status, st);
+}
+template <int OP>
+cudaError_t launch_batched_cls(int cls, bool full, bool nn, const mg_batch_mesh* meshes, int n_meshes,
+                               const mg_batch_item* items, int n_items, int* head, int grid, size_t smem, int* status,
+                               cudaStream_t st) {
+  switch (cls) {
+    case MG_BCLS_C8:
+      return full ? launch_batched_nn<OP, MG_BCLS_C8, 32>(nn, meshes, n_meshes, items, n_items, head, grid, smem, status, st)
+                  : launch_batched_nn<OP, MG_BCLS_C8>(nn, meshes, n_meshes, items, n_items, head, grid, smem, status, st);
+    case MG_BCLS_C16: return launch_batched_nn<OP, MG_BCLS_C16>(nn, meshes, n_meshes, items, n_items, head, grid, smem, status, st);
+    case MG_BCLS_R8: return launch_batched_nn<OP, MG_BCLS_R8>(nn, meshes, n_meshes, items, n_items, head, grid, smem, status, st);
+    default: return launch_batched_nn<OP, -1>(nn, meshes, n_meshes, items, n_items, head, grid, smem, status, st);
+  }
 }
 }  // namespace
 
 extern "C" int mg_batched_propagate(int op, const mg_batch_mesh* meshes, int n_meshes, const mg_batch_item* items,
                                     int n_items, int* head, int grid, size_t smem, int* status, void* stream) {
   const bool nn = (op & MG_BATCH_NN) != 0;
-  op &= ~MG_BATCH_NN;
+  const bool full = (op & MG_BATCH_FULL_WARP) != 0;
+  const int cls = ((op >> 8) & 0xff) - 1;   // MG_BATCH_ONLY(cls): one class per launch, -1 any
+  op &= 0x0f;
+  if (cls < -1 || cls > MG_BCLS_R8) return set_last_error(MG_E_ARG, "batched class %d not in {0,1,2}", cls);
+  if (full && cls != MG_BCLS_C8) return set_last_error(MG_E_ARG, "MG_BATCH_FULL_WARP needs MG_BATCH_ONLY(MG_BCLS_C8)");
   if (op != MG_OP_FWD && op != MG_OP_BWD) return set_last_error(MG_E_ARG, "batched op must be fwd or bwd");
   if (!meshes || n_meshes < 0 || (!items && n_items > 0) || !head || grid < 1)
     return set_last_error(MG_E_ARG, "batched launch: bad arguments");
@@ -143,11 +183,9 @@ extern "C" int mg_batched_propagate(int op, const mg_batch_mesh* meshes, int n_m
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t e;
   if (op == MG_OP_FWD)
-    e = nn ? launch_batched<OP_FWD, true>(meshes, n_meshes, items, n_items, head, grid, smem, status, st)
-           : launch_batched<OP_FWD, false>(meshes, n_meshes, items, n_items, head, grid, smem, status, st);
+    e = launch_batched_cls<OP_FWD>(cls, full, nn, meshes, n_meshes, items, n_items, head, grid, smem, status, st);
   else
-    e = nn ? launch_batched<OP_BWD, true>(meshes, n_meshes, items, n_items, head, grid, smem, status, st)
-           : launch_batched<OP_BWD, false>(meshes, n_meshes, items, n_items, head, grid, smem, status, st);
+    e = launch_batched_cls<OP_BWD>(cls, full, nn, meshes, n_meshes, items, n_items, head, grid, smem, status, st);
   if (e == cudaSuccess) e = cudaGetLastError();
   return e == cudaSuccess ? MG_OK : set_last_error(MG_E_CUDA, "batched_kernel: %s", cudaGetErrorString(e));
 }

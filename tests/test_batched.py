@@ -144,8 +144,47 @@ def test_nearest_neighbour_launch():
         st.x.copy_(torch.tensor(x, dtype=st.x.dtype))
     lib = _bind()
     bm2.head.zero_()
-    _lib.check(lib.mg_batched_propagate(_lib.OP_FWD | _lib.BATCH_NN, bm2.desc[0].data_ptr(), 2, bm2.items.data_ptr(),
-                                        bm2.n_items, bm2.head.data_ptr(), bm2.grid, bm2.smem[0], bm2.status.data_ptr(),
+    assert len(bm2.groups) == 1
+    _, n2, items2 = bm2.groups[0]
+    _lib.check(lib.mg_batched_propagate(_lib.OP_FWD | _lib.BATCH_NN, bm2.desc[0].data_ptr(), 2, items2.data_ptr(),
+                                        n2, bm2.head.data_ptr(), bm2.grid, bm2.smem[0], bm2.status.data_ptr(),
                                         torch.cuda.current_stream().cuda_stream), "mg_batched_propagate")
     assert bm2.check_status() == 2
     assert O.rel_err(bm2.states[0].y.cpu().numpy(), O.propagate(oms2[0], xs2[0])) < TOL
+
+
+def test_full_warp_class_launch():
+    """Meshes whose vectors fill the warp (complex M = 8, N in (128, 256]) run in their own launch on the one-mesh
+    kernel's body; a launch of that class refuses an item of another mesh (MG_ST_BAD_WORK) and leaves it."""
+    from meshes_gb300 import _lib
+    from meshes_gb300.batched import MG_BATCH_FULL_WARP, MG_BATCH_ONLY, BCLS_C8, BatchedMeshes, _bind
+    rng = np.random.default_rng(57)
+    oms = [O.random_mesh(rng, 256, "clements", "mzi", 0.01), O.random_mesh(rng, 200, "reck", "mzi", 0.01),
+           O.random_mesh(rng, 64, "clements", "mzi", 0.01)]
+    Bs = [70, 45, 33]
+    xs = [O.unit_columns(rng, om.N, B) for om, B in zip(oms, Bs)]
+    gs = [O.unit_columns(rng, om.N, B) for om, B in zip(oms, Bs)]
+    bm = BatchedMeshes([gpu_mesh(om) for om in oms], Bs)
+    assert [g[0] for g in bm.groups] == [MG_BATCH_ONLY(BCLS_C8) | MG_BATCH_FULL_WARP, 0]
+    for st, x, g in zip(bm.states, xs, gs):
+        st.x.copy_(torch.tensor(x, dtype=st.x.dtype))
+        st.gy.copy_(torch.tensor(g, dtype=st.gy.dtype))
+    bm.step(True)
+    assert bm.check_status() == 0
+    for om, st, x, g in zip(oms, bm.states, xs, gs):
+        y_ref = O.propagate(om, x)
+        G, _, gin = O.vjp_unitary(om, y_ref, g)
+        assert O.rel_err(st.y.cpu().numpy(), y_ref) < TOL
+        assert O.rel_err(st.gx.cpu().numpy(), gin) < TOL
+        assert O.rel_err(st.dp.cpu().numpy(), O.contract_dp(om, G)) < TOL
+    # the N = 64 mesh's items through the full-warp launch: refused, output untouched
+    lib = _bind()
+    _, n_rest, items_rest = bm.groups[1]
+    bm.states[2].y.zero_()
+    bm.head.zero_()
+    _lib.check(lib.mg_batched_propagate(_lib.OP_FWD | _lib.BATCH_NN | MG_BATCH_ONLY(BCLS_C8) | MG_BATCH_FULL_WARP,
+                                        bm.desc[0].data_ptr(), 3, items_rest.data_ptr(), n_rest, bm.head.data_ptr(),
+                                        bm.grid, bm.smem[0], bm.status.data_ptr(),
+                                        torch.cuda.current_stream().cuda_stream), "mg_batched_propagate")
+    assert bm.check_status() == 3
+    assert float(bm.states[2].y.abs().max()) == 0.0
