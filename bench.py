@@ -885,10 +885,11 @@ def run_plain_forward(args, peak):
     ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
     _lib.check(lib.mg_workspace_init(ws.data_ptr(), wsb, st), "mg_workspace_init")
     capi_args = (nc, len(lens), bc, m.lens.data_ptr(), m.shifts.data_ptr(), m.p_phase.data_ptr(), nc // 2 * 2, None, 0,
-                 x.data_ptr(), out.data_ptr(), nc, 0, ws.data_ptr(), wsb, st)
+                 x.data_ptr(), out.data_ptr(), nc, 0, ws.data_ptr(), wsb)
 
     def capi_call():
-        lib.mg_fwdprop(*capi_args)
+        # the current stream at call time (inside a capture, the capturing stream)
+        _lib.check(lib.mg_fwdprop(*capi_args, torch.cuda.current_stream(dev).cuda_stream), "mg_fwdprop")
 
     with ClockSampler(gpu_id(torch, dev)) as cs:
         t = event_ms(torch, lambda: m.dot(x, out=out), reps, warm=max(3, args.warmup), flush=flush)
@@ -901,15 +902,24 @@ def run_plain_forward(args, peak):
         with torch.cuda.graph(g):
             capi_call()
         t_dev = event_ms(torch, g.replay, reps, warm=3, flush=flush)
+        # calls issued back to back (the device time per call once the host runs ahead)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            capi_call()
+        e1.record()
+        torch.cuda.synchronize()
+        t_b2b = e0.elapsed_time(e1) * 1e-3 / reps
     y_h = out.t().cpu().numpy()
     U = m.matrix().t().to(torch.complex128)
     unit_err = float(torch.linalg.norm(U @ U.conj().t() - torch.eye(nc, dtype=torch.complex128, device=dev)))
     n_mzi = int(mask.sum())
     err = cpu_forward_check(nc, lens, shifts, p, None, x_h, y_h)
     return {"metric": "MZI-apps/s (fwd)", "value": n_mzi * bc / t, "unit": "MZI-apps/s", "ms": t * 1e3,
-            "ms_c_call": t_capi * 1e3, "ms_device": t_dev * 1e3,
-            "timing": "ms: one MeshNetworkGPU.dot call between CUDA events (host work included); ms_c_call: one "
-                      "mg_fwdprop call with prepared arguments; ms_device: that call replayed from a CUDA graph",
+            "ms_c_call": t_capi * 1e3, "ms_graph": t_dev * 1e3, "ms_back_to_back": t_b2b * 1e3,
+            "timing": "ms: one MeshNetworkGPU.dot call between CUDA events, L2 flushed before (host work included); "
+                      "ms_c_call: one mg_fwdprop call with prepared arguments; ms_graph: that call replayed from a "
+                      "CUDA graph; ms_back_to_back: per call of many issued without synchronisation",
             "config": {"workload": "clements_mzi_N64_L64_B1024_fwd", "n_mzi": n_mzi, "B": bc,
                        "call": "MeshNetworkGPU.dot -> mg_fwdprop (coefficient pass + propagation)",
                        "l2": "flushed between timed calls"},

@@ -157,6 +157,7 @@ class BatchedMeshes:
             self.desc[op] = _to_device(ds, self.device)
             self.smem[op] = max(st.info[op].smem for st in self.states)
         self.head = torch.zeros(max(len(self.groups), 1), dtype=torch.int32, device=self.device)
+        self.side = None
         self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.graph = None
 
@@ -190,11 +191,27 @@ class BatchedMeshes:
         lib = _bind()
         stream = _stream(self.device)
         self.head.zero_()
-        # all meshes nearest-neighbour: the kernel bodies without strided layers (MG_BATCH_NN)
+        main = torch.cuda.current_stream(self.device)
+        # the groups' persistent launches run concurrently (the first on the current stream, the others on side
+        # streams joined back with events), so the CTAs of one fill the SMs the other's tail leaves idle
+        if len(self.groups) > 1:
+            if self.side is None:
+                self.side = [torch.cuda.Stream(self.device) for _ in self.groups[1:]]
+            fork = torch.cuda.Event()
+            fork.record(main)
+            for sd in self.side:
+                sd.wait_event(fork)
         for g, (flags, n, items) in enumerate(self.groups):
+            s_g = stream if g == 0 else self.side[g - 1].cuda_stream
+            # all meshes nearest-neighbour: the kernel bodies without strided layers (MG_BATCH_NN)
             check(lib.mg_batched_propagate(op | self.nn | flags, self.desc[op].data_ptr(), len(self.states),
                                            items.data_ptr(), n, self.head[g:].data_ptr(), self.grid, self.smem[op],
-                                           self.status.data_ptr(), stream), "mg_batched_propagate")
+                                           self.status.data_ptr(), s_g), "mg_batched_propagate")
+        if len(self.groups) > 1:
+            for sd in self.side:
+                join = torch.cuda.Event()
+                join.record(sd)
+                main.wait_event(join)
         if op == OP_BWD:
             check(lib.mg_batched_reduce(self.desc[op].data_ptr(), len(self.states), stream), "mg_batched_reduce")
 
