@@ -363,6 +363,15 @@ int mg_generic_mzi_T_vjp(int n, const double* p, const double* s, const void* gT
 int mg_diag_configure(int N, int K, void* U, void* Z, void* VdV, void* WWd, int n1, const double* s1, double* c1,
                       int type1, int n2, const double* s2, double* c2, int type2, const int* ijzp, const double* init,
                       const double* noise, int improved);
+/* The direct method (reference configure.py:333-410, direct(m, U, 'down') and its directHelper_fn) for a
+ * nearest-neighbour mesh of output-phase MZIs (MZICrossingOutPhase) with its phase screen at the input: L layers
+ * (lens, shifts), U the N x N complex128 row-major target, s (n_cr x 2) splitting errors and p (n_cr x 2)
+ * (theta, phi) in the reference's flat crossing order (layer by layer, top to bottom); p is written in place
+ * (crossings outside every diagonal keep their values) and phi_out (N) receives the input screen.  dk_max as the
+ * reference's (1, or 2 for some divided Clements rectangles).  Returns MG_E_ARG when the geometry is invalid or two
+ * diagonals share an input mode.  Host code; does not touch the GPU. */
+int mg_direct_configure(int N, int L, const int* lens, const int* shifts, const void* U, const double* s, double* p,
+                        double* phi_out, int dk_max);
 
 /* ---- measurement helpers -------------------------------------------------------------------- */
 

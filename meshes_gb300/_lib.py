@@ -117,6 +117,7 @@ _SIGS = {
                                        c_int, c_ulonglong, c_int, c_void_p, c_size_t, c_void_p]),
     "mg_diag_configure": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_int,
                                   c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_int]),
+    "mg_direct_configure": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int]),
     "mg_fma_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
     "mg_fma2_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
     "mg_trig_check": (c_int, [c_void_p, c_void_p, c_int, c_void_p]),

@@ -121,21 +121,24 @@ class _MeshState:
 class BatchedMeshes:
     """A fixed composition of meshes and batch sizes, propagated by one persistent launch per op."""
 
-    def __init__(self, meshes: Sequence[MeshNetworkGPU], batch_sizes: Sequence[int], grid: Optional[int] = None):
+    def __init__(self, meshes: Sequence[MeshNetworkGPU], batch_sizes: Sequence[int], grid: Optional[int] = None,
+                 full_warp: bool = False):
         if len(meshes) != len(batch_sizes):
             raise ValueError("one batch size per mesh")
         self.device = meshes[0].device
         self.states: List[_MeshState] = [_MeshState(m, b) for m, b in zip(meshes, batch_sizes)]
         sms = torch.cuda.get_device_properties(self.device).multi_processor_count
         self.grid = grid or sms
-        # launch groups: with every mesh nearest-neighbour (MG_BATCH_NN), complex M = 8 meshes whose vector fills
-        # the warp (G = 32) run in their own launch on the one-mesh kernel's body (packed crossings, compile-time
-        # lane group), everything else in one launch of the three-class kernel; each group is sorted
-        # longest-first and drained from its own counter
+        # launch groups: by default every item runs in one launch of the three-class kernel.  With full_warp and
+        # every mesh nearest-neighbour (MG_BATCH_NN), complex M = 8 meshes whose vector fills the warp (G = 32)
+        # run in a launch of their own on the one-mesh kernel's body (packed crossings, compile-time lane
+        # group), concurrently with the rest on a side stream.  On 512 uneven meshes (N 8..256) that measured
+        # slower than the single launch (fwd+bwd 219 against 230 G MZI-apps/s on GB300): the two persistent
+        # grids compete for the same SMs.  Each group is sorted longest-first and drained from its own counter.
         self.nn = BATCH_NN if all(st.mesh.geometry == GEO_NN for st in self.states) else 0
         groups = {}
         for i, st in enumerate(self.states):
-            full = bool(self.nn) and st.cls == BCLS_C8 and st.G == 32
+            full = full_warp and bool(self.nn) and st.cls == BCLS_C8 and st.G == 32
             flags = (MG_BATCH_ONLY(BCLS_C8) | MG_BATCH_FULL_WARP) if full else 0
             for k in range(st.n_items):
                 v0 = k * st.cap

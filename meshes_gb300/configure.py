@@ -22,6 +22,12 @@ programming noise ``sigp``), so a seeded call reproduces the reference's program
 ``reck(U, ...)`` and ``diag_reck(mesh, U, improved)`` are the Reck entry points (reference reck.py:68-72,
 146-164, ``ReckNetwork(M=U, method='diag' | 'diag*')``); ``square(M, ...)`` programs a SquareNet
 (square.py:77-101, ``SquareNetwork(M=M, method='diag')``) into a clipped mesh.
+
+The direct method (reference configure.py:333-410, ``direct``) programs a mesh of output-phase MZIs with its
+phase screen at the input diagonal by diagonal from the target's columns, in closed form; it needs no
+propagation, so it runs entirely in the native host pass ``mg_direct_configure``, and the programmed mesh
+(a ``GenericMeshGPU`` of ``mzi_outphase`` crossings) propagates on the GPU.  ``reck(U, method='direct')`` and
+``square(M, method='direct')`` are its entry points (reck.py:69-74, square.py:65-66,103-113).
 """
 from __future__ import annotations
 
@@ -196,10 +202,18 @@ def diag_reck(mesh: MeshNetworkGPU, U, improved: bool = True, sigp: float = 0.0,
     return mesh
 
 
-def reck(U, p_splitter=0.0, improved: bool = True, sigp: float = 0.0, init="rand", device=None) -> MeshNetworkGPU:
-    """A Reck MeshNetworkGPU realising U (reference ReckNetwork(M=U, p_splitter=..., method='diag*' (improved)
-    or 'diag'), reck.py:68-72): p_splitter is a scalar or (N(N-1)/2, 2) splitting errors in the reference's
-    flat order."""
+def reck(U, p_splitter=0.0, improved: bool = True, sigp: float = 0.0, init="rand", device=None,
+         method: Optional[str] = None):
+    """A Reck mesh realising U (reference ReckNetwork(M=U, p_splitter=..., method=...), reck.py:68-74):
+    p_splitter is a scalar or (N(N-1)/2, 2) splitting errors in the reference's flat order.  method 'diag*'
+    (or improved=True) and 'diag' return a MeshNetworkGPU with its screen at the output; 'direct' returns the
+    reference's phi_pos='in' mesh of output-phase MZIs as a GenericMeshGPU."""
+    if method is not None:
+        if method not in ("diag", "diag*", "direct"):
+            raise ValueError("method must be 'diag', 'diag*' or 'direct'")
+        if method == "direct":
+            return reck_direct(U, p_splitter, device)
+        improved = method == "diag*"
     U = np.asarray(U, dtype=np.complex128)
     N = U.shape[0]
     lens, shifts = geom.reck(N)
@@ -212,13 +226,21 @@ def reck(U, p_splitter=0.0, improved: bool = True, sigp: float = 0.0, init="rand
     return diag_reck(m, U, improved, sigp, init)
 
 
-def square(M, p_splitter=0.0, eig: Optional[float] = None, improved: bool = False, init="rand", device=None):
+def square(M, p_splitter=0.0, eig: Optional[float] = None, improved: bool = False, init="rand", device=None,
+           method: str = "diag"):
     """A SquareNet (square.py:22-101, SquareNetwork(M=M, method='diag'), screen at the output) realising the
     (m, n) matrix M, returned as a ClippedMeshGPU over its (m + n)-mode diamond mesh, and the scale factor the
-    reference applies to M first (1, or sqrt(eig / max eigenvalue of M M^H) when eig is given)."""
+    reference applies to M first (1, or sqrt(eig / max eigenvalue of M M^H) when eig is given).  method='direct'
+    is SquareNetwork(M=M, method='direct', phi_pos='in') (square.py:103-113): the full mesh is then a
+    GenericMeshGPU of output-phase MZIs with its screen at the input."""
     from scipy.linalg import eigvalsh
 
     from .clipped import ClippedMeshGPU
+    if method == "direct":
+        return square_direct(M, p_splitter, eig, device)
+    if method not in ("diag", "diag*"):
+        raise ValueError("method must be 'diag', 'diag*' or 'direct'")
+    improved = improved or method == "diag*"
     M11 = np.array(M, dtype=np.complex128)
     m_out, n_in = M11.shape
     Nf = m_out + n_in
@@ -248,4 +270,105 @@ def square(M, p_splitter=0.0, eig: Optional[float] = None, improved: bool = Fals
     phi = np.zeros(Nf)
     diag(full, None, phi, U, m_out, nn, ijxyp, improved, 0.0, init)
     _set_screen(full, phi)
+    return ClippedMeshGPU(full, slice(n_in), slice(m_out)), fact
+
+
+# ---- the direct method
+
+def direct_core(N: int, lens, shifts, U, s_flat, p_flat=None, dk_max: int = 1):
+    """The direct method's host pass (mg_direct_configure): (theta, phi) of every crossing (n_cr, 2) in the
+    reference's flat order and the input screen (N,), for a nearest-neighbour mesh (lens, shifts) of output-phase
+    MZIs with splitting errors s_flat (n_cr, 2); p_flat holds the starting phases (zeros if None), kept for the
+    crossings no diagonal reaches."""
+    lens = np.ascontiguousarray(lens, dtype=np.int32)
+    shifts = np.ascontiguousarray(shifts, dtype=np.int32)
+    n_cr = int(lens.sum())
+    Ub = np.ascontiguousarray(np.asarray(U, dtype=np.complex128))
+    if Ub.shape != (N, N):
+        raise ValueError("U must be %d x %d" % (N, N))
+    s = np.ascontiguousarray(np.broadcast_to(np.asarray(s_flat, dtype=np.float64), (n_cr, 2)))
+    p = np.zeros((n_cr, 2)) if p_flat is None else np.array(p_flat, dtype=np.float64).reshape(n_cr, 2)
+    phi = np.zeros(N)
+
+    def ptr(a):
+        return a.ctypes.data_as(ctypes.c_void_p)
+    check(load().mg_direct_configure(N, len(lens), ptr(lens), ptr(shifts), ptr(Ub), ptr(s), ptr(p), ptr(phi),
+                                     int(dk_max)), "mg_direct_configure")
+    return p, phi
+
+
+def direct(mesh, U, diag: str = "down", dk_max: int = 1):
+    """Program mesh (a GenericMeshGPU of 'mzi_outphase' crossings, nearest-neighbour, phase screen at the input) to
+    realise U by the direct method (reference configure.py:333-368, direct(m, U, 'down', dk_max)); its crossing
+    phases and screen are written in place.  The reference's 'up' form flips an output-screen mesh and programs
+    the flipped one; no caller of the reference uses it, and it is not provided."""
+    from .lossy import GenericMeshGPU
+    if diag != "down":
+        raise NotImplementedError("only the 'down' diagonals (the form Reck and SquareNet meshes use)")
+    if not isinstance(mesh, GenericMeshGPU) or mesh.X != "mzi_outphase" or not mesh.is_phase or mesh.phi_pos != "in":
+        raise ValueError("the direct method programs a GenericMeshGPU of 'mzi_outphase' crossings with its phase "
+                         "screen at the input")
+    lm = mesh.mesh
+    if lm.geometry != geom_nn():
+        raise ValueError("the direct method programs nearest-neighbour meshes")
+    N, L = mesh.N, mesh.L
+    lay, slot = _flat_layout(lm.lens_h, lm.shifts_h)
+    n_cr = len(lay)
+    s = (mesh.p_splitter.detach().cpu().numpy()[lay, slot] if mesh.p_splitter is not None else np.zeros((n_cr, 2)))
+    grid = mesh.p_phase[:L * (N // 2) * 2].detach().cpu().numpy().reshape(L, N // 2, 2)
+    p, phi = direct_core(N, lm.lens_h, lm.shifts_h, U, s, grid[lay, slot], dk_max)
+    grid = np.zeros((L, N // 2, 2))
+    grid[lay, slot] = p
+    mesh.p_phase.copy_(torch.as_tensor(np.concatenate([grid.reshape(-1), phi]), dtype=mesh.p_phase.dtype))
+    return mesh
+
+
+def _outphase_mesh(N, lens, shifts, p_splitter, device):
+    from .lossy import GenericMeshGPU
+    lay = _flat_layout(list(lens), list(shifts))
+    s = np.zeros((len(lay[0]), 2)) + np.asarray(p_splitter, dtype=np.float64)
+    grid = np.zeros((len(lens), N // 2, 2))
+    grid[lay[0], lay[1]] = s
+    return GenericMeshGPU(N, len(lens), list(lens), list(shifts), np.zeros(len(lens) * (N // 2) * 2 + N), grid,
+                          X="mzi_outphase", phi_pos="in", is_phase=True, device=device)
+
+
+def reck_direct(U, p_splitter=0.0, device=None):
+    """ReckNetwork(M=U, p_splitter=..., method='direct', phi_pos='in') (reck.py:69-74): a GenericMeshGPU of
+    output-phase MZIs with its screen at the input, programmed by the direct method.  The GPU kernels take an
+    even number of modes (as the reference's GPU path, gpu/mesh.py:67): for odd N the mesh is built on N + 1
+    modes, the last one untouched by any MZI and unscreened, and returned as a ClippedMeshGPU on the first N."""
+    U = np.asarray(U, dtype=np.complex128)
+    N = U.shape[0]
+    lens, shifts = geom.reck(N)
+    if N % 2 == 0:
+        return direct(_outphase_mesh(N, lens, shifts, p_splitter, device), U)
+    from .clipped import ClippedMeshGPU
+    n_cr = sum(lens)
+    s = np.zeros((n_cr, 2)) + np.asarray(p_splitter, dtype=np.float64)
+    p, phi = direct_core(N, lens, shifts, U, s)
+    full = _outphase_mesh(N + 1, lens, shifts, p_splitter, device)
+    lay, slot = _flat_layout(lens, shifts)
+    grid = np.zeros((full.L, (N + 1) // 2, 2))
+    grid[lay, slot] = p
+    full.p_phase.copy_(torch.as_tensor(np.concatenate([grid.reshape(-1), phi, [0.0]]), dtype=full.p_phase.dtype))
+    return ClippedMeshGPU(full, slice(N), slice(N))
+
+
+def square_direct(M, p_splitter=0.0, eig: Optional[float] = None, device=None):
+    """SquareNetwork(M=M, method='direct', phi_pos='in') (square.py:103-113): the (m + n)-mode diamond mesh of
+    output-phase MZIs, screen at the input, programmed by the direct method to [[fact M, 0], [0, 0]]; returned
+    as a ClippedMeshGPU (inputs 0..n-1, outputs 0..m-1) and the scale factor fact."""
+    from scipy.linalg import eigvalsh
+
+    from .clipped import ClippedMeshGPU
+    M11 = np.array(M, dtype=np.complex128)
+    m_out, n_in = M11.shape
+    Nf = m_out + n_in
+    shifts = np.abs(np.arange(-n_in + 1, m_out))
+    lens = (Nf - shifts - shifts[::-1]) // 2
+    fact = np.sqrt(eig / eigvalsh(M11 @ M11.conj().T, subset_by_index=[m_out - 1, m_out - 1])[0]) if eig else 1.0
+    U = np.zeros((Nf, Nf), dtype=np.complex128)
+    U[:m_out, :n_in] = M11 * fact
+    full = direct(_outphase_mesh(Nf, lens.tolist(), shifts.tolist(), p_splitter, device), U)
     return ClippedMeshGPU(full, slice(n_in), slice(m_out)), fact

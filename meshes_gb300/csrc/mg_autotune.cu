@@ -35,11 +35,13 @@ extern "C" int mg_autotune(int op, int N, int L, int B, int crossing, int geomet
   int Np = 1;
   while (Np < N) Np <<= 1;
   std::vector<mg_config> cands;
-  static const int vs[3][3] = {{2, 4, 8}, {1, 2, 4}, {1, 2, 4}};
+  static const int vs[3][4] = {{1, 2, 4, 8}, {1, 2, 4, 0}, {1, 2, 4, 0}};
   for (int M : {2, 4, 8, 16}) {
     if (N > 512 || M > Np || Np / M > 32) continue;
-    for (int V : vs[op])
+    for (int V : vs[op]) {
+      if (!V) continue;
       for (int W : {2, 4, 8}) cands.push_back(mg_config{M, V, W, 0, 0, 2});
+    }
   }
   if (N > 512)   // wide meshes: 20 modes per lane
     for (int V : {1, 2})

@@ -199,7 +199,9 @@ int make_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_
   } else if (p.occ2) {
   } else if (wide ? (perm || stored || !wide_instantiated(op, crossing == CR_ORTH, V, p.gr))
            : perm ? !perm_instantiated(op, crossing == CR_ORTH, M, V, p.gr)
-                  : (stored ? !instantiated_stored(OP_BWD, M, V) : !instantiated(op, M, V)))
+                  : (stored ? !instantiated_stored(OP_BWD, M, V)
+                            : !(instantiated(op, M, V) ||
+                                (geometry == GEO_NN && nn_small_instantiated(op, p.real, M, V, p.gr, G == 32)))))
     return fail(MG_E_CONFIG, "no %skernel instantiated for op=%d M=%d V=%d",
                 wide ? "wide-mesh " : perm ? "permuted-mesh " : "", stored ? MG_OP_BWD_STORED : op, M, V);
   p.M = M; p.V = V; p.G = G; p.logG = ilog2(G); p.R = 32 / G; p.np2 = G * M / 2;
@@ -324,13 +326,17 @@ int build_tiles(const Plan& P, const int* lens, const int* shifts, const int* st
   a.dtiles = ws + P.off_dtiles; a.dlayer_bytes = P.dlb;
   a.kinds = reinterpret_cast<int*>(ws + P.off_kinds);
   a.status = reinterpret_cast<int*>(ws);
-  const int n = P.L * P.np2;
-  // one thread per slot.  The pass is bound by each SM's narrow FP64 pipe, so a small mesh is spread over
-  // every SM in blocks of 32 to 256 threads rather than packed into a few 256-thread blocks.
+  // MZI crossings without derivative tiles (forward, and back-propagation with direct gradients) take the
+  // float-float path with a quad of lanes per slot: the four sin/cos chains of a slot run side by side.  Measured
+  // on GB300 (ncu, N=64, L=64) one thread per slot spent ~8500 cycles per warp on a 1550-instruction chain; the
+  // pass is latency-bound for small meshes, so it is spread over every SM in blocks of 32 to 256 threads.
+  const bool quad = P.crossing == CR_MZI && (P.op == OP_FWD || (P.op == OP_BWD && P.gr == 1));
+  const int n = P.L * P.np2 * (quad ? 4 : 1);
   const int sms = dev_info().sms;
   int bt = 256;
   if (n < 256 * sms) bt = std::max(32, std::min(256, ((n + sms - 1) / sms + 31) / 32 * 32));
-  coef_kernel<<<(n + bt - 1) / bt, bt, 0, st>>>(a);
+  if (quad) coef_kernel<true><<<(n + bt - 1) / bt, bt, 0, st>>>(a);
+  else coef_kernel<false><<<(n + bt - 1) / bt, bt, 0, st>>>(a);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MG_OK : cuda_fail(e, "coef_kernel launch");
 }

@@ -44,6 +44,9 @@ __host__ __device__ inline int crossing_np(int c) { return c == CR_ORTH ? 1 : 2;
 __host__ __device__ inline int crossing_ns(int c) { return c == CR_MZI ? 2 : (c == CR_SYM ? 1 : 0); }
 
 // csb (MZI crossings): receives (cos, sin)(pi/4 + beta) of an active slot
+// QUAD: the four lanes of a quad compute the same slot together (mzi_T_ff_quad); only for MZI crossings
+// without derivative tiles, which the host guarantees when it launches the quad form.
+template <bool QUAD = false>
 __device__ __forceinline__ void slot_T(const CoefArgs& a, int l, int q, bool active, C2x2& T, C2x2& D0, C2x2& D1,
                                        float2* csb = nullptr) {
   if (!active) {
@@ -76,7 +79,7 @@ __device__ __forceinline__ void slot_T(const CoefArgs& a, int l, int q, bool act
     // T alone (and the splitter pair of the direct gradient) in float-float on the FP32 pipe; with derivative
     // tiles, or angles beyond the float-float range, the double-precision form
     const float al = ss ? ss[0] : 0.f, be = ss ? ss[1] : 0.f;
-    if (need_d || !mzi_T_ff(pp[0], pp[1], al, be, &T, csb))
+    if (need_d || !(QUAD ? mzi_T_ff_quad(pp[0], pp[1], al, be, &T, csb) : mzi_T_ff(pp[0], pp[1], al, be, &T, csb)))
       mzi_T(pp[0], pp[1], al, be, &T, need_d ? &D0 : nullptr, need_d ? &D1 : nullptr, csb);
   } else {   // CR_SYM
     sym_T(pp[0], pp[1], ss ? ss[0] : 0.f, &T, need_d ? &D0 : nullptr, need_d ? &D1 : nullptr);
@@ -111,14 +114,19 @@ __device__ __forceinline__ int layer_kind(const CoefArgs& a, int l, int q, bool*
   return (2 * st <= a.M) ? (ok ? e : 0) : KIND_XL + e;
 }
 
+// One thread per slot, or (QUAD) one quad of lanes per slot: a quad shares its slot, so quads leave at the bounds
+// check whole, and its first lane writes.
+template <bool QUAD>
 __global__ void coef_kernel(const CoefArgs a) {
   const int np2 = a.G * a.M / 2;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int idx = QUAD ? (t >> 2) : t;
+  const bool writer = !QUAD || (t & 3) == 0;
   if (idx >= a.L * np2) return;
   const int l = idx / np2, q = idx - l * np2;
   bool active = false;
   const int kind = layer_kind(a, l, q, &active);
-  if (q == 0) {
+  if (q == 0 && writer) {
     a.kinds[l] = kind;
     int sh = 0, ln = 0;
     if (a.geometry == GEO_NN) {
@@ -147,7 +155,8 @@ __global__ void coef_kernel(const CoefArgs a) {
   if (!real) {
     C2x2 T, D0, D1;
     float2 csv = make_float2(0.f, 0.f);   // (cos, sin)(pi/4 + beta) for the direct MZI gradient; 0 if inactive
-    slot_T(a, l, q, active, T, D0, D1, (a.op == OP_BWD && a.gr == 1) ? &csv : nullptr);
+    slot_T<QUAD>(a, l, q, active, T, D0, D1, (a.op == OP_BWD && a.gr == 1) ? &csv : nullptr);
+    if (!writer) return;
     if (a.op == OP_BWD && a.gr == 1) {
       float2* cs = reinterpret_cast<float2*>(tl + M * G);
       if (!xl) cs[e * G + j] = csv;
@@ -195,6 +204,7 @@ __global__ void coef_kernel(const CoefArgs a) {
   } else {
     R2x2 T, D0;
     slot_R(a, l, q, active, T, D0);
+    if (!writer) return;
     if (a.op == OP_BWD && a.gr == 0) {
       float4* D = reinterpret_cast<float4*>(a.dtiles + (size_t)l * a.dlayer_bytes) + slot_pos(q, M, G);
       D[0] = make_float4(D0.t00, D0.t01, D0.t10, D0.t11);

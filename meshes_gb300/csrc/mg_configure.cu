@@ -13,6 +13,13 @@
 // method) are held transposed while steps act on the left mesh (p = 0) and untransposed for the right mesh,
 // switching when p changes (configure.py:257-262, 289-292), and are returned in whichever form the last step
 // left them, as the reference's caller reads them (configure.py:246).
+//
+// mg_direct_configure is the reference's direct method (configure.py:333-410, its JIT-compiled
+// directHelper_fn): the MZIs are grouped into diagonals, each diagonal driven through its own input mode, and
+// programmed one MZI at a time from the target's column of that input (a closed-form solve of T[0][0] per MZI)
+// while a running product Upost of the diagonals already set is kept.  O(N) work per MZI plus an N x 2 column
+// update per diagonal step, sequential: host code in double precision, no propagation needed.
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <vector>
@@ -233,6 +240,143 @@ extern "C" int mg_diag_configure(int N, int K, void* U_, void* Z_, void* VdV_, v
         cols2(VdV, N, i1, T);
       }
     }
+  }
+  return MG_OK;
+}
+
+namespace {
+
+// the MZI phases (theta, phi) with T(theta, phi)[0][0] = t for splitter errors (alpha, beta) (configure.py:163-172);
+// a target outside the reachable range clips to the nearest splitting ratio, and an undefined ratio gives theta 0
+void tsolve_11(cd t, const double* s, double* out) {
+  const double Cm = std::cos(s[0] - s[1]), Sp = std::sin(s[0] + s[1]);
+  const double a = std::abs(t);
+  const double S2 = (a * a - Sp * Sp) / (Cm * Cm - Sp * Sp);
+  double h = 0.0;
+  if (!std::isnan(S2)) {
+    h = std::asin(std::sqrt(std::min(std::max(S2, 0.0), 1.0)));
+    if (std::isnan(h)) h = 0.0;
+  }
+  out[0] = 2.0 * h;
+  out[1] = angle(t) - angle(cd(-std::cos(h) * Sp, Cm * std::sin(h))) - h;
+}
+
+struct Cross {
+  int i, j, ind, d;   // layer, index in the layer, top mode, diagonal label i - ind
+};
+
+}  // namespace
+
+extern "C" int mg_direct_configure(int N, int L, const int* lens, const int* shifts, const void* U_, const double* s,
+                                   double* p, double* phi_out, int dk_max) {
+  using mg::set_last_error;
+  if (N < 2 || L < 0 || (L && (!lens || !shifts)) || !U_ || !phi_out || dk_max < 1)
+    return set_last_error(MG_E_ARG, "mg_direct_configure: bad arguments");
+  std::vector<int> inds(L + 1, 0);
+  for (int i = 0; i < L; ++i) {
+    if (lens[i] < 0 || shifts[i] < 0 || shifts[i] + 2 * lens[i] > N)
+      return set_last_error(MG_E_ARG, "mg_direct_configure: layer %d (shift %d, len %d) outside N=%d", i, shifts[i],
+                            lens[i], N);
+    inds[i + 1] = inds[i] + lens[i];
+  }
+  const int n_cr = inds[L];
+  if (n_cr && (!s || !p)) return set_last_error(MG_E_ARG, "mg_direct_configure: s or p is NULL");
+  const cd* U = static_cast<const cd*>(U_);
+  for (int k = 0; k < N; ++k) phi_out[k] = 0.0;
+
+  // diagonals (configure.py:348-350): crossings ordered by label descending, then layer descending, split where
+  // the label changes.  The reference's split drops its first piece, which holds every crossing when there is
+  // only one label, so a mesh with a single diagonal is left as it is.
+  std::vector<Cross> cr;
+  cr.reserve(n_cr);
+  int max_key = 0;
+  for (int i = 0; i < L; ++i)
+    for (int j = 0; j < lens[i]; ++j) {
+      const int ind = shifts[i] + 2 * j;
+      cr.push_back({i, j, ind, i - ind});
+      max_key = std::max(max_key, i + ind);
+    }
+  std::sort(cr.begin(), cr.end(), [](const Cross& a, const Cross& b) { return a.d != b.d ? a.d > b.d : a.i > b.i; });
+  std::vector<int> start;
+  for (int c = 0; c < n_cr; ++c)
+    if (c == 0 || cr[c].d != cr[c - 1].d) start.push_back(c);
+  if (start.size() < 2) return MG_OK;
+  start.push_back(n_cr);
+  const int n_diag = (int)start.size() - 1;
+  for (int g = 1; g < n_diag; ++g)   // each diagonal has its own input mode, increasing (configure.py:351)
+    if (cr[start[g + 1] - 1].ind <= cr[start[g] - 1].ind)
+      return set_last_error(MG_E_ARG, "mg_direct_configure: diagonals %d and %d share an input mode", g - 1, g);
+
+  // output field of each anti-diagonal i + ind: its topmost crossing's mode (configure.py:354-356)
+  const int n_of = 2 * max_key + 5;
+  std::vector<int> of(n_of, 0), is_of(n_of, 0);
+  for (const Cross& c : cr) {
+    const int key = c.i + c.ind;
+    if (!is_of[key] || c.ind < of[key]) of[key] = c.ind;
+    is_of[key] = 1;
+  }
+  // env[i]: the highest top mode of layers i..L-1 (configure.py:357)
+  std::vector<int> env(std::max(L, 1), 0);
+  for (int i = L - 1; i >= 0; --i) {
+    env[i] = shifts[i] + 2 * lens[i] - 2;
+    if (i + 1 < L) env[i] = std::max(env[i], env[i + 1]);
+  }
+
+  std::vector<cd> Upost((size_t)N * N, cd(0, 0)), w(N);
+  for (int k = 0; k < N; ++k) Upost[(size_t)k * N + k] = 1.0;
+  std::vector<M2> Tl(N + 5);
+  auto rows = [N](int k, int dk, int* r0, int* r1) {   // the rows k:k+dk of an N-row array, as numpy clips them
+    *r0 = std::min(k, N);
+    *r1 = std::max(*r0, std::min(k + dk, N));
+  };
+  for (int g = 0; g < n_diag; ++g) {
+    const int c0 = start[g], c1 = start[g + 1], len = c1 - c0;
+    const int l = cr[c1 - 1].ind;   // the diagonal's input mode
+    cd E_in = 1.0;
+    int ptr_last = 0, i = 0, ind = 0, ptr = 0;
+    std::fill(w.begin(), w.end(), cd(0, 0));
+    for (int m = 0; m < len; ++m) {   // down the diagonal: layer ascending (configure.py:383-398)
+      const Cross& c = cr[c1 - 1 - m];
+      i = c.i;
+      ind = c.ind;
+      ptr = inds[i] + c.j;
+      const int k = is_of[i + ind] ? of[i + ind] : ind;
+      const int dk = (i < L - 1) ? (is_of[i + ind + 2] ? std::min(dk_max, of[i + ind + 2] - k) : dk_max) : 1;
+      int r0, r1;
+      rows(k, dk, &r0, &r1);
+      cd num = 0, den = 0;
+      for (int r = r0; r < r1; ++r) {
+        num += U[(size_t)r * N + l] - w[r];
+        den += E_in * Upost[(size_t)r * N + ind];
+      }
+      double tp[2];
+      tsolve_11(num / den, s + 2 * ptr, tp);
+      p[2 * ptr] = tp[0];
+      if (m) p[2 * ptr_last + 1] = tp[1];
+      else phi_out[ind] = tp[1];
+      const M2 T = T_cross(tp, s + 2 * ptr, false);
+      Tl[m] = T;
+      for (int r = 0; r < N; ++r) w[r] += E_in * T.a00 * Upost[(size_t)r * N + ind];
+      E_in *= T.a10;
+      phi_out[ind + 1] = angle(U[(size_t)k * N + ind + 1]) - angle(Upost[(size_t)k * N + ind] * T.a01);
+      ptr_last = ptr;
+    }
+    // the last MZI's phi (configure.py:399-403)
+    const int k = (i == L - 1 || ind > env[i + 1]) ? ind + 1 : of[i + ind + 2];
+    const int dk = (i < L - 1) ? (is_of[i + ind + 4] ? std::min(dk_max, of[i + ind + 4] - k) : dk_max) : 1;
+    int r0, r1;
+    rows(k, dk, &r0, &r1);
+    cd num = 0, den = 0;
+    for (int r = r0; r < r1; ++r) {
+      num += U[(size_t)r * N + l] - w[r];
+      den += E_in * Upost[(size_t)r * N + ind + 1];
+    }
+    const double phi = angle(num) - angle(den);
+    p[2 * ptr + 1] = phi;
+    const cd e(std::cos(phi), std::sin(phi));
+    for (int r = 0; r < N; ++r) Upost[(size_t)r * N + ind + 1] *= e;
+    for (int m = len - 1; m >= 0; --m)   // Upost <- Upost T for the diagonal's MZIs, layer descending
+      cols2(Upost.data(), N, cr[c1 - 1 - m].ind, Tl[m]);
   }
   return MG_OK;
 }

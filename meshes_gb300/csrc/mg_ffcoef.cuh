@@ -101,14 +101,10 @@ __device__ __forceinline__ bool ff_sincos(float x, ff* s, ff* c) {
   return true;
 }
 
-// The standard MZI T (mzi_T in mg_device.cuh, reference crossing.py:216-221) and, when given, the
-// (cos, sin)(pi/4 + beta) pair of the direct gradient, in float-float; false (nothing written) when an angle
-// is outside the float-float range, and the caller takes the double path.
-__device__ __forceinline__ bool mzi_T_ff(float th, float ph, float al, float be, C2x2* T, float2* csb) {
-  ff S, C, Sph, Cph, sa, ca, sb, cb;
-  if (!ff_sincos(0.5f * th, &S, &C) || !ff_sincos(ph, &Sph, &Cph) || !ff_sincos(al, &sa, &ca) ||
-      !ff_sincos(be, &sb, &cb))
-    return false;
+// The standard MZI T (mzi_T in mg_device.cuh, reference crossing.py:216-221) from the float-float sin/cos of
+// th/2, ph, alpha and beta, and, when given, the (cos, sin)(pi/4 + beta) pair of the direct gradient.
+__device__ __forceinline__ void mzi_T_ff_from(ff S, ff C, ff Sph, ff Cph, ff sa, ff ca, ff sb, ff cb, C2x2* T,
+                                              float2* csb) {
   const ff Cp = ff_sub(ff_mul(ca, cb), ff_mul(sa, sb)), Sp = ff_add(ff_mul(sa, cb), ff_mul(ca, sb));
   const ff Cm = ff_add(ff_mul(ca, cb), ff_mul(sa, sb)), Sm = ff_sub(ff_mul(sa, cb), ff_mul(ca, sb));
   if (csb) {
@@ -124,6 +120,39 @@ __device__ __forceinline__ bool mzi_T_ff(float th, float ph, float al, float be,
   T->t01 = ffz_round(ffz_mul(E0, A01));
   T->t10 = ffz_round(ffz_mul(E1, A10));
   T->t11 = ffz_round(ffz_mul(E0, A11));
+}
+
+// mzi_T_ff_from on the angles of one thread; false (nothing written) when an angle is outside the float-float
+// range, and the caller takes the double path.
+__device__ __forceinline__ bool mzi_T_ff(float th, float ph, float al, float be, C2x2* T, float2* csb) {
+  ff S, C, Sph, Cph, sa, ca, sb, cb;
+  if (!ff_sincos(0.5f * th, &S, &C) || !ff_sincos(ph, &Sph, &Cph) || !ff_sincos(al, &sa, &ca) ||
+      !ff_sincos(be, &sb, &cb))
+    return false;
+  mzi_T_ff_from(S, C, Sph, Cph, sa, ca, sb, cb, T, csb);
+  return true;
+}
+
+// The same over the four lanes of a quad (lanes 4k..4k+3 of a warp, all given the same angles and all calling
+// it): lane k of the quad takes the sin/cos of angle k (th/2, ph, alpha, beta), the quad exchanges them by
+// shuffles, and every lane combines all four.  The four sin/cos chains, the longest part, then run side by side,
+// and the results are bitwise those of mzi_T_ff.  false on every lane of the quad when any angle is out of range.
+__device__ __forceinline__ bool mzi_T_ff_quad(float th, float ph, float al, float be, C2x2* T, float2* csb) {
+  const int lane = threadIdx.x & 31, base = lane & ~3, sub = lane & 3;
+  const unsigned qmask = 0xFu << base;
+  const float x = sub == 0 ? 0.5f * th : (sub == 1 ? ph : (sub == 2 ? al : be));
+  ff s = {0.f, 0.f}, c = {1.f, 0.f};
+  int ok = ff_sincos(x, &s, &c) ? 1 : 0;
+  ok &= __shfl_xor_sync(qmask, ok, 1);
+  ok &= __shfl_xor_sync(qmask, ok, 2);
+  if (!ok) return false;
+  ff v[4][2];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    v[k][0] = ff{__shfl_sync(qmask, s.h, base + k), __shfl_sync(qmask, s.l, base + k)};
+    v[k][1] = ff{__shfl_sync(qmask, c.h, base + k), __shfl_sync(qmask, c.l, base + k)};
+  }
+  mzi_T_ff_from(v[0][0], v[0][1], v[1][0], v[1][1], v[2][0], v[2][1], v[3][0], v[3][1], T, csb);
   return true;
 }
 

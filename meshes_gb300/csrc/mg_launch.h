@@ -76,6 +76,10 @@ cudaError_t launch_prop_perm(int op, bool real, int M, int V, int gr, const Laun
 // nearest-neighbour instantiations (layer kinds 0 and odd-shift only) of the configurations in
 // nn_instantiated(), uniform or split (mg_prop_nn.cu)
 bool nn_instantiated(int op, bool real, int M, int V, int gr, bool full, bool split);
+// the small-mesh forward tiles among them (complex, full warp, few modes and vectors per lane, so that a small
+// batch spreads over more schedulers; mg_prop_nn_small.cu)
+bool nn_small_instantiated(int op, bool real, int M, int V, int gr, bool full);
+cudaError_t launch_prop_nn_small(int M, int V, const LaunchCfg& lc, const PropArgs& a);
 cudaError_t launch_prop_nn(int op, bool real, int M, int V, int gr, bool full, bool split, const LaunchCfg& lc,
                            const PropArgs& a);
 // wide nearest-neighbour meshes (512 < N <= 640): kWideM modes in each of 32 lanes (mg_prop_wide.cu)

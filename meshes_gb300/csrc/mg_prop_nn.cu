@@ -1,6 +1,6 @@
 // Nearest-neighbour instantiations of the propagation kernel (layer kinds 0 and odd-shift only) for the
-// Clements and Reck meshes: the full-warp configurations (uniform and split) and the main runtime
-// lane-group ones.  Without the strided and butterfly layer bodies, and with one fused pair order, the
+// Clements and Reck meshes: the full-warp configurations (uniform and split) and the main runtime lane-group
+// ones; the small-mesh forward tiles are in mg_prop_nn_small.cu.  Without the strided and butterfly layer bodies, and with one fused pair order, the
 // back-propagation kernel does not spill; measured on GB300 at N=256, L=256, B=4096 it runs 9% faster than
 // the general instantiation, with identical results.
 #include "mg_launch.h"
@@ -17,6 +17,7 @@ constexpr int kNN[][6] = {{OP_FWD, 0, 8, 4, 0, 1}, {OP_FWD, 0, 16, 2, 0, 1}, {OP
 
 bool nn_instantiated(int op, bool real, int M, int V, int gr, bool full, bool split) {
   if (split && (op != OP_FWD || !full)) return false;
+  if (!split && nn_small_instantiated(op, real, M, V, gr, full)) return true;
   for (const auto& k : kNN)
     if (k[0] == op && k[1] == (real ? 1 : 0) && k[2] == M && k[3] == V && k[4] == gr && k[5] == (full ? 1 : 0))
       return true;
@@ -26,6 +27,7 @@ bool nn_instantiated(int op, bool real, int M, int V, int gr, bool full, bool sp
 cudaError_t launch_prop_nn(int op, bool real, int M, int V, int gr, bool full, bool split, const LaunchCfg& lc,
                            const PropArgs& a) {
   if (!nn_instantiated(op, real, M, V, gr, full, split)) return cudaErrorInvalidConfiguration;
+  if (!split && nn_small_instantiated(op, real, M, V, gr, full)) return launch_prop_nn_small(M, V, lc, a);
   const int key = op * 10000 + (real ? 1000 : 0) + M * 10 + V;
   if (!full) {
     switch (key) {

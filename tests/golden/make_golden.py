@@ -56,7 +56,9 @@ def import_reference(path):
     return m
 
 
-def main(ref_path):
+def main(ref_path, only=None):
+    """Write every fixture, or with only = [group, ...] just those groups of the later case functions
+    (converter, configure, direct), leaving the other files untouched."""
     meshes = import_reference(ref_path)
     mm = sys.modules["meshes.mesh"]
     from meshes.clements import ClementsNetwork
@@ -71,6 +73,13 @@ def main(ref_path):
         fn = os.path.join(HERE, name + ".npz")
         np.savez_compressed(fn, **kw)
         written.append(fn)
+
+    if only:
+        groups = {"converter": converter_cases, "configure": configure_cases, "direct": direct_cases}
+        for g in only:
+            groups[g](save)
+        print("wrote", *written, sep="\n  ")
+        return
 
     def nn_case(name, net, N, B, crossing="mzi", diff=True):
         n_p, n_s = {"mzi": (2, 2), "sym": (2, 1)}[crossing]
@@ -337,6 +346,7 @@ def main(ref_path):
 
     converter_cases(save)
     configure_cases(save)
+    direct_cases(save)
     print("wrote", *written, sep="\n  ")
 
 
@@ -372,6 +382,38 @@ def configure_cases(save):
     save("configure_square_diag_N3", N=n, method="diag", seed=seed, M=M, lens=np.array(net.full.lens),
          shifts=np.array(net.full.shifts), p_crossing=np.array(net.full.p_crossing),
          phi_out=np.array(net.full.phi_out), matrix=net.dot(np.eye(n, dtype=complex)))
+
+
+def direct_cases(save):
+    """The reference's direct method (configure.py:333-410): Reck meshes programmed with
+    ReckNetwork(M=U, p_splitter=sp, method='direct', phi_pos='in') and SquareNets with
+    SquareNetwork(M=M, method='direct', phi_pos='in') (the direct method needs no random draws).  Stored: the
+    target, splitting errors (reference flat order), geometry, the programmed crossing phases and input screen,
+    and the programmed mesh's matrix.  Own seeded stream."""
+    from meshes.reck import ReckNetwork
+    from meshes.square import SquareNetwork
+
+    rng = np.random.default_rng(20261206)
+
+    def haar(n):
+        Z = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+        Q, R = np.linalg.qr(Z)
+        return Q * (np.diag(R) / np.abs(np.diag(R)))[None, :]
+
+    for name, n, sig in (("reck_direct_N8", 8, 0.02), ("reck_direct_N5", 5, 0.0), ("reck_direct_N16", 16, 0.03)):
+        U = haar(n)
+        sp = rng.normal(0, sig, (n * (n - 1) // 2, 2)).astype(np.float32).astype(np.float64)
+        net = ReckNetwork(M=U, p_splitter=sp, method="direct", phi_pos="in")
+        save("configure_" + name, N=n, method="direct", U=U, p_splitter=sp, lens=np.array(net.lens),
+             shifts=np.array(net.shifts), p_crossing=np.array(net.p_crossing), phi_out=np.array(net.phi_out),
+             X=type(net.X).__name__, matrix=net.dot(np.eye(n, dtype=complex)))
+    for name, shape, eig in (("square_direct_N3", (3, 3), None), ("square_direct_4x2", (4, 2), 0.9)):
+        M = 0.8 * haar(max(shape))[:shape[0], :shape[1]]
+        net = SquareNetwork(M=M, method="direct", phi_pos="in", eig=eig)
+        save("configure_" + name, method="direct", M=M, eig=-1.0 if eig is None else eig, fact=net.fact,
+             lens=np.array(net.full.lens), shifts=np.array(net.full.shifts),
+             p_crossing=np.array(net.full.p_crossing), phi_out=np.array(net.full.phi_out),
+             X=type(net.full.X).__name__, matrix=net.dot(np.eye(shape[1], dtype=complex)))
 
 
 def converter_cases(save):
@@ -454,9 +496,11 @@ def converter_cases(save):
 
 
 if __name__ == "__main__":
-    if len(sys.argv) > 1:
-        main(sys.argv[1])
+    args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
+    only = [a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")]
+    if args:
+        main(args[0], only)
     elif os.environ.get("MESHES_REF"):
-        main(os.environ["MESHES_REF"])
+        main(os.environ["MESHES_REF"], only)
     else:
-        sys.exit("usage: make_golden.py /path/to/reference (or set MESHES_REF)")
+        sys.exit("usage: make_golden.py [--only=converter|configure|direct ...] /path/to/reference (or set MESHES_REF)")

@@ -154,8 +154,9 @@ def test_nearest_neighbour_launch():
 
 
 def test_full_warp_class_launch():
-    """Meshes whose vectors fill the warp (complex M = 8, N in (128, 256]) run in their own launch on the one-mesh
-    kernel's body; a launch of that class refuses an item of another mesh (MG_ST_BAD_WORK) and leaves it."""
+    """With full_warp, meshes whose vectors fill the warp (complex M = 8, N in (128, 256]) run in their own launch
+    on the one-mesh kernel's body; a launch of that class refuses an item of another mesh (MG_ST_BAD_WORK) and
+    leaves it."""
     from meshes_gb300 import _lib
     from meshes_gb300.batched import MG_BATCH_FULL_WARP, MG_BATCH_ONLY, BCLS_C8, BatchedMeshes, _bind
     rng = np.random.default_rng(57)
@@ -164,7 +165,8 @@ def test_full_warp_class_launch():
     Bs = [70, 45, 33]
     xs = [O.unit_columns(rng, om.N, B) for om, B in zip(oms, Bs)]
     gs = [O.unit_columns(rng, om.N, B) for om, B in zip(oms, Bs)]
-    bm = BatchedMeshes([gpu_mesh(om) for om in oms], Bs)
+    assert len(BatchedMeshes([gpu_mesh(om) for om in oms], Bs).groups) == 1
+    bm = BatchedMeshes([gpu_mesh(om) for om in oms], Bs, full_warp=True)
     assert [g[0] for g in bm.groups] == [MG_BATCH_ONLY(BCLS_C8) | MG_BATCH_FULL_WARP, 0]
     for st, x, g in zip(bm.states, xs, gs):
         st.x.copy_(torch.tensor(x, dtype=st.x.dtype))

@@ -5,7 +5,12 @@ and SquareNetwork(M=M, method='diag') after a recorded np.random seed).
 CPU: the native nulling pass (mg_diag_configure), started from the complex128 matrix of the seeded random
 start, reproduces the reference's programmed phases and screen to 1e-9.  GPU: the whole method, with the
 starting matrix evaluated by the propagation kernels in complex64, reproduces the programmed phases and
-screen to 1e-5 rad and the programmed mesh's matrix to 1e-5 relative error."""
+screen to 1e-5 rad and the programmed mesh's matrix to 1e-5 relative error.
+
+The direct method (configure.py:333-410) against ReckNetwork(M=U, method='direct', phi_pos='in') and
+SquareNetwork(M=M, method='direct', phi_pos='in') (configure_*_direct_*.npz): the native pass
+(mg_direct_configure) reproduces the programmed phases and input screen to 1e-9 on the CPU; on the GPU the
+programmed output-phase mesh's matrix equals the reference's to 1e-5."""
 import os
 
 import numpy as np
@@ -15,6 +20,8 @@ from oracle import meshes_oracle as O
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 RECK = ["reck_diagstar_N8", "reck_diag_N8"]
+DIRECT_RECK = ["reck_direct_N8", "reck_direct_N5", "reck_direct_N16"]
+DIRECT_SQUARE = ["square_direct_N3", "square_direct_4x2"]
 
 
 def load(name):
@@ -116,3 +123,71 @@ def test_square_programmed_on_gpu_matches_reference():
     assert np.max(np.abs(_wrap(p - z["p_crossing"]))) < 1e-5
     assert np.max(np.abs(_wrap(full.p_phase[n_grid:].double().cpu().numpy() - z["phi_out"]))) < 1e-5
     assert O.rel_err(cm.matrix().cpu().numpy(), z["matrix"]) < 1e-5
+
+
+def _direct_problem(name, z):
+    N = len(z["phi_out"])
+    if name.startswith("reck"):
+        return N, z["U"], z["p_splitter"]
+    M = z["M"] * float(z["fact"])
+    U = np.zeros((N, N), dtype=complex)
+    U[:M.shape[0], :M.shape[1]] = M
+    return N, U, np.zeros((int(z["lens"].sum()), 2))
+
+
+@pytest.mark.parametrize("name", DIRECT_RECK + DIRECT_SQUARE)
+def test_direct_pass_matches_reference(name):
+    from meshes_gb300 import configure as C
+    z = load(name)
+    assert str(z["X"]) == "MZICrossingOutPhase"
+    N, U, s = _direct_problem(name, z)
+    p, phi = C.direct_core(N, z["lens"], z["shifts"], U, s)
+    assert np.max(np.abs(_wrap(p - z["p_crossing"]))) < 1e-9
+    assert np.max(np.abs(_wrap(phi - z["phi_out"]))) < 1e-9
+
+
+def test_direct_pass_geometry_checks():
+    """A Clements layout (two diagonals driven through input 0) is refused with MG_E_ARG; a mesh of one
+    diagonal (N = 2) keeps its phases and gets a zero screen, as the reference's diagonal split leaves it."""
+    from meshes_gb300 import _lib
+    from meshes_gb300 import configure as C
+    with pytest.raises(_lib.MeshLibraryError, match="share an input mode"):
+        C.direct_core(4, [2, 1, 2, 1], [0, 1, 0, 1], np.eye(4), np.zeros((6, 2)))
+    with pytest.raises(_lib.MeshLibraryError, match="outside N"):
+        C.direct_core(4, [2, 2], [0, 1], np.eye(4), np.zeros((4, 2)))
+    p0 = np.array([[0.3, -0.2]])
+    p, phi = C.direct_core(2, [1], [0], np.eye(2), np.zeros((1, 2)), p0)
+    assert np.array_equal(p, p0) and np.array_equal(phi, np.zeros(2))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", DIRECT_RECK)
+def test_reck_direct_on_gpu_matches_reference(name):
+    from meshes_gb300 import configure as C
+    z = load(name)
+    N = int(z["N"])
+    m = C.reck(z["U"], p_splitter=z["p_splitter"], method="direct", device="cuda")
+    full = m.full if N % 2 else m                      # odd N: an (N + 1)-mode mesh clipped to N ports
+    Nf = full.N
+    lay, slot = C._flat_layout(full.mesh.lens_h, full.mesh.shifts_h)
+    n_grid = full.L * (Nf // 2) * 2
+    p = full.p_phase[:n_grid].reshape(full.L, Nf // 2, 2).cpu().numpy()[lay, slot]
+    assert np.max(np.abs(_wrap(p - z["p_crossing"]))) < 1e-9
+    assert np.max(np.abs(_wrap(full.p_phase[n_grid:n_grid + N].cpu().numpy() - z["phi_out"]))) < 1e-9
+    U = m.matrix().cpu().numpy()
+    assert U.shape == (N, N)
+    assert O.rel_err(U, z["matrix"]) < 1e-5
+    assert O.rel_err(U, z["U"]) < 1e-5
+    assert full.status() == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", DIRECT_SQUARE)
+def test_square_direct_on_gpu_matches_reference(name):
+    from meshes_gb300 import configure as C
+    z = load(name)
+    eig = float(z["eig"])
+    cm, fact = C.square(z["M"], eig=None if eig < 0 else eig, device="cuda", method="direct")
+    assert abs(fact - float(z["fact"])) < 1e-12
+    assert O.rel_err(cm.matrix().cpu().numpy(), z["matrix"]) < 1e-5
+    assert O.rel_err(cm.matrix().cpu().numpy(), fact * z["M"]) < 1e-5

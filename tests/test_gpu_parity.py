@@ -531,3 +531,35 @@ def test_conjugated_and_negated_views():
     dp1, g1 = m.grad_phi(v, g.conj())
     dp2, g2 = m.grad_phi(v.resolve_conj(), g.conj().resolve_conj())
     assert torch.equal(dp1, dp2) and torch.equal(g1, g2)
+
+
+@pytest.mark.parametrize("geo", ["clements", "reck"])
+@pytest.mark.parametrize("N,M,V", [(64, 2, 1), (64, 2, 2), (64, 2, 4), (40, 2, 2), (128, 4, 1), (96, 4, 2)])
+def test_small_mesh_forward_tiles(geo, N, M, V):
+    """The small-mesh nearest-neighbour forward tiles (2 or 4 modes and 1 to 4 vectors per lane, a vector over the
+    whole warp) on ragged batches, with and without splitter errors, against the oracle; the plan reports the
+    requested tile."""
+    from meshes_gb300 import _lib
+    import ctypes
+    lib = _lib.load()
+    rng = np.random.default_rng(N * 7 + M * 3 + V)
+    for sig, B in ((0.0, 1024), (0.02, 77)):
+        om = O.random_mesh(rng, N, geo, "mzi", sig)
+        x = O.unit_columns(rng, N, B)
+        m = gpu_mesh(om)
+        xd = torch.tensor(x, dtype=torch.complex64, device="cuda")
+        y = torch.empty_like(xd)
+        st = torch.cuda.current_stream().cuda_stream
+        s = m.p_splitter
+        cfg = _lib.config(M, V, 0, 0, 0, 2)
+        info = _lib.mg_plan_info()
+        assert lib.mg_plan(0, N, om.L, B, m.crossing, 0, _lib.cfg_ptr(cfg), ctypes.byref(info)) == 0, _lib.last_error()
+        assert (info.M, info.V, info.G) == (M, V, 32)
+        ws = torch.zeros(info.total, dtype=torch.uint8, device="cuda")
+        assert lib.mg_build_tiles(0, N, om.L, 0, m.lens.data_ptr(), m.shifts.data_ptr(), None, m.crossing,
+                                  m.p_phase.data_ptr(), N, s.data_ptr() if s.numel() else None, N, None, None, None,
+                                  B, _lib.cfg_ptr(cfg), ws.data_ptr(), info.total, st) == 0, _lib.last_error()
+        assert lib.mg_propagate(0, N, om.L, B, m.crossing, 0, xd.data_ptr(), None, y.data_ptr(), None, N, None, 0, 0,
+                                _lib.cfg_ptr(cfg), ws.data_ptr(), info.total, st) == 0, _lib.last_error()
+        assert lib.mg_read_status(ws.data_ptr(), 0, st) == 0
+        assert O.rel_err(y.cpu().numpy(), O.propagate(om, x)) < TOL
