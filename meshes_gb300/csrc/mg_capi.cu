@@ -18,6 +18,7 @@
 
 #include "../../include/meshes_gb300.h"
 #include "mg_coeffs.cuh"
+#include "mg_reduce.cuh"
 #include "mg_inst_table.h"
 #include "mg_launch.h"
 
@@ -308,12 +309,8 @@ int check_params(const Plan& p, const float* pp, int ldp, const float* s, int ld
   return MG_OK;
 }
 
-int build_tiles(const Plan& P, const int* lens, const int* shifts, const int* strides, const float* p, int ldp,
-                const float* s, int lds, const float* dp, const void* Tgen, const void* Dgen, unsigned char* ws,
-                cudaStream_t st) {
-  if (P.L == 0) return MG_OK;
-  if (P.geometry == GEO_NN && (!lens || !shifts)) return fail(MG_E_ARG, "lens/shifts are NULL");
-  if (P.geometry == GEO_FFT && !strides) return fail(MG_E_ARG, "strides is NULL");
+CoefArgs coef_args(const Plan& P, const int* lens, const int* shifts, const int* strides, const float* p, int ldp,
+                   const float* s, int lds, const float* dp, const void* Tgen, const void* Dgen, unsigned char* ws) {
   CoefArgs a;
   a.N = P.N; a.L = P.L; a.crossing = P.crossing; a.geometry = P.geometry; a.op = P.op;
   a.gr = P.gr;
@@ -326,11 +323,24 @@ int build_tiles(const Plan& P, const int* lens, const int* shifts, const int* st
   a.dtiles = ws + P.off_dtiles; a.dlayer_bytes = P.dlb;
   a.kinds = reinterpret_cast<int*>(ws + P.off_kinds);
   a.status = reinterpret_cast<int*>(ws);
+  return a;
+}
+
+// MZI crossings without derivative tiles take the float-float quad form of the coefficient pass
+bool quad_coef(const Plan& P) { return P.crossing == CR_MZI && (P.op == OP_FWD || (P.op == OP_BWD && P.gr == 1)); }
+
+int build_tiles(const Plan& P, const int* lens, const int* shifts, const int* strides, const float* p, int ldp,
+                const float* s, int lds, const float* dp, const void* Tgen, const void* Dgen, unsigned char* ws,
+                cudaStream_t st) {
+  if (P.L == 0) return MG_OK;
+  if (P.geometry == GEO_NN && (!lens || !shifts)) return fail(MG_E_ARG, "lens/shifts are NULL");
+  if (P.geometry == GEO_FFT && !strides) return fail(MG_E_ARG, "strides is NULL");
+  const CoefArgs a = coef_args(P, lens, shifts, strides, p, ldp, s, lds, dp, Tgen, Dgen, ws);
   // MZI crossings without derivative tiles (forward, and back-propagation with direct gradients) take the
   // float-float path with a quad of lanes per slot: the four sin/cos chains of a slot run side by side.  Measured
   // on GB300 (ncu, N=64, L=64) one thread per slot spent ~8500 cycles per warp on a 1550-instruction chain; the
   // pass is latency-bound for small meshes, so it is spread over every SM in blocks of 32 to 256 threads.
-  const bool quad = P.crossing == CR_MZI && (P.op == OP_FWD || (P.op == OP_BWD && P.gr == 1));
+  const bool quad = quad_coef(P);
   const int n = P.L * P.np2 * (quad ? 4 : 1);
   const int sms = dev_info().sms;
   int bt = 256;
@@ -359,10 +369,8 @@ void set_perm_args(const Plan& P, unsigned char* ws, int l0, int l1, PropArgs& a
   }
 }
 
-int run_prop(const Plan& P, const void* in0, const void* in1, void* out0, void* out1, int ldu, float* dp, int ldp,
-             int accumulate, unsigned char* ws, cudaStream_t st, const void* target = nullptr, void* ckpt = nullptr,
-             int ckpt_every = 0, unsigned long long wait_ns = 0, int unarmed = 0) {
-  if (P.B == 0) return MG_OK;
+PropArgs prop_args(const Plan& P, const void* in0, const void* in1, void* out0, void* out1, int ldu, unsigned char* ws,
+                   const void* target, void* ckpt, int ckpt_every, unsigned long long wait_ns, int unarmed) {
   PropArgs a{};
   a.wait_ns = wait_ns;
   a.unarmed = unarmed;
@@ -381,13 +389,21 @@ int run_prop(const Plan& P, const void* in0, const void* in1, void* out0, void* 
   a.ckpt_every = ckpt_every;
   a.ckpt_plane = (size_t)P.B * ldu;
   set_perm_args(P, ws, 0, P.L, a);
+  a.nA = P.nA;
+  return a;
+}
+
+int run_prop(const Plan& P, const void* in0, const void* in1, void* out0, void* out1, int ldu, float* dp, int ldp,
+             int accumulate, unsigned char* ws, cudaStream_t st, const void* target = nullptr, void* ckpt = nullptr,
+             int ckpt_every = 0, unsigned long long wait_ns = 0, int unarmed = 0) {
+  if (P.B == 0) return MG_OK;
+  PropArgs a = prop_args(P, in0, in1, out0, out1, ldu, ws, target, ckpt, ckpt_every, wait_ns, unarmed);
   LaunchCfg lc;
   lc.grid = dim3(P.grid);
   lc.block = dim3(32 * P.W);
   lc.smem = P.smem;
   lc.stream = st;
   cudaError_t e;
-  a.nA = P.nA;
   if (P.pair)
     e = launch_prop_pair(P.V, lc, a);
   else if (P.occ2)
