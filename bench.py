@@ -902,7 +902,14 @@ def run_plain_forward(args, peak):
         with torch.cuda.graph(g):
             capi_call()
         t_dev = event_ms(torch, g.replay, reps, warm=3, flush=flush)
-        # calls issued back to back (the device time per call once the host runs ahead)
+        # device time per call without launch latency: 50 calls recorded in one graph, L2 flushed before each replay
+        k_calls = 50
+        gk = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(gk):
+            for _ in range(k_calls):
+                capi_call()
+        t_dev_k = event_ms(torch, gk.replay, max(5, reps // 10), warm=2, flush=flush) / k_calls
+        # calls issued back to back from the host (bound by the host's issue rate for a call this short)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         for _ in range(reps):
@@ -916,10 +923,14 @@ def run_plain_forward(args, peak):
     n_mzi = int(mask.sum())
     err = cpu_forward_check(nc, lens, shifts, p, None, x_h, y_h)
     return {"metric": "MZI-apps/s (fwd)", "value": n_mzi * bc / t, "unit": "MZI-apps/s", "ms": t * 1e3,
-            "ms_c_call": t_capi * 1e3, "ms_graph": t_dev * 1e3, "ms_back_to_back": t_b2b * 1e3,
+            "ms_c_call": t_capi * 1e3, "ms_graph": t_dev * 1e3, "ms_device_per_call": t_dev_k * 1e3,
+            "ms_back_to_back": t_b2b * 1e3,
             "timing": "ms: one MeshNetworkGPU.dot call between CUDA events, L2 flushed before (host work included); "
                       "ms_c_call: one mg_fwdprop call with prepared arguments; ms_graph: that call replayed from a "
-                      "CUDA graph; ms_back_to_back: per call of many issued without synchronisation",
+                      "CUDA graph (graph launch latency included); ms_device_per_call: 50 calls in one graph, per "
+                      "call (the device time of the coefficient pass, the propagation and the boundary between "
+                      "them); ms_back_to_back: per call of many issued from the host without synchronisation "
+                      "(bound by the host's issue rate)",
             "config": {"workload": "clements_mzi_N64_L64_B1024_fwd", "n_mzi": n_mzi, "B": bc,
                        "call": "MeshNetworkGPU.dot -> mg_fwdprop (coefficient pass + propagation)",
                        "l2": "flushed between timed calls"},
