@@ -372,3 +372,93 @@ def square_direct(M, p_splitter=0.0, eig: Optional[float] = None, device=None):
     U[:m_out, :n_in] = M11 * fact
     full = direct(_outphase_mesh(Nf, lens.tolist(), shifts.tolist(), p_splitter, device), U)
     return ClippedMeshGPU(full, slice(n_in), slice(m_out)), fact
+
+
+# ---- local error correction
+
+def _mzi_T(p, s) -> np.ndarray:
+    """(2, 2, n) transfer matrices of MZI crossings, p (n, 2) = (theta, phi), s (n, 2) = (alpha, beta): the
+    reference's MZICrossing.T (crossing.py:216-221)."""
+    th, ph = p[:, 0], p[:, 1]
+    a, b = s[:, 0], s[:, 1]
+    Cp, Cm, C = np.cos(a + b), np.cos(a - b), np.cos(th / 2)
+    Sp, Sm, S = np.sin(a + b), np.sin(a - b), np.sin(th / 2)
+    f = np.exp(1j * ph)
+    return np.exp(1j * th / 2) * np.array([[f * (1j * S * Cm - C * Sp), 1j * C * Cp - S * Sm],
+                                           [f * (1j * C * Cp + S * Sm), -1j * S * Cm - C * Sp]])
+
+
+def _solve_row0(t0, t1, s) -> np.ndarray:
+    """(theta, phi) per MZI (n, 2) whose first row is proportional to (t0, t1), for splitting errors s (n, 2):
+    the reference's MZICrossing.Tsolve(..., 'T1:') (crossing.py:246-251); unreachable ratios clip to the
+    nearest splitting ratio."""
+    a, b = s[:, 0], s[:, 1]
+    Cp, Cm, Sp, Sm = np.cos(a + b), np.cos(a - b), np.sin(a + b), np.sin(a - b)
+    R2 = np.abs(t1) ** 2 / (np.abs(t0) ** 2 + 1e-30)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        S2 = (Cp ** 2 - R2 * Sp ** 2) / ((Cp ** 2 - Sm ** 2) + R2 * (Cm ** 2 - Sp ** 2))
+        h = np.nan_to_num(np.arcsin(np.sqrt(np.clip(S2, 0, 1))), nan=0.0, posinf=0.0, neginf=0.0)
+    C, S = np.cos(h), np.sin(h)
+    phi = np.angle(1j * C * Cp - S * Sm) - np.angle(1j * Cm * S - C * Sp) + np.angle(t0) - np.angle(t1)
+    return np.stack([2 * h, phi], axis=1)
+
+
+def errcorr_core(N: int, lens, shifts, p0, s0, s1, perm_rows=None):
+    """Local error correction (reference configure.py:412-433, errcorr_local; S. Bandyopadhyay et al.,
+    arXiv:2103.04993) on flat arrays: a nearest-neighbour MZI mesh of N modes (lens, shifts) with phases p0 (n_cr, 2) realises
+    its matrix with splitting errors s0; returns the phases p1 (n_cr, 2) that, with splitting errors s1, match each
+    MZI's first row up to output phases, and the phases (N,) those leave at the output, which the caller adds to the
+    output screen.  perm_rows: (L + 1, N) gather rows between layers (row i before layer i, row L after the last),
+    or None.  Host code: one vectorised solve per layer."""
+    lens = [int(v) for v in lens]
+    shifts = [int(v) for v in shifts]
+    p0 = np.asarray(p0, dtype=np.float64).reshape(-1, 2)
+    n_cr = p0.shape[0]
+    s0 = np.broadcast_to(np.asarray(s0, dtype=np.float64), (n_cr, 2))
+    s1 = np.broadcast_to(np.asarray(s1, dtype=np.float64), (n_cr, 2))
+    phase = np.zeros(int(N))
+    p1 = np.zeros((n_cr, 2))
+    ind = 0
+    for i, (ln, sh) in enumerate(zip(lens, shifts)):
+        if perm_rows is not None:
+            phase = phase[np.asarray(perm_rows[i])]
+        sl = slice(ind, ind + ln)
+        psi = phase[sh:sh + 2 * ln]
+        T0 = _mzi_T(p0[sl], s0[sl])
+        T0[:, 0, :] *= np.exp(1j * psi[::2])
+        T0[:, 1, :] *= np.exp(1j * psi[1::2])
+        p1[sl] = _solve_row0(T0[0, 0], T0[0, 1], s1[sl])
+        with np.errstate(invalid="ignore", divide="ignore"):
+            phase[sh:sh + 2 * ln] = np.angle(T0 / _mzi_T(p1[sl], s1[sl]))[:, 0, :].T.reshape(-1)
+        ind += ln
+    if perm_rows is not None:
+        phase = phase[np.asarray(perm_rows[len(lens)])]
+    return p1, phase
+
+
+def errcorr_local(mesh: MeshNetworkGPU, p_splitter) -> MeshNetworkGPU:
+    """A copy of mesh (nearest-neighbour MZI crossings, phase screen at the output or none) reprogrammed for the
+    splitting errors p_splitter (scalar or (n_cr, 2) in the reference's flat order) by local error correction
+    (reference configure.py:412-433): each MZI's first row is matched up to phases, which are carried forward and
+    added to the output screen.  The result has an output screen."""
+    if mesh.X != "mzi" or mesh.geometry != geom_nn():
+        raise ValueError("local error correction takes nearest-neighbour meshes of MZI crossings")
+    if mesh.is_phase and mesh.phi_pos != "out":
+        raise ValueError("local error correction adds its phases to an output screen")
+    N, L = mesh.N, mesh.L
+    lay, slot = _flat_layout(mesh.lens_h, mesh.shifts_h)
+    n_grid = L * (N // 2) * 2
+    grid = mesh.p_phase[:n_grid].detach().double().cpu().numpy().reshape(L, N // 2, 2)
+    sp = mesh.p_splitter
+    s0 = sp.detach().double().cpu().numpy()[lay, slot] if sp.numel() else np.zeros((len(lay), 2))
+    s1 = np.broadcast_to(np.asarray(p_splitter, dtype=np.float64), (len(lay), 2))
+    perm = None if mesh.perm_table is None else np.asarray(mesh.perm_h)
+    p1, phase = errcorr_core(N, mesh.lens_h, mesh.shifts_h, grid[lay, slot], s0, s1, perm)
+    screen = mesh.p_phase[n_grid:].detach().double().cpu().numpy() if mesh.is_phase else np.zeros(N)
+    g1 = np.zeros((L, N // 2, 2))
+    g1[lay, slot] = p1
+    gs = np.zeros((L, N // 2, 2))
+    gs[lay, slot] = s1
+    return MeshNetworkGPU(N, L, mesh.lens_h, mesh.shifts_h, np.concatenate([g1.reshape(-1), screen + phase]),
+                          gs.astype(np.float32), "mzi", phi_pos="out", is_phase=True, device=mesh.device,
+                          perm=None if perm is None else [row for row in perm])

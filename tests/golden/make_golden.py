@@ -75,7 +75,8 @@ def main(ref_path, only=None):
         written.append(fn)
 
     if only:
-        groups = {"converter": converter_cases, "configure": configure_cases, "direct": direct_cases}
+        groups = {"converter": converter_cases, "configure": configure_cases, "direct": direct_cases,
+                  "errcorr": errcorr_cases}
         for g in only:
             groups[g](save)
         print("wrote", *written, sep="\n  ")
@@ -347,6 +348,7 @@ def main(ref_path, only=None):
     converter_cases(save)
     configure_cases(save)
     direct_cases(save)
+    errcorr_cases(save)
     print("wrote", *written, sep="\n  ")
 
 
@@ -414,6 +416,47 @@ def direct_cases(save):
              lens=np.array(net.full.lens), shifts=np.array(net.full.shifts),
              p_crossing=np.array(net.full.p_crossing), phi_out=np.array(net.full.phi_out),
              X=type(net.full.X).__name__, matrix=net.dot(np.eye(shape[1], dtype=complex)))
+
+
+def errcorr_cases(save):
+    """The reference's local error correction (configure.py:412-433, errcorr_local): a Clements mesh with ideal
+    splitters and a permuted nearest-neighbour mesh with splitting errors, both with random phases, each corrected
+    for random splitting errors.  Stored: geometry, permutation rows, the target's phases, splitters and screen, the new
+    splitting errors, the corrected phases and screen, and both matrices.  Own seeded stream."""
+    from meshes.clements import ClementsNetwork
+    from meshes.configure import errcorr_local
+    from meshes.mesh import StructuredMeshNetwork
+
+    rng = np.random.default_rng(20261207)
+
+    def f32(a):
+        return np.asarray(a, np.float64).astype(np.float32).astype(np.float64)
+
+    def record(name, net, sp):
+        N = net.N
+        p0, s0 = np.array(net.p_crossing), np.array(net.p_splitter) * np.ones((net.n_cr, 2))
+        phi0 = np.array(net.phi_out)
+        U0 = net.dot(np.eye(N, dtype=complex))
+        out = errcorr_local(net, sp)
+        rows = np.array([np.arange(N) if r is None else np.asarray(r) for r in net.perm])
+        save("errcorr_" + name, N=N, lens=np.array(net.lens), shifts=np.array(net.shifts), perm_rows=rows,
+             perm_none=np.array([r is None for r in net.perm]), p_crossing0=p0, p_splitter0=s0, phi_out0=phi0,
+             p_splitter=sp, p_crossing=np.array(out.p_crossing), phi_out=np.array(out.phi_out), matrix0=U0,
+             matrix=out.dot(np.eye(N, dtype=complex)))
+
+    # (random phases: the decomposition ClementsNetwork(M=U) calls np.nan_to_num with a positional copy=0 on
+    # scalars, which NumPy 2 refuses; errcorr_local itself passes arrays)
+    net = ClementsNetwork(N=8)
+    net.p_crossing[:] = f32(rng.uniform(0, 2 * np.pi, net.p_crossing.shape))
+    net.phi_out[:] = f32(rng.uniform(0, 2 * np.pi, 8))
+    record("clements_N8", net, f32(rng.normal(0, 0.05, (net.n_cr, 2))))
+    N, lens, shifts = 8, [4, 3, 4, 3, 4, 3], [0, 1, 0, 1, 0, 1]
+    perm = [None, rng.permutation(N), None, rng.permutation(N), None, None, rng.permutation(N)]
+    n_cr = sum(lens)
+    net = StructuredMeshNetwork(N, lens, shifts, p_crossing=f32(rng.uniform(0, 2 * np.pi, (n_cr, 2))),
+                                phi_out=f32(rng.uniform(0, 2 * np.pi, N)), perm=perm,
+                                p_splitter=f32(rng.normal(0, 0.02, (n_cr, 2))))
+    record("perm_N8", net, f32(rng.normal(0, 0.05, (n_cr, 2))))
 
 
 def converter_cases(save):
@@ -503,4 +546,5 @@ if __name__ == "__main__":
     elif os.environ.get("MESHES_REF"):
         main(os.environ["MESHES_REF"], only)
     else:
-        sys.exit("usage: make_golden.py [--only=converter|configure|direct ...] /path/to/reference (or set MESHES_REF)")
+        sys.exit("usage: make_golden.py [--only=converter|configure|direct|errcorr ...] /path/to/reference "
+                 "(or set MESHES_REF)")

@@ -191,3 +191,49 @@ def test_square_direct_on_gpu_matches_reference(name):
     assert abs(fact - float(z["fact"])) < 1e-12
     assert O.rel_err(cm.matrix().cpu().numpy(), z["matrix"]) < 1e-5
     assert O.rel_err(cm.matrix().cpu().numpy(), fact * z["M"]) < 1e-5
+
+
+ERRCORR = ["clements_N8", "perm_N8"]
+
+
+def _errcorr(name):
+    z = np.load(os.path.join(GOLDEN, "errcorr_%s.npz" % name))
+    perm = None if z["perm_none"].all() else z["perm_rows"]
+    return z, perm
+
+
+@pytest.mark.parametrize("name", ERRCORR)
+def test_errcorr_core_matches_reference(name):
+    """Local error correction (configure.py:412-433) on the host: the corrected phases and the phases added to
+    the output screen equal the reference's errcorr_local (to 1e-9; a Clements mesh and a permuted mesh)."""
+    from meshes_gb300 import configure as C
+    z, perm = _errcorr(name)
+    p1, phase = C.errcorr_core(int(z["N"]), z["lens"], z["shifts"], z["p_crossing0"], z["p_splitter0"],
+                               z["p_splitter"], perm)
+    assert np.max(np.abs(_wrap(p1 - z["p_crossing"]))) < 1e-9
+    assert np.max(np.abs(_wrap(z["phi_out0"] + phase - z["phi_out"]))) < 1e-9
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ERRCORR)
+def test_errcorr_on_gpu_matches_reference(name):
+    """errcorr_local on a MeshNetworkGPU: the corrected mesh (new splitting errors) propagates on the GPU to the
+    reference's corrected matrix within 1e-5, and the uncorrected mesh to the reference's target matrix."""
+    from meshes_gb300 import MeshNetworkGPU
+    from meshes_gb300 import configure as C
+    z, perm = _errcorr(name)
+    N = int(z["N"])
+    lens, shifts = z["lens"].tolist(), z["shifts"].tolist()
+    L = len(lens)
+    lay, slot = C._flat_layout(lens, shifts)
+    grid = np.zeros((L, N // 2, 2))
+    grid[lay, slot] = z["p_crossing0"]
+    sgrid = np.zeros((L, N // 2, 2))
+    sgrid[lay, slot] = z["p_splitter0"]
+    rows = None if perm is None else [None if none else row for row, none in zip(perm, z["perm_none"])]
+    m = MeshNetworkGPU(N, L, lens, shifts, np.concatenate([grid.reshape(-1), z["phi_out0"]]), sgrid.astype(np.float32),
+                       "mzi", phi_pos="out", is_phase=True, device="cuda", perm=rows)
+    assert O.rel_err(m.matrix().cpu().numpy(), z["matrix0"]) < 1e-5
+    m1 = C.errcorr_local(m, z["p_splitter"])
+    assert O.rel_err(m1.matrix().cpu().numpy(), z["matrix"]) < 1e-5
+    assert m1.status() == 0
