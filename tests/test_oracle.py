@@ -16,7 +16,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def fixtures():
     """Fixtures of the plain meshes (the phase-screen and lossy fixtures have their own tests)."""
     return sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz") and "_screen_" not in f and "lossy" not in f
-                  and not f.startswith(("clipped_", "perm_", "piloss_", "xmesh_", "crossings_", "converter_", "configure_")))
+                  and not f.startswith(("clipped_", "perm_", "piloss_", "xmesh_", "crossings_", "converter_", "configure_", "errcorr_")))
 
 
 def load(name):
