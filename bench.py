@@ -371,6 +371,124 @@ def cpu_baseline_forward(n, lens, shifts, p, s, x, seconds=2.0):
             "kind": "port", "sample": "the full batch, forward (mode 0), complex64, median of %d" % len(times)}
 
 
+def cpu_timed(run, seconds):
+    """Median seconds of run() over at least 2 repetitions lasting about `seconds` (one warm-up call first)."""
+    run()
+    times, t0 = [], time.perf_counter()
+    while time.perf_counter() - t0 < seconds or len(times) < 2:
+        a = time.perf_counter()
+        run()
+        times.append(time.perf_counter() - a)
+    return statistics.median(times), len(times)
+
+
+def cpu_baseline_batched(prob, seconds=8.0):
+    """The batched workload on the host: every mesh's forward (mode 0) and back-propagation (mode 2) through the
+    port in complex64 on all host cores, one call per mesh as the reference's CPU path would (T built per call,
+    mesh.py:97-113); MZI-apps/s of whole passes."""
+    O, P = _cpu_modules()
+    fns = P.port_lib()
+    threads = host_threads()
+    oms = [cpu_oracle_mesh(d["N"], d["lens"], d["shifts"], d["p"], d["s"], d["cr"]) for d in prob]
+
+    def run():
+        for om, d in zip(oms, prob):
+            y = P.forward(fns, om, d["x"], threads=threads, dtype=np.complex64)
+            P.vjp(fns, om, y, d["gy"], threads=threads, dtype=np.complex64)
+
+    t, n = cpu_timed(run, seconds)
+    units = sum(d["n_mzi"] * d["B"] for d in prob)
+    return {"value": units / t, "unit": "MZI-apps/s", "cores": threads, "kind": "port",
+            "sample": "whole passes over the %d meshes (fwd + bwd, complex64), median of %d" % (len(prob), n)}
+
+
+def cpu_baseline_fit(lens, shifts, p0, s0, Ut, seconds=6.0):
+    """Unitary-fitting steps on the host: forward of the identity batch and back-propagation through the port
+    (complex64, all cores), dJ/dp contracted from dJ/dT, and an Adam update in numpy; steps/s."""
+    O, P = _cpu_modules()
+    fns = P.port_lib()
+    threads = host_threads()
+    n = Ut.shape[0]
+    p = p0.astype(np.float64).copy()
+    m1, m2 = np.zeros_like(p), np.zeros_like(p)
+    x = np.eye(n, dtype=np.complex64)
+    k = [0]
+
+    def run():
+        om = cpu_oracle_mesh(n, lens, shifts, p.astype(np.float32), s0)
+        y = P.forward(fns, om, x, threads=threads, dtype=np.complex64)
+        G, _ = P.vjp(fns, om, y, 2 * (y - Ut.T), threads=threads, dtype=np.complex64)
+        g = O.contract_dp(om, G)
+        k[0] += 1
+        m1[:] = 0.9 * m1 + 0.1 * g
+        m2[:] = 0.999 * m2 + 0.001 * g * g
+        p[:] -= 1e-2 * (m1 / (1 - 0.9 ** k[0])) / (np.sqrt(m2 / (1 - 0.999 ** k[0])) + 1e-8)
+
+    t, n_steps = cpu_timed(run, seconds)
+    return {"value": 1.0 / t, "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": "%d Adam steps of the same fit (fwd + bwd through the port, complex64; dJ/dp and Adam in "
+                      "numpy), median step" % n_steps}
+
+
+def cpu_baseline_served(meshes_h, pools, mesh_ids, bsz, grad, n_req=2000):
+    """The served stream's first n_req requests processed one after another on the host: Clements meshes through
+    the port (complex64, all cores), butterflies through the numpy restatement (complex128); MZI-apps/s and
+    requests/s of compute alone (no queueing)."""
+    O, P = _cpu_modules()
+    fns = P.port_lib()
+    threads = host_threads()
+    oms = [cpu_oracle_mesh(d["N"], d["lens"], d["shifts"], d["p"], d["s"], "mzi", d["strides"]) for d in meshes_h]
+    n_req = min(n_req, len(mesh_ids))
+    apps = 0.0
+    per = []
+    t0 = time.perf_counter()
+    for k in range(n_req):
+        i, b = int(mesh_ids[k]), int(bsz[k])
+        om, d, x = oms[i], meshes_h[i], pools[int(mesh_ids[k])][:b]
+        a = time.perf_counter()
+        if d["strides"] is None:
+            y = P.forward(fns, om, x, threads=threads, dtype=np.complex64)
+            if grad[k]:
+                G, _ = P.vjp(fns, om, y, x, threads=threads, dtype=np.complex64)
+                O.contract_dp(om, G)
+        else:
+            y = O.propagate(om, x)
+            if grad[k]:
+                G, _, _ = O.vjp_unitary(om, y, x)
+                O.contract_dp(om, G)
+        per.append(time.perf_counter() - a)
+        apps += d["n_mzi"] * b * (2 if grad[k] else 1)
+    span = time.perf_counter() - t0
+    return {"value": apps / span, "unit": "MZI-apps/s", "cores": threads, "kind": "port",
+            "req_per_s": n_req / span, "per_request_ms_p50": 1e3 * float(np.median(per)),
+            "per_request_ms_p99": 1e3 * float(np.percentile(per, 99)),
+            "sample": "the stream's first %d requests, one after another (Clements through the port in complex64, "
+                      "butterflies through the numpy restatement in complex128)" % n_req}
+
+
+def cpu_baseline_lossy(lens, shifts, p, s14, x, yt, n_vec=32, seconds=6.0):
+    """Lossy generic MZIs on the host: the reference's CPU path has no gradient for this crossing (its dot_vjp
+    inverts T by T^H), so the baseline is the port's forward (complex64, all cores, full batch) plus the oracle's
+    stored-activation adjoint (numpy, complex128) on n_vec vectors, combined per vector."""
+    O, P = _cpu_modules()
+    fns = P.port_lib()
+    threads = host_threads()
+    om = cpu_oracle_mesh(N, lens, shifts, p, s14, "mzi_generic")
+    t_fwd, n_f = cpu_timed(lambda: P.forward(fns, om, x, threads=threads, dtype=np.complex64), seconds / 2)
+    xs = x[:n_vec]
+
+    def adjoint():
+        y = O.propagate(om, xs)
+        O.vjp_stored(om, xs, 2 * (y - yt[:n_vec]))
+
+    t_adj, n_a = cpu_timed(adjoint, seconds / 2)
+    n_mzi = int(active_mask(N, lens, shifts).sum())
+    per_vec = t_fwd / x.shape[0] + t_adj / n_vec
+    return {"value": n_mzi / per_vec, "unit": "MZI-apps/s", "cores": threads, "kind": "port",
+            "sample": "forward of the full batch through the port (median of %d) plus forward and stored-activation "
+                      "adjoint of %d vectors in numpy (median of %d), per vector" % (n_f, n_vec, n_a)}
+
+
 def cpu_check_batched(prob, outs):
     """Per-mesh errors of the batched forward + backward against the complex128 port: y = U x, g_x = U^H g_y,
     dJ/dp; the maximum over the meshes of each."""
@@ -1041,6 +1159,7 @@ def run_batched(args, peak):
             "roofline": roofline_fp32((flops_f + flops_b) / t_bat_fb, peak,
                                       "batched_kernel (forward + back-propagation launches and reduce)"),
             "roofline_fwd": roofline_fp32(flops_f / t_bat_f, peak, "batched_kernel (forward launch)"),
+            "cpu_baseline": cpu_baseline_batched(prob),
             "clocks": cs.summary(), "status": status}
 
 
@@ -1122,6 +1241,7 @@ def run_unitary_fit(args, peak):
                                       "whole Adam step (forward, back-propagation, optimizer) as one CUDA graph"),
             "timing": "host wall clock per optimisation step (fwd + bwd + Adam), device synchronised; "
                       "headline: CUDA-graph replay of the whole step",
+            "cpu_baseline": cpu_baseline_fit(lens, shifts, p0, s0, Ut),
             "clocks": cs.summary()}
 
 
@@ -1181,6 +1301,7 @@ def run_lossy(args, peak):
                                    "gradient is checked against central differences by the GPU tests)" % n_chk},
             "roofline": roofline_fp32(n_mzi * B * (FLOP_FWD + FLOP_BWD) / t, peak,
                                       "lossy step (the reference's 32 + 96 FLOP per MZI-application)"),
+            "cpu_baseline": cpu_baseline_lossy(lens, shifts, p, s14, x_h, yt_h),
             "clocks": cs.summary(), "status": mesh.status()}
 
 
@@ -1295,6 +1416,7 @@ def run_serve(args, peak):
             "rel_err": err,
             "roofline": roofline_fp32(flops / span, peak, "served traffic (persistent forward and back-propagation "
                                                           "launches per tick)"),
+            "cpu_baseline": cpu_baseline_served(meshes_h, pools, mesh_ids, bsz, grad),
             "clocks": cs.summary(), "status": status}
 
 
