@@ -79,7 +79,8 @@ __device__ __forceinline__ void slot_T(const CoefArgs& a, int l, int q, bool act
     // T alone (and the splitter pair of the direct gradient) in float-float on the FP32 pipe; with derivative
     // tiles, or angles beyond the float-float range, the double-precision form
     const float al = ss ? ss[0] : 0.f, be = ss ? ss[1] : 0.f;
-    if (need_d || !(QUAD ? mzi_T_ff_quad(pp[0], pp[1], al, be, &T, csb) : mzi_T_ff(pp[0], pp[1], al, be, &T, csb)))
+    if (need_d ||
+        !(QUAD ? mzi_T_ff_quad(pp[0], pp[1], al, be, ss == nullptr, &T, csb) : mzi_T_ff(pp[0], pp[1], al, be, &T, csb)))
       mzi_T(pp[0], pp[1], al, be, &T, need_d ? &D0 : nullptr, need_d ? &D1 : nullptr, csb);
   } else {   // CR_SYM
     sym_T(pp[0], pp[1], ss ? ss[0] : 0.f, &T, need_d ? &D0 : nullptr, need_d ? &D1 : nullptr);

@@ -122,6 +122,23 @@ __device__ __forceinline__ void mzi_T_ff_from(ff S, ff C, ff Sph, ff Cph, ff sa,
   T->t11 = ffz_round(ffz_mul(E0, A11));
 }
 
+// The same for ideal splitters (alpha = beta = 0: cos = 1, sin = 0), without the splitter products.  Each entry is
+// the value mzi_T_ff_from computes for those angles, its operations reduced to the ones that are not exact
+// multiplications by 1 or additions of 0.
+__device__ __forceinline__ void mzi_T_ff_ideal(ff S, ff C, ff Sph, ff Cph, C2x2* T, float2* csb) {
+  if (csb) {
+    const float r = 0.707106769f;   // (1/sqrt 2)(cos 0 -+ sin 0), rounded
+    *csb = make_float2(r, r);
+  }
+  const ffz E1 = ffz_mul(ffz{C, S}, ffz{Cph, Sph});        // e^{i(th/2 + ph)}
+  const ff E1yS = ff_mul(E1.y, S), E1xS = ff_mul(E1.x, S), E1yC = ff_mul(E1.y, C), E1xC = ff_mul(E1.x, C);
+  const ff SC = ff_mul(S, C), CC = ff_mul(C, C), SS = ff_mul(S, S), CS = ff_mul(C, S);
+  T->t00 = make_float2(ff_round(ff_neg(E1yS)), ff_round(E1xS));   // e^{i(th/2+ph)} (i S)
+  T->t01 = make_float2(ff_round(ff_neg(SC)), ff_round(CC));       // e^{i th/2} (i C)
+  T->t10 = make_float2(ff_round(ff_neg(E1yC)), ff_round(E1xC));   // e^{i(th/2+ph)} (i C)
+  T->t11 = make_float2(ff_round(SS), ff_round(ff_neg(CS)));       // e^{i th/2} (-i S)
+}
+
 // mzi_T_ff_from on the angles of one thread; false (nothing written) when an angle is outside the float-float
 // range, and the caller takes the double path.
 __device__ __forceinline__ bool mzi_T_ff(float th, float ph, float al, float be, C2x2* T, float2* csb) {
@@ -137,7 +154,9 @@ __device__ __forceinline__ bool mzi_T_ff(float th, float ph, float al, float be,
 // it): lane k of the quad takes the sin/cos of angle k (th/2, ph, alpha, beta), the quad exchanges them by
 // shuffles, and every lane combines all four.  The four sin/cos chains, the longest part, then run side by side,
 // and the results are bitwise those of mzi_T_ff.  false on every lane of the quad when any angle is out of range.
-__device__ __forceinline__ bool mzi_T_ff_quad(float th, float ph, float al, float be, C2x2* T, float2* csb) {
+// ideal (uniform over the launch): no splitter array, alpha = beta = 0, and the lanes 2 and 3 of the quad idle.
+__device__ __forceinline__ bool mzi_T_ff_quad(float th, float ph, float al, float be, bool ideal, C2x2* T,
+                                              float2* csb) {
   const int lane = threadIdx.x & 31, base = lane & ~3, sub = lane & 3;
   const unsigned qmask = 0xFu << base;
   const float x = sub == 0 ? 0.5f * th : (sub == 1 ? ph : (sub == 2 ? al : be));
@@ -152,7 +171,8 @@ __device__ __forceinline__ bool mzi_T_ff_quad(float th, float ph, float al, floa
     v[k][0] = ff{__shfl_sync(qmask, s.h, base + k), __shfl_sync(qmask, s.l, base + k)};
     v[k][1] = ff{__shfl_sync(qmask, c.h, base + k), __shfl_sync(qmask, c.l, base + k)};
   }
-  mzi_T_ff_from(v[0][0], v[0][1], v[1][0], v[1][1], v[2][0], v[2][1], v[3][0], v[3][1], T, csb);
+  if (ideal) mzi_T_ff_ideal(v[0][0], v[0][1], v[1][0], v[1][1], T, csb);
+  else mzi_T_ff_from(v[0][0], v[0][1], v[1][0], v[1][1], v[2][0], v[2][1], v[3][0], v[3][1], T, csb);
   return true;
 }
 

@@ -11,7 +11,7 @@ from oracle import meshes_oracle as O
 pytestmark = pytest.mark.gpu
 
 
-def _build(om, op, B):
+def _build(om, op, B, no_splitters=False):
     from meshes_gb300 import _lib
     from meshes_gb300.batched import plan
     lib = _lib.load()
@@ -23,9 +23,10 @@ def _build(om, op, B):
     shifts = torch.tensor(om.shifts, dtype=torch.int32, device="cuda")
     p = torch.tensor(np.asarray(om.p, np.float32).reshape(-1), device="cuda")
     s = torch.tensor(np.asarray(om.s, np.float32).reshape(-1), device="cuda")
+    assert no_splitters or s.numel() == L * (N // 2) * 2          # the kernel reads a full (L, N/2, 2) grid
     _lib.check(lib.mg_build_tiles(op, N, L, 0, lens.data_ptr(), shifts.data_ptr(), None, 0, p.data_ptr(), N,
-                                  s.data_ptr(), N, None, None, None, B, None, ws.data_ptr(), info.total, st),
-               "mg_build_tiles")
+                                  None if no_splitters else s.data_ptr(), N, None, None, None, B, None,
+                                  ws.data_ptr(), info.total, st), "mg_build_tiles")
     assert lib.mg_read_status(ws.data_ptr(), 0, st) == 0
     raw = ws.cpu().numpy()
     tiles = raw[info.off_tiles: info.off_tiles + L * info.layer_bytes].view(np.float32).reshape(L, -1)
@@ -86,3 +87,23 @@ def test_tiles_are_correctly_rounded(op):
         beta = om.s[..., 1].astype(np.float64)
         cs_ref = np.stack([np.cos(np.pi / 4 + beta), np.sin(np.pi / 4 + beta)], -1).astype(np.float32)
         assert (cs[mask] != cs_ref[mask]).mean() < 1e-4
+
+
+@pytest.mark.parametrize("op", [0, 2])
+def test_ideal_splitter_tiles(op):
+    """Without a splitter array the coefficient pass takes its ideal-splitter form (no splitter products); its
+    tiles equal those built from an explicit all-zero splitter array (the general form) entry for entry, and
+    are correctly rounded."""
+    rng = np.random.default_rng(23 + op)
+    om = O.random_mesh(rng, 128, "clements", "mzi", 0.0)
+    p = om.p.astype(np.float64)
+    big = rng.random(p.shape) < 0.2
+    p[big] = rng.uniform(-300, 300, big.sum())
+    om.p = (p * om.active_mask()[..., None]).astype(np.float32)
+    om.s = np.zeros((om.L, om.N // 2, 2), dtype=np.float32)          # an explicit all-zero splitter grid
+    info, t_ideal = _build(om, op, 1024, no_splitters=True)
+    _, t_zero = _build(om, op, 1024)
+    assert np.array_equal(t_ideal, t_zero)          # +0 and -0 compare equal
+    T, _ = _decode(info, t_ideal, 128)
+    mask = om.active_mask()
+    assert (T[mask] != _nearest(om.T_grid())[mask]).mean() < 1e-4
