@@ -805,6 +805,22 @@ __device__ __forceinline__ void run_chunk(const PropArgs& pa, int vb0, const int
         k0 &= ~KIND_PERM;
       }
     }
+    if constexpr (NN && OP == OP_FWD && !PERM) {
+      // four nearest-neighbour layers (aligned, odd, aligned, odd) as one straight-line block: more independent
+      // crossings for the scheduler than a fused pair.  Measured on GB300 with bitwise the same results: forward
+      // N=256 B=4096 2% faster, N=64 B=1024 13% faster; eight layers were slower at N=256 (0.106 against 0.101 ms)
+      if (i + 3 < nl && k0 == 0 && kinds[l0 + 1] == KIND_MIS && kinds[l0 + 2] == 0 && kinds[l0 + 3] == KIND_MIS) {
+        const float4* t1 = reinterpret_cast<const float4*>(st + (size_t)(l0 + 1 - lo) * layer_bytes);
+        const float4* t2 = reinterpret_cast<const float4*>(st + (size_t)(l0 + 2 - lo) * layer_bytes);
+        const float4* t3 = reinterpret_cast<const float4*>(st + (size_t)(l0 + 3 - lo) * layer_bytes);
+        layer_local<OP, M, V, REAL, GR, 1, PK>(t0, G, j, r, u, w, g0);
+        layer_mis<OP, M, V, REAL, GR, PK>(t1, G, j, r, u, w, g0);
+        layer_local<OP, M, V, REAL, GR, 1, PK>(t2, G, j, r, u, w, g0);
+        layer_mis<OP, M, V, REAL, GR, PK>(t3, G, j, r, u, w, g0);
+        i += 4;
+        continue;
+      }
+    }
     if (i + 1 < nl && (k0 == 0 || k0 == KIND_MIS)) {
       const int l1 = (OP == OP_BWD) ? (l0 - 1) : (l0 + 1);
       const int k1 = kinds[l1];
