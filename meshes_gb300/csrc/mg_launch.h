@@ -80,6 +80,9 @@ bool nn_instantiated(int op, bool real, int M, int V, int gr, bool full, bool sp
 // batch spreads over more schedulers; mg_prop_nn_small.cu)
 bool nn_small_instantiated(int op, bool real, int M, int V, int gr, bool full);
 cudaError_t launch_prop_nn_small(int M, int V, const LaunchCfg& lc, const PropArgs& a);
+// and the forward-mode derivative's full-warp tiles (mg_prop_nn_fwddiff.cu)
+bool nn_fwddiff_instantiated(int op, bool real, int M, int V, int gr, bool full);
+cudaError_t launch_prop_nn_fwddiff(bool real, int M, int V, const LaunchCfg& lc, const PropArgs& a);
 cudaError_t launch_prop_nn(int op, bool real, int M, int V, int gr, bool full, bool split, const LaunchCfg& lc,
                            const PropArgs& a);
 // wide nearest-neighbour meshes (512 < N <= 640): kWideM modes in each of 32 lanes (mg_prop_wide.cu)

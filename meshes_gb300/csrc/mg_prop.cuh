@@ -805,10 +805,11 @@ __device__ __forceinline__ void run_chunk(const PropArgs& pa, int vb0, const int
         k0 &= ~KIND_PERM;
       }
     }
-    if constexpr (NN && OP == OP_FWD && !PERM) {
+    if constexpr (NN && (OP == OP_FWD || OP == OP_FWDDIFF) && !PERM) {
       // four nearest-neighbour layers (aligned, odd, aligned, odd) as one straight-line block: more independent
       // crossings for the scheduler than a fused pair.  Measured on GB300 with bitwise the same results: forward
-      // N=256 B=4096 2% faster, N=64 B=1024 13% faster; eight layers were slower at N=256 (0.106 against 0.101 ms)
+      // N=256 B=4096 2% faster, N=64 B=1024 13% faster, forward-mode derivative N=256 1.5% faster; eight layers
+      // were slower at N=256 (0.106 against 0.101 ms), and back-propagation spilled with four
       if (i + 3 < nl && k0 == 0 && kinds[l0 + 1] == KIND_MIS && kinds[l0 + 2] == 0 && kinds[l0 + 3] == KIND_MIS) {
         const float4* t1 = reinterpret_cast<const float4*>(st + (size_t)(l0 + 1 - lo) * layer_bytes);
         const float4* t2 = reinterpret_cast<const float4*>(st + (size_t)(l0 + 2 - lo) * layer_bytes);

@@ -17,7 +17,8 @@ constexpr int kNN[][6] = {{OP_FWD, 0, 8, 4, 0, 1}, {OP_FWD, 0, 16, 2, 0, 1}, {OP
 
 bool nn_instantiated(int op, bool real, int M, int V, int gr, bool full, bool split) {
   if (split && (op != OP_FWD || !full)) return false;
-  if (!split && nn_small_instantiated(op, real, M, V, gr, full)) return true;
+  if (!split && (nn_small_instantiated(op, real, M, V, gr, full) || nn_fwddiff_instantiated(op, real, M, V, gr, full)))
+    return true;
   for (const auto& k : kNN)
     if (k[0] == op && k[1] == (real ? 1 : 0) && k[2] == M && k[3] == V && k[4] == gr && k[5] == (full ? 1 : 0))
       return true;
@@ -28,6 +29,7 @@ cudaError_t launch_prop_nn(int op, bool real, int M, int V, int gr, bool full, b
                            const PropArgs& a) {
   if (!nn_instantiated(op, real, M, V, gr, full, split)) return cudaErrorInvalidConfiguration;
   if (!split && nn_small_instantiated(op, real, M, V, gr, full)) return launch_prop_nn_small(M, V, lc, a);
+  if (!split && nn_fwddiff_instantiated(op, real, M, V, gr, full)) return launch_prop_nn_fwddiff(real, M, V, lc, a);
   const int key = op * 10000 + (real ? 1000 : 0) + M * 10 + V;
   if (!full) {
     switch (key) {
