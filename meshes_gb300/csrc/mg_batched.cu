@@ -99,7 +99,12 @@ batched_kernel(const mg_batch_mesh* __restrict__ meshes, int n_meshes, const mg_
   }
 }
 
-// one CTA per mesh: dp[l][q][k] = sum over the mesh's items (in order) of the partials
+// dp[l][q][k] = sum over the mesh's items (in item order) of the partials.  Grid (meshes, kReduceY): the
+// kReduceY CTAs of a mesh stride over its slot positions, one position per thread at a time, consecutive
+// threads on consecutive positions (coalesced); each thread keeps 8 item loads in flight and adds them in item
+// order, so the sums are those of a plain sequential loop.  (One CTA per mesh, one load in flight per thread,
+// took 3.85 ms on the 512-mesh benchmark - 23% of its forward + backward step.)
+constexpr int kReduceY = 64;
 __global__ void batched_reduce_kernel(const mg_batch_mesh* __restrict__ meshes) {
   const mg_batch_mesh md = meshes[blockIdx.x];
   if (!md.dp || !md.partial || md.n_items <= 0) return;
@@ -107,7 +112,8 @@ __global__ void batched_reduce_kernel(const mg_batch_mesh* __restrict__ meshes) 
   const int* geo = md.kinds + L;
   const float2* part = static_cast<const float2*>(md.partial);
   const size_t stride = (size_t)L * np2;
-  for (int idx = threadIdx.x; idx < L * np2; idx += blockDim.x) {
+  const int n = md.n_items;
+  for (int idx = blockIdx.y * blockDim.x + threadIdx.x; idx < L * np2; idx += gridDim.y * blockDim.x) {
     const int l = idx / np2, pos = idx - l * np2;
     const int q = pos_slot(pos, M, G);
     if (q >= N / 2) continue;
@@ -115,7 +121,18 @@ __global__ void batched_reduce_kernel(const mg_batch_mesh* __restrict__ meshes) 
     float sx = 0.f, sy = 0.f;
     if (q >= sh / 2 && q < sh / 2 + ln) {
       const float2* p = part + (size_t)l * np2 + pos;
-      for (int k = 0; k < md.n_items; ++k) {
+      int k = 0;
+      for (; k + 8 <= n; k += 8) {
+        float2 v[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v[i] = p[(size_t)(k + i) * stride];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          sx += v[i].x;
+          sy += v[i].y;
+        }
+      }
+      for (; k < n; ++k) {
         const float2 v = p[(size_t)k * stride];
         sx += v.x;
         sy += v.y;
@@ -193,7 +210,7 @@ extern "C" int mg_batched_propagate(int op, const mg_batch_mesh* meshes, int n_m
 extern "C" int mg_batched_reduce(const mg_batch_mesh* meshes, int n_meshes, void* stream) {
   if (!meshes || n_meshes < 0) return set_last_error(MG_E_ARG, "batched reduce: bad arguments");
   if (n_meshes == 0) return MG_OK;
-  batched_reduce_kernel<<<n_meshes, 256, 0, static_cast<cudaStream_t>(stream)>>>(meshes);
+  batched_reduce_kernel<<<dim3(n_meshes, kReduceY), 256, 0, static_cast<cudaStream_t>(stream)>>>(meshes);
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MG_OK : set_last_error(MG_E_CUDA, "batched_reduce_kernel: %s", cudaGetErrorString(e));
 }
