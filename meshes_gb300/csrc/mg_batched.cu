@@ -89,7 +89,15 @@ batched_kernel(const mg_batch_mesh* __restrict__ meshes, int n_meshes, const mg_
         // one-vector crossings here: with three class bodies in one kernel the packed forms made
         // back-propagation spill and gained nothing going forward (measured on GB300: the batched engine
         // 13% and 3.5% slower)
-        case MG_BCLS_C8: prop_body<OP, 8, 4, false, 0, (OP == OP_BWD ? 1 : 0), false, NN, false>(a, smem); break;
+        case MG_BCLS_C8:
+          // nearest-neighbour forward launches: compile-time lane groups for G = 32, 16, 8 (no run-time lane
+          // index arithmetic; 2% faster on the 512-mesh benchmark).  Back-propagation keeps the run-time body:
+          // a second one made the 254-register kernel spill.
+          if (NN && OP == OP_FWD && md.G == 32) prop_body<OP, 8, 4, false, 32, 0, false, NN, false>(a, smem);
+          else if (NN && OP == OP_FWD && md.G == 16) prop_body<OP, 8, 4, false, 16, 0, false, NN, false>(a, smem);
+          else if (NN && OP == OP_FWD && md.G == 8) prop_body<OP, 8, 4, false, 8, 0, false, NN, false>(a, smem);
+          else prop_body<OP, 8, 4, false, 0, (OP == OP_BWD ? 1 : 0), false, NN, false>(a, smem);
+          break;
         case MG_BCLS_C16: prop_body<OP, 16, 2, false, 0, (OP == OP_BWD ? 1 : 0), false, NN, false>(a, smem); break;
         case MG_BCLS_R8: prop_body<OP, 8, 4, true, 0, (OP == OP_BWD ? 2 : 0), false, NN>(a, smem); break;
         default:
