@@ -146,11 +146,11 @@ int mg_backdiff_ft(int N, int L, int B, const int* strides, const float* p, floa
                    int accumulate, void* workspace, size_t workspace_bytes, void* stream);
 
 /* Forward propagation like mg_fwdprop (nearest-neighbour geometry), for callers that cannot allocate
- * device memory - code that runs inside a stream capture, plugin hosts that forbid allocations, loops
- * that must not touch an allocator - and so cannot provide a workspace.  No counterpart in the
+ * device memory - plugin hosts that forbid allocations, loops that must not touch an allocator - and so
+ * cannot provide a workspace.  No counterpart in the
  * reference.  The scratch is an 8 MiB array compiled into the library (held on every GPU that loads
  * it until exit); problems needing more return MG_E_WORKSPACE without launching.  The first call on
- * each device looks up the array's device address and should come before any stream capture.  All
+ * each device looks up the array's device address.  All
  * calls share the array, so calls that overlap on the GPU race: serialise them.  Kernel status codes
  * are not reported by this entry point.  The array's address is cached per device for the life of the
  * process: do not call it again after cudaDeviceReset re-creates the device's context. */

@@ -1,16 +1,14 @@
 // mg_fwdprop_noalloc: forward propagation for callers that cannot allocate device memory.
 //
-// Some callers cannot call cudaMalloc or an allocator: code running while a CUDA graph is being
-// captured in relaxed/global mode, plugin hosts that own the device heap and forbid side allocations,
-// or real-time loops that must not hit the allocator's locks and possible synchronisations.
+// Some callers cannot call cudaMalloc or an allocator: plugin hosts that own the device heap and forbid side
+// allocations, or real-time loops that must not hit the allocator's locks and possible synchronisations.
 // mg_fwdprop needs a scratch workspace (coefficient tiles, layer kinds, a status word) that the caller
 // normally provides; this entry point instead uses one scratch array compiled into the library.
 //
 // The scratch is a file-scope __device__ array of kNoAllocScratchBytes (8 MiB).  Every GPU that loads
 // the library holds it until the process exits.  Its host-side name is only a stand-in for the symbol,
 // not a device address, so the device address is looked up with cudaGetSymbolAddress once per device,
-// with that device current, on the first call made on that device.  That first call should therefore
-// come before any stream capture.
+// with that device current, on the first call made on that device.
 //
 // Every call shares the one array: calls that overlap on the GPU (different streams, or host threads
 // issuing to the same device without ordering) race on it and corrupt each other's coefficients.

@@ -1,7 +1,7 @@
 """The allocation-free forward entry point (mg_fwdprop_noalloc) against the workspace one (mg_fwdprop).
 
-Callers that cannot allocate device memory (inside a stream capture, in plugin hosts that own the
-device heap, in loops that must not touch an allocator) use mg_fwdprop_noalloc, which keeps its
+Callers that cannot allocate device memory (plugin hosts that own the device heap, loops that must not
+touch an allocator) use mg_fwdprop_noalloc, which keeps its
 scratch in a fixed array compiled into the library.  This file is collected last so that a failure
 here leaves every other test already run; it also passes alone in a fresh process.
 """
