@@ -122,19 +122,19 @@ class BatchedMeshes:
     """A fixed composition of meshes and batch sizes, propagated by one persistent launch per op."""
 
     def __init__(self, meshes: Sequence[MeshNetworkGPU], batch_sizes: Sequence[int], grid: Optional[int] = None,
-                 full_warp: bool = False):
+                 full_warp: bool = True):
         if len(meshes) != len(batch_sizes):
             raise ValueError("one batch size per mesh")
         self.device = meshes[0].device
         self.states: List[_MeshState] = [_MeshState(m, b) for m, b in zip(meshes, batch_sizes)]
         sms = torch.cuda.get_device_properties(self.device).multi_processor_count
         self.grid = grid or sms
-        # launch groups: by default every item runs in one launch of the three-class kernel.  With full_warp and
-        # every mesh nearest-neighbour (MG_BATCH_NN), complex M = 8 meshes whose vector fills the warp (G = 32)
-        # run in a launch of their own on the one-mesh kernel's body (packed crossings, compile-time lane
-        # group), concurrently with the rest on a side stream.  On 512 uneven meshes (N 8..256) that measured
-        # slower than the single launch (fwd+bwd 219 against 230 G MZI-apps/s on GB300): the two persistent
-        # grids compete for the same SMs.  Each group is sorted longest-first and drained from its own counter.
+        # launch groups: with full_warp (the default) and every mesh nearest-neighbour (MG_BATCH_NN), complex M = 8
+        # meshes whose vector fills the warp (G = 32) run in a launch of their own with a compile-time lane
+        # group, issued first; everything else runs in one launch of the three-class kernel on a side stream,
+        # whose CTAs take the SMs as the first launch's CTAs finish.  Measured on GB300 on 512 uneven meshes
+        # (N 8..256): fwd+bwd 318 against 301 G MZI-apps/s for a single launch, dJ/dp bitwise the same.  Each
+        # group is sorted longest-first and drained from its own counter.
         self.nn = BATCH_NN if all(st.mesh.geometry == GEO_NN for st in self.states) else 0
         groups = {}
         for i, st in enumerate(self.states):

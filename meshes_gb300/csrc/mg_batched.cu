@@ -23,9 +23,10 @@ __device__ __forceinline__ int cls_M(int cls) { return cls == MG_BCLS_C16 ? 16 :
 // the strided and butterfly layers run (fewer registers; a mesh with another kind is refused per item).
 // CLS >= 0: every item's mesh is of kernel class CLS (others are refused per item) and only that class's body
 // is compiled.  GT = 32 (class MG_BCLS_C8 with MG_BATCH_FULL_WARP): every item's mesh has a vector filling
-// the warp (G = 32, N in (128, 256]) and the body is the one-mesh kernel's, compile-time lane group and
-// packed f32x2 crossings, without spills; with a run-time lane group the packed forms spill and the
-// bodies keep the one-vector crossings (measured on GB300 in the three-class kernel: 13% slower packed).
+// the warp (G = 32, N in (128, 256]) and the body has a compile-time lane group.  All batched bodies keep the
+// one-vector crossings: the packed forms spilled in the three-class kernel (13% slower) and, in the G = 32
+// launch, raised the ALU pipe from 11% to 42% of cycles (measured on GB300: the 512-mesh fwd+bwd 285 against
+// 318 G MZI-apps/s with the one-vector body).
 template <int OP, bool NN, int CLS = -1, int GT = 0>
 __global__ void __launch_bounds__(kBatchWarps * 32, 1)
 batched_kernel(const mg_batch_mesh* __restrict__ meshes, int n_meshes, const mg_batch_item* __restrict__ items,
@@ -79,7 +80,7 @@ batched_kernel(const mg_batch_mesh* __restrict__ meshes, int n_meshes, const mg_
       }
     }
     if constexpr (CLS == MG_BCLS_C8) {
-      prop_body<OP, 8, 4, false, GT, (OP == OP_BWD ? 1 : 0), false, NN, GT == 32>(a, smem);
+      prop_body<OP, 8, 4, false, GT, (OP == OP_BWD ? 1 : 0), false, NN, false>(a, smem);
     } else if constexpr (CLS == MG_BCLS_C16) {
       prop_body<OP, 16, 2, false, 0, (OP == OP_BWD ? 1 : 0), false, NN, false>(a, smem);
     } else if constexpr (CLS == MG_BCLS_R8) {

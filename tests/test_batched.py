@@ -154,9 +154,9 @@ def test_nearest_neighbour_launch():
 
 
 def test_full_warp_class_launch():
-    """With full_warp, meshes whose vectors fill the warp (complex M = 8, N in (128, 256]) run in their own launch
-    on the one-mesh kernel's body; a launch of that class refuses an item of another mesh (MG_ST_BAD_WORK) and
-    leaves it."""
+    """By default (full_warp) meshes whose vectors fill the warp (complex M = 8, N in (128, 256]) run in their own
+    launch with a compile-time lane group (full_warp=False: one launch); a launch of that class refuses an item
+    of another mesh (MG_ST_BAD_WORK) and leaves it."""
     from meshes_gb300 import _lib
     from meshes_gb300.batched import MG_BATCH_FULL_WARP, MG_BATCH_ONLY, BCLS_C8, BatchedMeshes, _bind
     rng = np.random.default_rng(57)
@@ -165,8 +165,8 @@ def test_full_warp_class_launch():
     Bs = [70, 45, 33]
     xs = [O.unit_columns(rng, om.N, B) for om, B in zip(oms, Bs)]
     gs = [O.unit_columns(rng, om.N, B) for om, B in zip(oms, Bs)]
-    assert len(BatchedMeshes([gpu_mesh(om) for om in oms], Bs).groups) == 1
-    bm = BatchedMeshes([gpu_mesh(om) for om in oms], Bs, full_warp=True)
+    assert len(BatchedMeshes([gpu_mesh(om) for om in oms], Bs, full_warp=False).groups) == 1
+    bm = BatchedMeshes([gpu_mesh(om) for om in oms], Bs)
     assert [g[0] for g in bm.groups] == [MG_BATCH_ONLY(BCLS_C8) | MG_BATCH_FULL_WARP, 0]
     for st, x, g in zip(bm.states, xs, gs):
         st.x.copy_(torch.tensor(x, dtype=st.x.dtype))
@@ -178,6 +178,19 @@ def test_full_warp_class_launch():
         G, _, gin = O.vjp_unitary(om, y_ref, g)
         assert O.rel_err(st.y.cpu().numpy(), y_ref) < TOL
         assert O.rel_err(st.gx.cpu().numpy(), gin) < TOL
+        assert O.rel_err(st.dp.cpu().numpy(), O.contract_dp(om, G)) < TOL
+    # both launch groups recorded in one CUDA graph (the side stream forked and joined inside the capture),
+    # replayed with new inputs: the same results as eager steps
+    bm.capture(backward=True)
+    xs2 = [O.unit_columns(rng, om.N, B) for om, B in zip(oms, Bs)]
+    for st, x in zip(bm.states, xs2):
+        st.x.copy_(torch.tensor(x, dtype=torch.complex64))
+    bm.replay()
+    assert bm.check_status() == 0
+    for om, st, x, g in zip(oms, bm.states, xs2, gs):
+        y_ref = O.propagate(om, x)
+        G, _, gin = O.vjp_unitary(om, y_ref, g)
+        assert O.rel_err(st.y.cpu().numpy(), y_ref) < TOL
         assert O.rel_err(st.dp.cpu().numpy(), O.contract_dp(om, G)) < TOL
     # the N = 64 mesh's items through the full-warp launch: refused, output untouched
     lib = _bind()
