@@ -224,8 +224,8 @@ int mg_plan(int op, int N, int L, int B, int crossing, int geometry, const mg_co
 /* OR-ed into mg_batched_propagate's op: every item's mesh is of kernel class cls, and the launch runs only that
  * class's body, with its own register budget; an item of another class records MG_ST_BAD_WORK and is skipped. */
 #define MG_BATCH_ONLY(cls) (((cls) + 1) << 8)
-/* OR-ed with MG_BATCH_ONLY(MG_BCLS_C8): every item's mesh has G = 32 lanes per vector (N in (128, 256]); the
- * launch runs the one-mesh kernel's body for that lane group (packed f32x2 crossings, no spills). */
+/* OR-ed with MG_BATCH_ONLY(MG_BCLS_C8) or MG_BATCH_ONLY(MG_BCLS_R8): every item's mesh has G = 32 lanes per
+ * vector (N in (128, 256]); the launch runs a body compiled for that lane group. */
 #define MG_BATCH_FULL_WARP 32
 #define MG_BCLS_C8 0
 #define MG_BCLS_C16 1

@@ -129,22 +129,24 @@ class BatchedMeshes:
         self.states: List[_MeshState] = [_MeshState(m, b) for m, b in zip(meshes, batch_sizes)]
         sms = torch.cuda.get_device_properties(self.device).multi_processor_count
         self.grid = grid or sms
-        # launch groups: with full_warp (the default) and every mesh nearest-neighbour (MG_BATCH_NN), complex M = 8
-        # meshes whose vector fills the warp (G = 32) run in a launch of their own with a compile-time lane
-        # group, issued first; everything else runs in one launch of the three-class kernel on a side stream,
-        # whose CTAs take the SMs as the first launch's CTAs finish.  Measured on GB300 on 512 uneven meshes
+        # launch groups: with full_warp (the default) and every mesh nearest-neighbour (MG_BATCH_NN), the M = 8
+        # meshes whose vector fills the warp (G = 32; complex, and real ones in a second group) run in launches
+        # of their own with a compile-time lane group, issued first; everything else runs in one launch of the
+        # three-class kernel on a side stream, whose CTAs take the SMs as the earlier launches' CTAs finish.  Measured on GB300 on 512 uneven meshes
         # (N 8..256): fwd+bwd 318 against 301 G MZI-apps/s for a single launch, dJ/dp bitwise the same.  Each
         # group is sorted longest-first and drained from its own counter.
         self.nn = BATCH_NN if all(st.mesh.geometry == GEO_NN for st in self.states) else 0
         groups = {}
         for i, st in enumerate(self.states):
-            full = full_warp and bool(self.nn) and st.cls == BCLS_C8 and st.G == 32
-            flags = (MG_BATCH_ONLY(BCLS_C8) | MG_BATCH_FULL_WARP) if full else 0
+            full = full_warp and bool(self.nn) and st.cls in (BCLS_C8, BCLS_R8) and st.G == 32
+            flags = (MG_BATCH_ONLY(st.cls) | MG_BATCH_FULL_WARP) if full else 0
             for k in range(st.n_items):
                 v0 = k * st.cap
                 groups.setdefault(flags, []).append((st.cost(), i, v0, min(v0 + st.cap, st.B), k))
         self.groups = []
-        for flags, items in sorted(groups.items(), reverse=True):
+        # the full-warp groups first, the largest total work first; the mixed launch (short items) last
+        order = sorted(groups.items(), key=lambda kv: (kv[0] == 0, -sum(t[0] for t in kv[1])))
+        for flags, items in order:
             items.sort(key=lambda t: -t[0])               # longest processing time first
             arr = (mg_batch_item * max(len(items), 1))()
             for n, (_, i, v0, v1, k) in enumerate(items):

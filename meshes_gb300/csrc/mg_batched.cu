@@ -84,7 +84,7 @@ batched_kernel(const mg_batch_mesh* __restrict__ meshes, int n_meshes, const mg_
     } else if constexpr (CLS == MG_BCLS_C16) {
       prop_body<OP, 16, 2, false, 0, (OP == OP_BWD ? 1 : 0), false, NN, false>(a, smem);
     } else if constexpr (CLS == MG_BCLS_R8) {
-      prop_body<OP, 8, 4, true, 0, (OP == OP_BWD ? 2 : 0), false, NN>(a, smem);
+      prop_body<OP, 8, 4, true, GT, (OP == OP_BWD ? 2 : 0), false, NN>(a, smem);
     } else {
       switch (md.cls) {
         // one-vector crossings here: with three class bodies in one kernel the packed forms made
@@ -183,7 +183,9 @@ cudaError_t launch_batched_cls(int cls, bool full, bool nn, const mg_batch_mesh*
       return full ? launch_batched_nn<OP, MG_BCLS_C8, 32>(nn, meshes, n_meshes, items, n_items, head, grid, smem, status, st)
                   : launch_batched_nn<OP, MG_BCLS_C8>(nn, meshes, n_meshes, items, n_items, head, grid, smem, status, st);
     case MG_BCLS_C16: return launch_batched_nn<OP, MG_BCLS_C16>(nn, meshes, n_meshes, items, n_items, head, grid, smem, status, st);
-    case MG_BCLS_R8: return launch_batched_nn<OP, MG_BCLS_R8>(nn, meshes, n_meshes, items, n_items, head, grid, smem, status, st);
+    case MG_BCLS_R8:
+      return full ? launch_batched_nn<OP, MG_BCLS_R8, 32>(nn, meshes, n_meshes, items, n_items, head, grid, smem, status, st)
+                  : launch_batched_nn<OP, MG_BCLS_R8>(nn, meshes, n_meshes, items, n_items, head, grid, smem, status, st);
     default: return launch_batched_nn<OP, -1>(nn, meshes, n_meshes, items, n_items, head, grid, smem, status, st);
   }
 }
@@ -196,7 +198,8 @@ extern "C" int mg_batched_propagate(int op, const mg_batch_mesh* meshes, int n_m
   const int cls = ((op >> 8) & 0xff) - 1;   // MG_BATCH_ONLY(cls): one class per launch, -1 any
   op &= 0x0f;
   if (cls < -1 || cls > MG_BCLS_R8) return set_last_error(MG_E_ARG, "batched class %d not in {0,1,2}", cls);
-  if (full && cls != MG_BCLS_C8) return set_last_error(MG_E_ARG, "MG_BATCH_FULL_WARP needs MG_BATCH_ONLY(MG_BCLS_C8)");
+  if (full && cls != MG_BCLS_C8 && cls != MG_BCLS_R8)
+    return set_last_error(MG_E_ARG, "MG_BATCH_FULL_WARP needs MG_BATCH_ONLY(MG_BCLS_C8) or MG_BATCH_ONLY(MG_BCLS_R8)");
   if (op != MG_OP_FWD && op != MG_OP_BWD) return set_last_error(MG_E_ARG, "batched op must be fwd or bwd");
   if (!meshes || n_meshes < 0 || (!items && n_items > 0) || !head || grid < 1)
     return set_last_error(MG_E_ARG, "batched launch: bad arguments");
