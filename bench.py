@@ -1166,13 +1166,15 @@ def run_batched(args, peak):
 def run_unitary_fit(args, peak):
     """Unitary fitting: Clements mzi N=128 L=128 with splitting errors N(0, 0.02), target a Haar-random
     unitary (QR of a complex Gaussian with the R-diagonal phase fix), x = I, J = ||U - U_t||_F^2,
-    2000 Adam steps (lr 1e-2) on theta, phi through the autograd function; steps/s and the fidelity
+    2000 Adam steps (lr 1e-2) on theta, phi through the autograd function (mesh_l2_loss: the loss gradient
+    is formed inside the back-propagation kernel; torch's Adam in its single-tensor form, which measured
+    faster on this one-tensor problem than the multi-tensor and fused forms); steps/s and the fidelity
     |tr(U^H U_t)|^2 / N^2 of the fitted phases re-evaluated in complex128.  The headline runs the step as a
     CUDA graph (GraphedStep: captured once, replayed); the same 2000 steps run eagerly beside it, from the same
     start, with the same device-side Adam, and must end at the same phases."""
     import torch
     from meshes_gb300 import MeshNetworkGPU
-    from meshes_gb300.autograd import GraphedStep, mesh_apply
+    from meshes_gb300.autograd import GraphedStep, mesh_apply, mesh_l2_loss
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     rng = np.random.default_rng(1004)
@@ -1194,11 +1196,11 @@ def run_unitary_fit(args, peak):
 
     def trainer():
         p = torch.tensor(p0, device=dev, requires_grad=True)
-        opt = torch.optim.Adam([p], lr=1e-2, capturable=True)
+        opt = torch.optim.Adam([p], lr=1e-2, capturable=True, foreach=False)
 
         def step():
             opt.zero_grad(set_to_none=True)
-            loss = ((mesh_apply(m, x, p) - target).abs() ** 2).sum()
+            loss = mesh_l2_loss(m, x, target, p)
             loss.backward()
             opt.step()
             return loss

@@ -75,23 +75,12 @@ class MeshFunction(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, x: torch.Tensor, p: torch.Tensor, mesh: MeshNetworkGPU):
-        lib = load()
         x = x.resolve_conj().resolve_neg().contiguous()
         p = p.detach().to(torch.float32).contiguous()
-        B, N = x.shape
-        assert N == mesh.N, "x must be (B, N) with N=%d" % mesh.N
-        y = torch.empty_like(x)
-        shared = mesh.geometry == GEO_NN
-        if shared:      # back-propagation tiles serve the forward kernel and, later, the backward
-            ws, nb, ver = _build(mesh, OP_BWD, p, B)
-            op, cfg = OP_FWD_BWDTILES, mesh.config.get(OP_BWD)
-        else:
-            ws, nb, ver = _build(mesh, OP_FWD, p, B)
-            op, cfg = OP_FWD, mesh.config.get(OP_FWD)
-        check(lib.mg_propagate(op, N, mesh.L, B, mesh.crossing, mesh.geo_code, x.data_ptr(), None, y.data_ptr(),
-                               None, N, None, 0, 0, _lib.cfg_ptr(cfg), ws, nb, _stream(mesh.device)), "mg_propagate")
+        # nearest-neighbour meshes: the back-propagation tiles serve the forward kernel and, later, the backward
+        y, ver = _forward_y(mesh, x, p)
         ctx.mesh = mesh
-        ctx.tiles_version = ver if shared else None
+        ctx.tiles_version = ver
         ctx.save_for_backward(y, p)
         return y
 
@@ -113,6 +102,79 @@ class MeshFunction(torch.autograd.Function):
                                gx.data_ptr(), N, dp.data_ptr(), N // 2 * mesh.X_np, 0,
                                _lib.cfg_ptr(mesh.config.get(OP_BWD)), ws, nb, _stream(mesh.device)), "mg_propagate")
         return gx, dp.view_as(p), None
+
+
+def _forward_y(mesh: MeshNetworkGPU, x: torch.Tensor, p: torch.Tensor):
+    """y = U(p) x through the kernels; returns (y, tiles version or None) as MeshFunction.forward does."""
+    lib = load()
+    B, N = x.shape
+    assert N == mesh.N, "x must be (B, N) with N=%d" % mesh.N
+    y = torch.empty_like(x)
+    shared = mesh.geometry == GEO_NN
+    if shared:
+        ws, nb, ver = _build(mesh, OP_BWD, p, B)
+        op, cfg = OP_FWD_BWDTILES, mesh.config.get(OP_BWD)
+    else:
+        ws, nb, ver = _build(mesh, OP_FWD, p, B)
+        op, cfg = OP_FWD, mesh.config.get(OP_FWD)
+    check(lib.mg_propagate(op, N, mesh.L, B, mesh.crossing, mesh.geo_code, x.data_ptr(), None, y.data_ptr(),
+                           None, N, None, 0, 0, _lib.cfg_ptr(cfg), ws, nb, _stream(mesh.device)), "mg_propagate")
+    return y, (ver if shared else None)
+
+
+class MeshL2Function(torch.autograd.Function):
+    """J = sum_b ||U(p) x_b - t_b||^2 for a lossless mesh.  The backward pass forms dJ/dy* = 2 (y - t)
+    inside the back-propagation kernel (mg_propagate_l2) instead of in separate elementwise passes, the
+    fused form of the reference's L2 gradient (gpu/mesh.py:176-181, 219-221)."""
+
+    @staticmethod
+    def forward(ctx, x: torch.Tensor, p: torch.Tensor, t: torch.Tensor, mesh: MeshNetworkGPU):
+        x = x.resolve_conj().resolve_neg().contiguous()
+        t = t.resolve_conj().resolve_neg().to(x.dtype).contiguous()
+        p = p.detach().to(torch.float32).contiguous()
+        assert t.shape == x.shape, "target must have the shape of x"
+        y, ver = _forward_y(mesh, x, p)
+        d = y - t
+        J = (torch.view_as_real(d) if d.is_complex() else d).square().sum()
+        ctx.mesh, ctx.tiles_version = mesh, ver
+        ctx.save_for_backward(y, p, t)
+        return J
+
+    @staticmethod
+    def backward(ctx, gJ: torch.Tensor):
+        lib = load()
+        y, p, t = ctx.saved_tensors
+        mesh = ctx.mesh
+        B, N = y.shape
+        plan_ = _plans(mesh)[OP_BWD]
+        if ctx.tiles_version is not None and getattr(plan_, "version", None) == ctx.tiles_version:
+            ws, nb = plan_.workspace(B)
+        else:
+            ws, nb, _ = _build(mesh, OP_BWD, p, B)
+        gx = torch.empty_like(y)
+        dp = torch.empty(p.numel(), dtype=torch.float32, device=y.device)
+        check(lib.mg_propagate_l2(N, mesh.L, B, mesh.crossing, mesh.geo_code, y.data_ptr(), t.data_ptr(), None,
+                                  gx.data_ptr(), N, dp.data_ptr(), N // 2 * mesh.X_np, 0,
+                                  _lib.cfg_ptr(mesh.config.get(OP_BWD)), ws, nb, _stream(mesh.device)),
+              "mg_propagate_l2")
+        dp = dp.view_as(p).mul_(gJ)
+        gx = gx.mul_(gJ) if ctx.needs_input_grad[0] else None
+        gt = (y - t).mul_(-2 * gJ) if ctx.needs_input_grad[2] else None
+        return gx, dp, gt, None
+
+
+def mesh_l2_loss(mesh: MeshNetworkGPU, x: torch.Tensor, target: torch.Tensor,
+                 p: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """Differentiable J = sum |U(p) x - target|^2 over the batch; x and target (B, N), p (L, N/2, n_p)
+    (defaults to the mesh's own phases).  The same J as ``((mesh_apply(mesh, x, p) - target).abs() ** 2).sum()``
+    with the loss gradient formed inside the back-propagation kernel; meshes without a phase screen."""
+    if p is None:
+        p = mesh.p_crossing
+    if mesh.is_phase:
+        raise ValueError("mesh_l2_loss takes meshes without a phase screen; use mesh_apply for those")
+    if x.dtype != mesh.dtype:
+        x = x.to(mesh.dtype)
+    return MeshL2Function.apply(x, p, target, mesh)
 
 
 def mesh_apply(mesh: MeshNetworkGPU, x: torch.Tensor, p: Optional[torch.Tensor] = None,

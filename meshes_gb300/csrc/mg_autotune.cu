@@ -40,7 +40,7 @@ extern "C" int mg_autotune(int op, int N, int L, int B, int crossing, int geomet
     if (N > 512 || M > Np || Np / M > 32) continue;
     for (int V : vs[op]) {
       if (!V) continue;
-      for (int W : {2, 4, 8}) cands.push_back(mg_config{M, V, W, 0, 0, 2});
+      for (int W : {1, 2, 4, 8}) cands.push_back(mg_config{M, V, W, 0, 0, 2});
     }
   }
   if (N > 512)   // wide meshes: 20 modes per lane

@@ -76,10 +76,10 @@ cudaError_t launch_prop_perm(int op, bool real, int M, int V, int gr, const Laun
 // nearest-neighbour instantiations (layer kinds 0 and odd-shift only) of the configurations in
 // nn_instantiated(), uniform or split (mg_prop_nn.cu)
 bool nn_instantiated(int op, bool real, int M, int V, int gr, bool full, bool split);
-// the small-mesh forward tiles among them (complex, full warp, few modes and vectors per lane, so that a small
-// batch spreads over more schedulers; mg_prop_nn_small.cu)
+// the small-mesh tiles among them (complex, full warp, few modes and vectors per lane, so that a small batch
+// spreads over more schedulers; forward, and back-propagation at 4 x 2; mg_prop_nn_small.cu)
 bool nn_small_instantiated(int op, bool real, int M, int V, int gr, bool full);
-cudaError_t launch_prop_nn_small(int M, int V, const LaunchCfg& lc, const PropArgs& a);
+cudaError_t launch_prop_nn_small(int op, int M, int V, const LaunchCfg& lc, const PropArgs& a);
 // and the forward-mode derivative's full-warp tiles (mg_prop_nn_fwddiff.cu)
 bool nn_fwddiff_instantiated(int op, bool real, int M, int V, int gr, bool full);
 cudaError_t launch_prop_nn_fwddiff(bool real, int M, int V, const LaunchCfg& lc, const PropArgs& a);

@@ -28,7 +28,7 @@ bool nn_instantiated(int op, bool real, int M, int V, int gr, bool full, bool sp
 cudaError_t launch_prop_nn(int op, bool real, int M, int V, int gr, bool full, bool split, const LaunchCfg& lc,
                            const PropArgs& a) {
   if (!nn_instantiated(op, real, M, V, gr, full, split)) return cudaErrorInvalidConfiguration;
-  if (!split && nn_small_instantiated(op, real, M, V, gr, full)) return launch_prop_nn_small(M, V, lc, a);
+  if (!split && nn_small_instantiated(op, real, M, V, gr, full)) return launch_prop_nn_small(op, M, V, lc, a);
   if (!split && nn_fwddiff_instantiated(op, real, M, V, gr, full)) return launch_prop_nn_fwddiff(real, M, V, lc, a);
   const int key = op * 10000 + (real ? 1000 : 0) + M * 10 + V;
   if (!full) {

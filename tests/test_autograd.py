@@ -47,6 +47,55 @@ def test_autograd_matches_oracle(geo, cr, N, B):
     assert O.rel_err(xd.grad.cpu().numpy(), gin) < 1e-5
 
 
+@pytest.mark.parametrize("geo,cr,N,B", [("clements", "mzi", 64, 37), ("reck", "mzi", 32, 9), ("fft", "mzi", 128, 20),
+                                        ("clements", "orth", 64, 33)])
+def test_l2_loss_matches_oracle(geo, cr, N, B):
+    """mesh_l2_loss: J = sum |U x - t|^2 with the loss gradient formed inside the back-propagation kernel;
+    J, dJ/dp, dJ/dx and dJ/dt against the complex128 adjoint, scaled by a grad_output of 0.5."""
+    from meshes_gb300.autograd import mesh_l2_loss
+    rng = np.random.default_rng(7 * N + B)
+    om = O.random_mesh(rng, N, geo, cr, 0.02)
+    real = cr == "orth"
+    x = O.unit_columns(rng, N, B, real=real)
+    t = O.unit_columns(rng, N, B, real=real)
+    m = gpu_mesh(om)
+    dt = torch.float32 if real else torch.complex64
+    xd = torch.tensor(x, dtype=dt, device="cuda", requires_grad=True)
+    td = torch.tensor(t, dtype=dt, device="cuda", requires_grad=True)
+    pd = torch.tensor(om.p, dtype=torch.float32, device="cuda", requires_grad=True)
+    J = mesh_l2_loss(m, xd, td, pd)
+    (0.5 * J).backward()
+    y_ref = O.propagate(om, x)
+    J_ref = float(np.sum(np.abs(y_ref - t) ** 2))
+    G, _, gin = O.vjp_unitary(om, y_ref, 2 * (y_ref - t))
+    assert abs(float(J) - J_ref) < 1e-5 * J_ref
+    assert O.rel_err(pd.grad.cpu().numpy(), 0.5 * O.contract_dp(om, G)) < 1e-5
+    assert O.rel_err(xd.grad.cpu().numpy(), 0.5 * gin) < 1e-5
+    assert O.rel_err(td.grad.cpu().numpy(), -(y_ref - t)) < 1e-5
+    assert m.status() == 0
+
+
+def test_l2_loss_equals_mesh_apply_form():
+    """mesh_l2_loss gives bitwise the loss and gradients of sum(view_as_real(y - t)^2) through mesh_apply: the
+    kernel's 2 (y - t) is torch's gradient of that sum, and both reach the same back-propagation kernel."""
+    from meshes_gb300.autograd import mesh_apply, mesh_l2_loss
+    rng = np.random.default_rng(4242)
+    N, B = 128, 128
+    om = O.random_mesh(rng, N, "clements", "mzi", 0.02)
+    m = gpu_mesh(om)
+    x = torch.tensor(O.unit_columns(rng, N, B), dtype=torch.complex64, device="cuda")
+    t = torch.tensor(O.unit_columns(rng, N, B), dtype=torch.complex64, device="cuda")
+    grads = []
+    for fused in (True, False):
+        xd = x.clone().requires_grad_(True)
+        pd = torch.tensor(om.p, dtype=torch.float32, device="cuda", requires_grad=True)
+        J = mesh_l2_loss(m, xd, t, pd) if fused else torch.view_as_real(mesh_apply(m, xd, pd) - t).square().sum()
+        J.backward()
+        grads.append((J.detach(), pd.grad, xd.grad))
+    for a, b in zip(*grads):
+        assert torch.equal(a, b)
+
+
 @pytest.mark.parametrize("pos", ["out", "in"])
 def test_autograd_with_phase_screen(pos):
     """mesh_apply on a mesh with a phase screen: the screen phases get their gradient too."""
@@ -173,11 +222,12 @@ def test_unitary_fitting_training_loop():
     assert abs(loss_ref - loss_end) < 1e-4 * loss_ref
 
 
-@pytest.mark.parametrize("geo,N,B", [("clements", 32, 16), ("fft", 64, 24)])
-def test_graphed_training_step_matches_eager(geo, N, B):
+@pytest.mark.parametrize("geo,N,B,fused", [("clements", 32, 16, False), ("fft", 64, 24, False), ("clements", 64, 32, True)])
+def test_graphed_training_step_matches_eager(geo, N, B, fused):
     """A training step captured in a CUDA graph (GraphedStep) and replayed follows the eager steps
-    exactly: same losses, bitwise the same phases after 3 warm-up and 12 replayed steps."""
-    from meshes_gb300.autograd import GraphedStep, mesh_apply
+    exactly: same losses, bitwise the same phases after 3 warm-up and 12 replayed steps.  fused: the
+    step uses mesh_l2_loss and torch's single-tensor Adam (as the unitary-fitting benchmark does)."""
+    from meshes_gb300.autograd import GraphedStep, mesh_apply, mesh_l2_loss
     rng = np.random.default_rng(2024 + N)
     om = O.random_mesh(rng, N, geo, "mzi", 0.02)
     m = gpu_mesh(om)
@@ -186,11 +236,14 @@ def test_graphed_training_step_matches_eager(geo, N, B):
 
     def trainer():
         p = torch.tensor(om.p, dtype=torch.float32, device="cuda", requires_grad=True)
-        opt = torch.optim.Adam([p], lr=1e-2, capturable=True)
+        opt = torch.optim.Adam([p], lr=1e-2, capturable=True, foreach=not fused)
 
         def step():
             opt.zero_grad(set_to_none=True)
-            loss = ((mesh_apply(m, x, p) - target).abs() ** 2).sum()
+            if fused:
+                loss = mesh_l2_loss(m, x, target, p)
+            else:
+                loss = ((mesh_apply(m, x, p) - target).abs() ** 2).sum()
             loss.backward()
             opt.step()
             return loss

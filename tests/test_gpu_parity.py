@@ -534,6 +534,48 @@ def test_conjugated_and_negated_views():
 
 
 @pytest.mark.parametrize("geo", ["clements", "reck"])
+@pytest.mark.parametrize("N,V,W", [(128, 1, 4), (128, 2, 4), (96, 1, 1), (112, 2, 2)])
+def test_small_mesh_backprop_tiles(geo, N, V, W):
+    """The small-mesh nearest-neighbour back-propagation tiles (4 modes and 1 or 2 vectors per lane, a vector over
+    the whole warp) with the fused L2 gradient, on ragged batches, against the complex128 adjoint; the plan reports
+    the requested tile."""
+    from meshes_gb300 import _lib
+    import ctypes
+    lib = _lib.load()
+    rng = np.random.default_rng(N * 5 + V * 3 + W)
+    for sig, B in ((0.0, 128), (0.02, 77)):
+        om = O.random_mesh(rng, N, geo, "mzi", sig)
+        x = O.unit_columns(rng, N, B)
+        t = O.unit_columns(rng, N, B)
+        m = gpu_mesh(om)
+        xd = torch.tensor(x, dtype=torch.complex64, device="cuda")
+        td = torch.tensor(t, dtype=torch.complex64, device="cuda")
+        y, gx = torch.empty_like(xd), torch.empty_like(xd)
+        dp = torch.empty(m.p_phase.numel(), device="cuda")
+        st = torch.cuda.current_stream().cuda_stream
+        s = m.p_splitter
+        cfg = _lib.config(4, V, W, 0, 0, 2)
+        info = _lib.mg_plan_info()
+        assert lib.mg_plan(2, N, om.L, B, m.crossing, 0, _lib.cfg_ptr(cfg), ctypes.byref(info)) == 0, _lib.last_error()
+        assert (info.M, info.V, info.G) == (4, V, 32)
+        ws = torch.zeros(info.total, dtype=torch.uint8, device="cuda")
+        assert lib.mg_build_tiles(2, N, om.L, 0, m.lens.data_ptr(), m.shifts.data_ptr(), None, m.crossing,
+                                  m.p_phase.data_ptr(), N, s.data_ptr() if s.numel() else None, N, None, None, None,
+                                  B, _lib.cfg_ptr(cfg), ws.data_ptr(), info.total, st) == 0, _lib.last_error()
+        assert lib.mg_propagate(3, N, om.L, B, m.crossing, 0, xd.data_ptr(), None, y.data_ptr(), None, N, None, 0, 0,
+                                _lib.cfg_ptr(cfg), ws.data_ptr(), info.total, st) == 0, _lib.last_error()
+        assert lib.mg_propagate_l2(N, om.L, B, m.crossing, 0, y.data_ptr(), td.data_ptr(), None, gx.data_ptr(), N,
+                                   dp.data_ptr(), N, 0, _lib.cfg_ptr(cfg), ws.data_ptr(), info.total, st) == 0, \
+            _lib.last_error()
+        assert lib.mg_read_status(ws.data_ptr(), 0, st) == 0
+        y_ref = O.propagate(om, x)
+        G, _, gin = O.vjp_unitary(om, y_ref, 2 * (y_ref - t))
+        assert O.rel_err(y.cpu().numpy(), y_ref) < TOL
+        assert O.rel_err(gx.cpu().numpy(), gin) < TOL
+        assert O.rel_err(dp.cpu().numpy().reshape(om.L, N // 2, 2), O.contract_dp(om, G)) < TOL
+
+
+@pytest.mark.parametrize("geo", ["clements", "reck"])
 @pytest.mark.parametrize("N,M,V", [(64, 2, 1), (64, 2, 2), (64, 2, 4), (40, 2, 2), (128, 4, 1), (96, 4, 2)])
 def test_small_mesh_forward_tiles(geo, N, M, V):
     """The small-mesh nearest-neighbour forward tiles (2 or 4 modes and 1 to 4 vectors per lane, a vector over the
