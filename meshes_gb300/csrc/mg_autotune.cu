@@ -135,6 +135,9 @@ extern "C" int mg_autotune(int op, int N, int L, int B, int crossing, int geomet
     const mg_config c1 = done[w1];
     for (int CL : {0, 4, 8, 16})
       for (int S : {2, 3}) measure(mg_config{c1.M, c1.V, c1.W, CL, S, 2});
+    // every layer resident at once, in 1, 2 or 4 stages (no stage reused; shapes whose tiles do not fit are
+    // not valid configurations and are skipped)
+    for (int S : {1, 2, 4}) measure(mg_config{c1.M, c1.V, c1.W, (L + S - 1) / S, S, 2});
     if (op == MG_OP_FWD && c1.V >= 2)
       for (int CL : {0, 4, 6, 8, 12})
         for (int S : {2, 3}) measure(mg_config{c1.M, c1.V, 4, CL, S, 1});
