@@ -704,10 +704,36 @@ __device__ __forceinline__ void chunk_reduce(const PropArgs& a, const int* kinds
 }
 
 // ---- chunk-end reduction of the direct modes: sum the W warps' (dJ/dth, dJ/dph) per slot
-template <int M, int GR>
+// (nearest-neighbour kernels: every slot stays in place, so two slots go per 16-byte load; the sums run in the
+// same warp order, so the results are bitwise those of the general form)
+template <int M, int GR, bool NN = false>
 __device__ __forceinline__ void chunk_reduce_direct(const PropArgs& a, const int* kinds, int lo, int nl,
                                                     const unsigned char* gst, int np2, int G) {
   const size_t gst_layer = (size_t)np2 * 8;
+  if constexpr (NN) {
+    const int half = np2 >> 1;
+    if ((half & (half - 1)) == 0) {
+      const int lg = __ffs(half) - 1;
+      for (int idx = threadIdx.x; idx < (nl << lg); idx += blockDim.x) {
+        const int li = idx >> lg, q = idx & (half - 1);
+        float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 8
+        for (int w = 0; w < a.W; ++w) {
+          const float4 v = reinterpret_cast<const float4*>(gst + ((size_t)w * a.CL + li) * gst_layer)[q];
+          t.x += v.x;
+          t.y += v.y;
+          t.z += v.z;
+          t.w += v.w;
+        }
+        if constexpr (GR == 2) {
+          t.x *= 0.5f;
+          t.z *= 0.5f;
+        }
+        reinterpret_cast<float4*>(a.partial + (size_t)(lo + li) * np2)[q] = t;
+      }
+      return;
+    }
+  }
   for (int idx = threadIdx.x; idx < nl * np2; idx += blockDim.x) {
     const int li = idx / np2, pos = idx - li * np2;
     const int l = lo + li;
@@ -966,7 +992,7 @@ __device__ __forceinline__ void prop_body(const PropArgs& a, unsigned char* smem
                                  a.vend, a.N, a.ldu, j);
     }
     __syncthreads();
-    if constexpr (OP == OP_BWD && kDirect) chunk_reduce_direct<M, GR>(a, kinds, lo, hi - lo, gst, np2, G);
+    if constexpr (OP == OP_BWD && kDirect) chunk_reduce_direct<M, GR, NN>(a, kinds, lo, hi - lo, gst, np2, G);
     if constexpr (OP == OP_BWD && GR == 4) chunk_reduce_raw<M>(a, kinds, lo, hi - lo, gst, np2, G);
     if constexpr (kDT) {
       const bool okd = mbar_wait_bounded(smem_u32(bars + a.S), (uint32_t)(c & 1), wlim);
