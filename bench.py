@@ -1167,14 +1167,14 @@ def run_unitary_fit(args, peak):
     """Unitary fitting: Clements mzi N=128 L=128 with splitting errors N(0, 0.02), target a Haar-random
     unitary (QR of a complex Gaussian with the R-diagonal phase fix), x = I, J = ||U - U_t||_F^2,
     2000 Adam steps (lr 1e-2) on theta, phi through the autograd function (mesh_l2_loss: the loss gradient
-    is formed inside the back-propagation kernel; torch's Adam in its single-tensor form, which measured
-    faster on this one-tensor problem than the multi-tensor and fused forms); steps/s and the fidelity
+    is formed inside the back-propagation kernel; the library's Adam, one fused launch per step, with torch's
+    single-tensor Adam timed beside it); steps/s and the fidelity
     |tr(U^H U_t)|^2 / N^2 of the fitted phases re-evaluated in complex128.  The headline runs the step as a
     CUDA graph (GraphedStep: captured once, replayed); the same 2000 steps run eagerly beside it, from the same
     start, with the same device-side Adam, and must end at the same phases."""
     import torch
     from meshes_gb300 import MeshNetworkGPU
-    from meshes_gb300.autograd import GraphedStep, mesh_apply, mesh_l2_loss
+    from meshes_gb300.autograd import Adam, GraphedStep, mesh_apply, mesh_l2_loss
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     rng = np.random.default_rng(1004)
@@ -1194,9 +1194,10 @@ def run_unitary_fit(args, peak):
     n_steps = 2000
     n_mzi = int(mask.sum())
 
-    def trainer():
+    def trainer(torch_adam=False):
         p = torch.tensor(p0, device=dev, requires_grad=True)
-        opt = torch.optim.Adam([p], lr=1e-2, capturable=True, foreach=False)
+        opt = (torch.optim.Adam([p], lr=1e-2, capturable=True, foreach=False) if torch_adam
+               else Adam([p], lr=1e-2))
 
         def step():
             opt.zero_grad(set_to_none=True)
@@ -1226,6 +1227,15 @@ def run_unitary_fit(args, peak):
             loss = graphed()
         torch.cuda.synchronize()
         t = (time.perf_counter() - t0) / (n_steps - warm)
+        # the same graphed fit with torch's Adam (single-tensor form, state on the device)
+        _, step_t = trainer(torch_adam=True)
+        graphed_t = GraphedStep(step_t, warmup=warm)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(n_steps - warm):
+            loss_t = graphed_t()
+        torch.cuda.synchronize()
+        t_torch = (time.perf_counter() - t0) / (n_steps - warm)
     with torch.no_grad():
         U = mesh_apply(m, x, p).t().to(torch.complex128)
         fid = float(torch.abs(torch.trace(U.conj().t() @ torch.tensor(Ut, dtype=torch.complex128, device=dev))) ** 2
@@ -1237,6 +1247,10 @@ def run_unitary_fit(args, peak):
             "fidelity_complex128": fid128,
             "rel_err": {"U": err_U, "fidelity_abs_diff": abs(fid - fid128), "tolerance": TOL, "ok": bool(err_U <= TOL),
                         "against": "the fitted phases re-evaluated by the complex128 port of c/dot.cpp"},
+            "optimizer": "meshes_gb300.autograd.Adam (mg_adam_step: one launch per step, state on the device)",
+            "torch_adam": {"steps_per_s": 1.0 / t_torch, "ms_per_step": t_torch * 1e3,
+                           "loss_last": float(loss_t.detach()),
+                           "optimizer": "torch.optim.Adam(capturable=True, foreach=False), the same graphed step"},
             "eager": {"steps_per_s": 1.0 / t_eager, "ms_per_step": t_eager * 1e3,
                       "loss_last": float(loss_e.detach()), "same_phases": bool(torch.equal(p.detach(), p_e.detach()))},
             "roofline": roofline_fp32(n_mzi * nc * (FLOP_FWD + FLOP_BWD) / t, peak,

@@ -373,6 +373,17 @@ int mg_diag_configure(int N, int K, void* U, void* Z, void* VdV, void* WWd, int 
 int mg_direct_configure(int N, int L, const int* lens, const int* shifts, const void* U, const double* s, double* p,
                         double* phi_out, int dk_max);
 
+/* ---- training ------------------------------------------------------------------------------- */
+
+/* One Adam step (Kingma and Ba 2015, with bias correction) over n float32 parameters p with gradient g and
+ * moments m, v (device arrays, updated in place), in one launch on `stream`.  state is a device int[2], zeroed
+ * before the first step: state[0] counts the steps taken (the kernel advances it), state[1] is the kernel's own
+ * block counter.  lr, the betas, their complements 1 - beta and eps enter the float arithmetic rounded from
+ * double.  The step count on the device lets a CUDA graph record the update.  No counterpart in the
+ * reference, whose training loops use an external optimizer. */
+int mg_adam_step(float* p, const float* g, float* m, float* v, int n, double lr, double beta1, double beta2, double eps,
+                 int* state, void* stream);
+
 /* ---- measurement helpers -------------------------------------------------------------------- */
 
 /* FP32 FMA throughput probe: `blocks` x `threads` threads each run `iters` iterations of 64

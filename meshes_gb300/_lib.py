@@ -8,7 +8,7 @@ from __future__ import annotations
 import ctypes
 import os
 import threading
-from ctypes import POINTER, Structure, c_char_p, c_float, c_int, c_size_t, c_uint, c_ulonglong, c_void_p
+from ctypes import POINTER, Structure, c_char_p, c_double, c_float, c_int, c_size_t, c_uint, c_ulonglong, c_void_p
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libmeshes_gb300.so")
@@ -118,6 +118,8 @@ _SIGS = {
     "mg_diag_configure": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_int,
                                   c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_int]),
     "mg_direct_configure": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int]),
+    "mg_adam_step": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_double, c_double, c_double, c_double,
+                             c_void_p, c_void_p]),
     "mg_fma_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
     "mg_fma2_probe": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p]),
     "mg_trig_check": (c_int, [c_void_p, c_void_p, c_int, c_void_p]),

@@ -199,6 +199,41 @@ def mesh_apply(mesh: MeshNetworkGPU, x: torch.Tensor, p: Optional[torch.Tensor] 
     return MeshFunction.apply(x, p, mesh) * d
 
 
+class Adam:
+    """Adam (Kingma and Ba 2015, with bias correction) over float32 CUDA tensors, one fused launch per tensor
+    (mg_adam_step).  The update of ``torch.optim.Adam(params, lr, betas, eps)`` without weight decay or amsgrad:
+    each parameter, gradient and moment is read and written once per step instead of in a dozen elementwise
+    passes.  Moments and the step count stay on the device, so ``GraphedStep`` can capture ``step()``."""
+
+    def __init__(self, params, lr: float = 1e-3, betas=(0.9, 0.999), eps: float = 1e-8):
+        self.params = list(params)
+        for p in self.params:
+            if p.dtype != torch.float32 or not p.is_cuda or not p.is_contiguous():
+                raise ValueError("Adam takes contiguous float32 CUDA tensors")
+        self.lr, self.betas, self.eps = float(lr), (float(betas[0]), float(betas[1])), float(eps)
+        self.exp_avg = [torch.zeros_like(p) for p in self.params]
+        self.exp_avg_sq = [torch.zeros_like(p) for p in self.params]
+        self.state = [torch.zeros(2, dtype=torch.int32, device=p.device) for p in self.params]   # steps, counter
+
+    def zero_grad(self, set_to_none: bool = True):
+        for p in self.params:
+            if set_to_none:
+                p.grad = None
+            elif p.grad is not None:
+                p.grad.zero_()
+
+    @torch.no_grad()
+    def step(self):
+        lib = load()
+        for p, m, v, s in zip(self.params, self.exp_avg, self.exp_avg_sq, self.state):
+            if p.grad is None:
+                continue
+            g = p.grad.to(torch.float32).contiguous()
+            check(lib.mg_adam_step(p.data_ptr(), g.data_ptr(), m.data_ptr(), v.data_ptr(), p.numel(), self.lr,
+                                   self.betas[0], self.betas[1], self.eps, s.data_ptr(), _stream(p.device)),
+                  "mg_adam_step")
+
+
 class GraphedStep:
     """A training step captured once in a CUDA graph and replayed.
 

@@ -96,6 +96,30 @@ def test_l2_loss_equals_mesh_apply_form():
         assert torch.equal(a, b)
 
 
+def test_fused_adam_matches_torch_adam():
+    """autograd.Adam (one mg_adam_step launch per tensor) against torch.optim.Adam on the same 30 seeded
+    gradients: parameters and both moments within float32 rounding (1e-5 absolute on parameters in [0, 2 pi], a
+    thousandth of one lr = 1e-2 step; 1e-5 relative on the moments); the device step count advances by one per
+    step."""
+    from meshes_gb300.autograd import Adam
+    rng = np.random.default_rng(77)
+    p0 = rng.uniform(0, 2 * np.pi, (65, 32, 2)).astype(np.float32)
+    pa = torch.tensor(p0, device="cuda", requires_grad=True)
+    pt = torch.tensor(p0, device="cuda", requires_grad=True)
+    oa = Adam([pa], lr=1e-2, betas=(0.9, 0.999), eps=1e-8)
+    ot = torch.optim.Adam([pt], lr=1e-2, betas=(0.9, 0.999), eps=1e-8, foreach=False)
+    for k in range(30):
+        g = torch.tensor(rng.standard_normal(p0.shape).astype(np.float32) * (10.0 ** rng.uniform(-3, 1)), device="cuda")
+        pa.grad, pt.grad = g.clone(), g.clone()
+        oa.step()
+        ot.step()
+        assert float((pa - pt).abs().max()) < 1e-5, k
+    st = ot.state[pt]
+    assert float((oa.exp_avg[0] - st["exp_avg"]).abs().max()) <= 1e-5 * float(st["exp_avg"].abs().max())
+    assert float((oa.exp_avg_sq[0] - st["exp_avg_sq"]).abs().max()) <= 1e-5 * float(st["exp_avg_sq"].abs().max())
+    assert oa.state[0].tolist() == [30, 0]
+
+
 @pytest.mark.parametrize("pos", ["out", "in"])
 def test_autograd_with_phase_screen(pos):
     """mesh_apply on a mesh with a phase screen: the screen phases get their gradient too."""
@@ -226,8 +250,8 @@ def test_unitary_fitting_training_loop():
 def test_graphed_training_step_matches_eager(geo, N, B, fused):
     """A training step captured in a CUDA graph (GraphedStep) and replayed follows the eager steps
     exactly: same losses, bitwise the same phases after 3 warm-up and 12 replayed steps.  fused: the
-    step uses mesh_l2_loss and torch's single-tensor Adam (as the unitary-fitting benchmark does)."""
-    from meshes_gb300.autograd import GraphedStep, mesh_apply, mesh_l2_loss
+    step uses mesh_l2_loss and the library's fused Adam (as the unitary-fitting benchmark does)."""
+    from meshes_gb300.autograd import Adam, GraphedStep, mesh_apply, mesh_l2_loss
     rng = np.random.default_rng(2024 + N)
     om = O.random_mesh(rng, N, geo, "mzi", 0.02)
     m = gpu_mesh(om)
@@ -236,7 +260,7 @@ def test_graphed_training_step_matches_eager(geo, N, B, fused):
 
     def trainer():
         p = torch.tensor(om.p, dtype=torch.float32, device="cuda", requires_grad=True)
-        opt = torch.optim.Adam([p], lr=1e-2, capturable=True, foreach=not fused)
+        opt = Adam([p], lr=1e-2) if fused else torch.optim.Adam([p], lr=1e-2, capturable=True)
 
         def step():
             opt.zero_grad(set_to_none=True)

@@ -351,6 +351,29 @@ def test_header_symbols_exported():
     assert lib.mg_version().decode().startswith("meshes_gb300")
 
 
+def test_adam_step_rejects_bad_arguments():
+    """mg_adam_step checks its arguments before it launches anything (no GPU needed): a negative size, a
+    learning rate or betas out of range, a missing pointer."""
+    from meshes_gb300 import _lib
+    from meshes_gb300.build import build
+    build()
+    lib = _lib.load()
+    ok = dict(p=8, g=8, m=8, v=8, n=4, lr=1e-2, b1=0.9, b2=0.999, eps=1e-8, state=8)
+
+    def call(**kw):
+        a = dict(ok, **kw)
+        return lib.mg_adam_step(a["p"], a["g"], a["m"], a["v"], a["n"], a["lr"], a["b1"], a["b2"], a["eps"],
+                                a["state"], None)
+    assert call(n=-1) == -1
+    assert call(lr=-1.0) == -1
+    assert call(b1=1.0) == -1
+    assert call(b2=-0.5) == -1
+    assert call(eps=float("nan")) == -1
+    assert call(p=None) == -1
+    assert call(state=None) == -1
+    assert call(n=0, p=None, g=None, m=None, v=None, state=None) == 0
+
+
 def test_tuning_table_entries_are_valid_plans():
     """Every configuration in the committed tuning table plans (mg_plan: host-side arithmetic only) at both
     ends of its batch range, with the register tile it names; planning needs no GPU."""
