@@ -68,7 +68,7 @@ def test_l2_loss_matches_oracle(geo, cr, N, B):
     y_ref = O.propagate(om, x)
     J_ref = float(np.sum(np.abs(y_ref - t) ** 2))
     G, _, gin = O.vjp_unitary(om, y_ref, 2 * (y_ref - t))
-    assert abs(float(J) - J_ref) < 1e-5 * J_ref
+    assert abs(float(J.detach()) - J_ref) < 1e-5 * J_ref
     assert O.rel_err(pd.grad.cpu().numpy(), 0.5 * O.contract_dp(om, G)) < 1e-5
     assert O.rel_err(xd.grad.cpu().numpy(), 0.5 * gin) < 1e-5
     assert O.rel_err(td.grad.cpu().numpy(), -(y_ref - t)) < 1e-5
@@ -274,10 +274,10 @@ def test_graphed_training_step_matches_eager(geo, N, B, fused):
         return p, step
 
     p_e, step_e = trainer()
-    eager = [float(step_e()) for _ in range(15)]
+    eager = [float(step_e().detach()) for _ in range(15)]
     p_g, step_g = trainer()
     g = GraphedStep(step_g, warmup=3)
-    graphed = [float(g()) for _ in range(12)]
+    graphed = [float(g().detach()) for _ in range(12)]
     assert graphed == eager[3:]
     assert torch.equal(p_g.detach(), p_e.detach())
     assert eager[-1] < eager[0]
