@@ -374,6 +374,15 @@ def test_adam_step_rejects_bad_arguments():
     assert call(n=0, p=None, g=None, m=None, v=None, state=None) == 0
 
 
+def test_adam_wrapper_rejects_unsupported_tensors():
+    """autograd.Adam takes contiguous float32 CUDA tensors only, and says so before anything touches a GPU."""
+    import torch
+    from meshes_gb300.autograd import Adam
+    for bad in (torch.zeros(4), torch.zeros(4, dtype=torch.float64), torch.zeros(4, 2).t()):
+        with pytest.raises(ValueError):
+            Adam([bad])
+
+
 def test_tuning_table_entries_are_valid_plans():
     """Every configuration in the committed tuning table plans (mg_plan: host-side arithmetic only) at both
     ends of its batch range, with the register tile it names; planning needs no GPU."""
